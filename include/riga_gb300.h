@@ -1,0 +1,329 @@
+/*
+ * riga_gb300.h — C ABI of the GB300 Monte Carlo engine for riga-flow's scenario hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and POD structs, and returns an
+ * int32 status (0 = success).  A non-zero status maps 1:1 onto the reference's
+ * `RigaError { code, message }` (crates/riga-core/src/lib.rs:5-19): `rg_status_code()` gives the
+ * stable `code` string, `rg_last_error()` the thread's last `message`.  No C++ exception crosses
+ * this boundary and there is no CPU fallback: without a usable sm_103a device every compute entry
+ * point fails with RG_ERR_GPU_UNAVAILABLE ("gpu_unavailable"), as the reference's `gpu` build does
+ * (crates/riga-engine/src/lib.rs:188-202, crates/riga-engine/src/gpu.rs:490-512).
+ *
+ * Structs mirror the reference's serde types field by field.  `Option<T>` fields become a
+ * `has_<field>` flag plus the value.  Asset arrays are length `n_assets`; the reference accepts
+ * exactly two assets (crates/riga-engine/src/lib.rs:234-245) and this engine accepts
+ * 1..RG_MAX_ASSETS, reducing exactly to the reference at two.
+ */
+#ifndef RIGA_GB300_H
+#define RIGA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_ABI_VERSION 1
+#define RG_MAX_ASSETS 5
+#define RG_TRACE_EVENT_CAP 64 /* crates/riga-engine/src/note.rs:57 */
+#define RG_N_TRANSITIONS 3    /* daily_global_ko, final_fixing_eki, memory_coupon */
+
+/* ------------------------------------------------------------------ status codes -------------- */
+/* Stable error codes; the strings returned by rg_status_code() are the reference's RigaError.code
+ * values (crates/riga-engine/src/lib.rs:209-321, gpu.rs:78-80,143-144,173-176,
+ * crates/riga-risk/src/lib.rs:338-457). */
+enum {
+  RG_OK = 0,
+  RG_ERR_MISSING_AS_OF = 1,          /* "missing_as_of" */
+  RG_ERR_AS_OF_MISMATCH = 2,         /* "as_of_mismatch" */
+  RG_ERR_INVALID_PATHS = 3,          /* "invalid_paths" */
+  RG_ERR_INVALID_SCHEDULE = 4,       /* "invalid_schedule" */
+  RG_ERR_INVALID_MARKET_SHAPE = 5,   /* "invalid_market_shape" */
+  RG_ERR_INVALID_MARKET = 6,         /* "invalid_market" */
+  RG_ERR_INVALID_TRADE = 7,          /* "invalid_trade" */
+  RG_ERR_INVALID_LOCAL_VOL = 8,      /* "invalid_local_vol" */
+  RG_ERR_SHAPE_MISMATCH = 9,         /* "shape_mismatch" */
+  RG_ERR_GPU_UNAVAILABLE = 10,       /* "gpu_unavailable" */
+  RG_ERR_GPU_ERROR = 11,             /* "gpu_error" */
+  RG_ERR_NO_CRN_REJECTED = 12,       /* "no_crn_rejected" */
+  RG_ERR_INVALID_SPOT_BUMP = 13,     /* "invalid_spot_bump" */
+  RG_ERR_INVALID_VOLATILITY_BUMP = 14, /* "invalid_volatility_bump" */
+  RG_ERR_INVALID_RATE_BUMP = 15,     /* "invalid_rate_bump" */
+  RG_ERR_INVALID_CORRELATION_BUMP = 16, /* "invalid_correlation_bump" */
+  RG_ERR_RISK_INPUT_SHAPE = 17,      /* "risk_input_shape" */
+  RG_ERR_RISK_PATHS_REQUIRED = 18,   /* "risk_paths_required" */
+  RG_ERR_PATH_OUT_OF_RANGE = 19,     /* "path_out_of_range" */
+  RG_ERR_INVALID_ARGUMENT = 20,      /* "invalid_argument" (null pointer, bad enum, size limit) */
+  RG_ERR_UNSUPPORTED = 21,           /* "unsupported" (a lane this engine does not run) */
+  RG_ERR_INVALID_PERCENTILE = 22,    /* "invalid_percentile" */
+  RG_ERR_CANCELLED = 23,             /* "cancelled" */
+  RG_ERR_TIMEOUT = 24                /* "device_timeout": a bounded device wait expired */
+};
+
+/* ------------------------------------------------------------------ enums --------------------- */
+/* TraceLevel, crates/riga-core/src/lib.rs:21-28 */
+enum { RG_TRACE_OFF = 0, RG_TRACE_AGGREGATED = 1, RG_TRACE_SAMPLED = 2, RG_TRACE_FULL = 3 };
+/* VarianceReduction, crates/riga-core/src/lib.rs:88-106 */
+enum { RG_VR_NONE = 0, RG_VR_HALTON = 1, RG_VR_SOBOL = 2 };
+/* Engine knobs that the reference does not have.  The defaults (all zero) reproduce the
+ * reference: Owen scrambling (qmc.rs:292-308), FP64 arithmetic, dimension clamp+wrap at 512
+ * (qmc.rs:9,249,271), the 96-point Dupire log-strike axis (riga-market/src/lib.rs:28). */
+enum { RG_SCRAMBLE_OWEN = 0, RG_SCRAMBLE_DIGITAL_SHIFT = 1 };
+enum { RG_PRECISION_FP64_PARITY = 0, RG_PRECISION_FP32 = 1 };
+enum { RG_DIM_WRAP_REFERENCE = 0, RG_DIM_FULL = 1 };
+
+/* ------------------------------------------------------------------ request types ------------- */
+/* PhoenixTrade, crates/riga-core/src/lib.rs:57-75 */
+typedef struct rg_phoenix_trade {
+  const char* trade_id;
+  int32_t n_assets;
+  const double* initial_spots; /* [n_assets] */
+  double maturity_years;
+  int64_t steps;
+  double strike;
+  double knock_in_barrier;
+  int32_t has_knock_out_barrier;
+  double knock_out_barrier;
+  int32_t has_coupon_barrier;
+  double coupon_barrier;
+  int32_t has_coupon_rate;
+  double coupon_rate;
+  int32_t memory_coupon;
+  int32_t has_coupon_periods;
+  int64_t coupon_periods;
+  int32_t fixed_first_coupon;
+  int32_t has_call_start_step;
+  int64_t call_start_step;
+} rg_phoenix_trade;
+
+/* MarketSnapshot, crates/riga-core/src/lib.rs:37-45 */
+typedef struct rg_market_snapshot {
+  const char* as_of;
+  int32_t n_assets;
+  const double* spots;           /* [n_assets] */
+  const double* vols;            /* [n_assets] */
+  double risk_free_rate;
+  const double* dividend_yields; /* [n_assets] */
+  const double* correlation;     /* [n_assets * n_assets], row-major */
+} rg_market_snapshot;
+
+/* SimulationConfig, crates/riga-core/src/lib.rs:77-86, plus this engine's knobs. */
+typedef struct rg_simulation_config {
+  uint64_t paths;
+  uint64_t path_block_size;
+  uint64_t seed;
+  int32_t trace_level;        /* RG_TRACE_* */
+  int32_t variance_reduction; /* RG_VR_* */
+  uint64_t qmc_dimension;     /* VarianceReduction::{Halton,Sobol}{dimension} */
+  int32_t scrambler;          /* RG_SCRAMBLE_* (Sobol only) */
+  int32_t precision;          /* RG_PRECISION_* */
+  int32_t dim_mode;           /* RG_DIM_* */
+  int32_t lv_grid_x;          /* Dupire log-strike points; 0 = 96 (riga-market/src/lib.rs:28) */
+} rg_simulation_config;
+
+/* ImpliedVolGrid, crates/riga-market/src/lib.rs:83-91 */
+typedef struct rg_implied_vol_grid {
+  int32_t n_maturities;
+  int32_t n_strikes;
+  const double* maturities_years; /* [n_maturities], strictly increasing */
+  const double* strikes;          /* [n_strikes], strictly increasing */
+  const double* vols;             /* [n_maturities * n_strikes], row-major */
+} rg_implied_vol_grid;
+
+/* PriceRequest, crates/riga-engine/src/lib.rs:36-46.  n_local_vol == 0 is `local_vol: None`. */
+typedef struct rg_price_request {
+  rg_phoenix_trade trade;
+  rg_market_snapshot market;
+  rg_simulation_config config;
+  const char* as_of;
+  int32_t n_local_vol;
+  const rg_implied_vol_grid* local_vol; /* [n_local_vol] */
+} rg_price_request;
+
+/* ------------------------------------------------------------------ result types -------------- */
+/* LegAttribution, crates/riga-core/src/lib.rs:209-217 */
+typedef struct rg_leg_attribution {
+  double par_redemption, coupon, memory_coupon, down_and_in_put, funding, discounting, total;
+} rg_leg_attribution;
+
+/* TransitionStats, crates/riga-core/src/lib.rs:219-229 (transition_id implied by the index:
+ * 0 daily_global_ko, 1 final_fixing_eki, 2 memory_coupon; note.rs:277-308) */
+typedef struct rg_transition_stats {
+  uint64_t input_count, output_count;
+  double probability, mean_payoff, variance_payoff, mean_delta, mean_vega;
+} rg_transition_stats;
+
+/* LedgerEntry numeric fields, crates/riga-core/src/lib.rs:231-241 (note.rs:314-354); the
+ * condition and evidence strings are formatted by the caller from the request. */
+typedef struct rg_ledger_entry {
+  uint64_t population_before, population_after;
+  double pv_impact, delta_impact, vega_impact;
+} rg_ledger_entry;
+
+/* One `daily_global_ko:path={path_id}:t={time:.6}` trace event (note.rs:174-180). */
+typedef struct rg_trace_event {
+  uint64_t path_id;
+  double time;
+} rg_trace_event;
+
+/* PriceResult, crates/riga-core/src/lib.rs:243-255 */
+typedef struct rg_price_result {
+  double pv, mc_error, ki_probability;
+  rg_leg_attribution legs;
+  rg_transition_stats stats[RG_N_TRANSITIONS];
+  rg_ledger_entry ledger[RG_N_TRANSITIONS];
+  uint64_t seed;
+  uint64_t ko_count, ki_count, put_eligible_count, coupon_path_count;
+  int32_t n_trace_events;
+  rg_trace_event trace_events[RG_TRACE_EVENT_CAP];
+} rg_price_result;
+
+/* One scenario of a common-random-number batch: a complete market plus an optional parallel
+ * implied-vol shift per asset (sticky strike, crates/riga-risk/src/lib.rs:260-279).  Every
+ * scenario of a batch reuses the request's seed, trade and simulation config. */
+typedef struct rg_scenario {
+  rg_market_snapshot market;
+  const double* implied_vol_shift; /* [n_assets] or NULL */
+} rg_scenario;
+
+/* CentralDifferenceConfig, crates/riga-risk/src/lib.rs:24-49 */
+enum { RG_CRN = 0, RG_NO_CRN = 1 };
+typedef struct rg_central_difference_config {
+  double spot_relative_bump;
+  double volatility_absolute_bump;
+  double rate_absolute_bump;
+  double correlation_absolute_bump;
+  int32_t random_number_policy; /* RG_CRN; RG_NO_CRN is rejected */
+} rg_central_difference_config;
+
+/* FiniteDifferenceEstimate, crates/riga-risk/src/lib.rs:63-72 */
+typedef struct rg_fd_estimate {
+  double value, mc_error_upper_bound;
+} rg_fd_estimate;
+
+/* AssetGreeks + BatchAssetGreeks, crates/riga-risk/src/lib.rs:74-94, 468-476 */
+typedef struct rg_asset_greeks {
+  int32_t asset_index;
+  double spot_bump, volatility_bump;
+  rg_fd_estimate delta, gamma, vega;
+  double spot_up_pv, spot_down_pv, vol_up_pv, vol_down_pv;
+  double spot_up_mc_error, spot_down_mc_error, vol_up_mc_error, vol_down_mc_error;
+} rg_asset_greeks;
+
+/* TransitionRisk, crates/riga-risk/src/lib.rs:478-493 (index as in rg_transition_stats) */
+typedef struct rg_transition_risk {
+  double pv_impact, delta_impact, vega_impact;
+} rg_transition_risk;
+
+/* BatchRiskReport, crates/riga-risk/src/lib.rs:495-516.  `base` is the full base-case result. */
+typedef struct rg_batch_risk_report {
+  rg_price_result base;
+  uint64_t scenario_count;
+  uint64_t seed;
+  int32_t n_assets;
+  rg_asset_greeks assets[RG_MAX_ASSETS];
+  rg_transition_risk transitions[RG_N_TRANSITIONS];
+  double rate_up_pv, rate_down_pv, correlation_up_pv, correlation_down_pv;
+  double rate_bump, correlation_bump, pv_mc_error;
+} rg_batch_risk_report;
+
+/* PathRecord scalar fields, crates/riga-engine/src/explain.rs:57-74 */
+typedef struct rg_path_record {
+  uint64_t path_id, rng_seed, sobol_index;
+  double worst_final;
+  int32_t knocked_out;
+  int32_t ko_step;      /* -1 when the path never knocked out */
+  double ko_time;       /* NaN when the path never knocked out */
+  int32_t ki_hit;
+  int32_t qualified_steps; /* qualifying coupon observations while alive (explain.rs:226) */
+  int32_t paid_periods;    /* period ends and KO dates that paid a coupon */
+  double put_payoff, coupon_pv, memory_coupon_pv, funding, pv;
+} rg_path_record;
+
+/* ------------------------------------------------------------------ errors -------------------- */
+/* The RigaError.code string for a status (crates/riga-core/src/lib.rs:5-19). */
+const char* rg_status_code(int32_t status);
+/* Copies the calling thread's last error message (NUL-terminated, truncated to len); returns
+ * the full message length. */
+int32_t rg_last_error(char* buf, size_t len);
+int32_t rg_abi_version(void);
+
+/* ------------------------------------------------------------------ device -------------------- */
+/* gpu::ensure_available, crates/riga-engine/src/gpu.rs:500-503 */
+int32_t rg_ensure_available(void);
+/* gpu::device_name, crates/riga-engine/src/gpu.rs:505-508 */
+int32_t rg_device_name(char* buf, size_t len);
+/* gpu::arch, crates/riga-engine/src/gpu.rs:510-512 ("sm_103" on GB300) */
+int32_t rg_arch(char* buf, size_t len);
+
+/* ------------------------------------------------------------------ engine -------------------- */
+/* An engine owns one CUDA stream, its device workspace and cached tables.  Calls on one engine
+ * are serialised by the engine; separate engines run concurrently.  Replaces the process-wide
+ * `OnceLock<Gpu>` of crates/riga-engine/src/gpu.rs:490-497. */
+typedef struct rg_engine rg_engine;
+int32_t rg_engine_create(int32_t device, rg_engine** out);
+void rg_engine_destroy(rg_engine* engine);
+
+/* riga_engine::price_put_leg, crates/riga-engine/src/lib.rs:183-186 (-> note::price_full_phoenix,
+ * note.rs:38-373).  Runs the fused generation+step+payoff kernel on the device. */
+int32_t rg_price_put_leg(rg_engine* engine, const rg_price_request* request, rg_price_result* out);
+
+/* A CRN scenario batch in one fused launch: out[i] is the request priced under scenarios[i] with
+ * the request's seed (crates/riga-risk/src/lib.rs:253-258; crates/riga-engine/src/dispatch.rs:23-70). */
+int32_t rg_price_scenarios(rg_engine* engine, const rg_price_request* request,
+                           const rg_scenario* scenarios, int32_t n_scenarios,
+                           rg_price_result* out);
+
+/* riga_risk::price_risk_batch, crates/riga-risk/src/lib.rs:573-626 (with the central Greeks of
+ * price_central_greeks, :117-186): base + spot/vol up/down per asset + rate up/down +
+ * correlation up/down, all priced in one CRN launch. */
+int32_t rg_price_risk_batch(rg_engine* engine, const rg_price_request* request,
+                            const rg_central_difference_config* config,
+                            rg_batch_risk_report* out);
+
+/* explain::run_paths restricted to [first_path, first_path + count),
+ * crates/riga-engine/src/explain.rs:90-316 (reconstruct_path :319-333 is count == 1). */
+int32_t rg_run_paths(rg_engine* engine, const rg_price_request* request, uint64_t first_path,
+                     uint64_t count, rg_path_record* out);
+
+/* ------------------------------------------------------------------ gpu backend drop-in ------- */
+/* gpu::worst_of, crates/riga-engine/src/gpu.rs:171-205 / :515-517 (out = min(a, b)). */
+int32_t rg_worst_of(const float* a, const float* b, float* out, int64_t n);
+
+/* gpu::lv_terminal_spots, crates/riga-engine/src/gpu.rs:209-277 / :538-564.  normals
+ * [paths, steps, 2], rows [2, steps, gx], ls_axis [2 * gx], s0/references/dividends [2];
+ * writes terminal spots [paths, 2] and the first autocall step (or -1) [paths]. */
+int32_t rg_lv_terminal_spots(const float* normals, const float* rows, const float* ls_axis,
+                             int64_t gx, const float* s0, const float* references,
+                             float call_barrier, int64_t paths, int64_t steps, float dt,
+                             float rate, const float* dividends, float* out_terminal,
+                             int32_t* out_ko);
+
+/* gpu::resident_lv / ResidentLv::{run, download, synchronize}, crates/riga-engine/src/gpu.rs:
+ * 283-327, 409-488, 525-534: upload the scenario-independent buffers once, re-run per bump. */
+typedef struct rg_resident_lv rg_resident_lv;
+int32_t rg_resident_lv_create(const float* normals, const float* rows, const float* ls_axis,
+                              int64_t gx, int64_t paths, int64_t steps, float dt,
+                              rg_resident_lv** out);
+int32_t rg_resident_lv_run(rg_resident_lv* lv, const float* s0, const float* references,
+                           float call_barrier, float rate, const float* dividends);
+int32_t rg_resident_lv_download(rg_resident_lv* lv, float* out_terminal, int32_t* out_ko);
+int32_t rg_resident_lv_synchronize(rg_resident_lv* lv);
+void rg_resident_lv_destroy(rg_resident_lv* lv);
+
+/* gpu::resident_worst_of / ResidentWorstOf::{reduce, download, synchronize},
+ * crates/riga-engine/src/gpu.rs:362-405. */
+typedef struct rg_resident_worst_of rg_resident_worst_of;
+int32_t rg_resident_worst_of_create(const float* a, const float* b, int64_t n,
+                                    rg_resident_worst_of** out);
+int32_t rg_resident_worst_of_reduce(rg_resident_worst_of* w);
+int32_t rg_resident_worst_of_download(rg_resident_worst_of* w, float* out);
+int32_t rg_resident_worst_of_synchronize(rg_resident_worst_of* w);
+void rg_resident_worst_of_destroy(rg_resident_worst_of* w);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RIGA_GB300_H */
