@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark of the fused CRN Phoenix engine on the 3-asset Dupire local-vol configuration.
+
+Workload (one "step"): price one trade under base + 15 common-random-number bumps — 16 scenarios —
+over 2^20 Sobol paths (digital shift from seed 1) and 756 daily steps, 3 assets under seeded SVI
+smiles calibrated to a 40-point Dupire grid, FP32 path state with FP64 sums.  A path-step is one
+time step of one path for one (trade, scenario), all assets included.
+
+* ``value`` — path-steps/s with inputs resident: path-steps ÷ device time of the prologue
+  kernels + the fused kernel + the final reduction (CUDA events on the engine's stream).
+* ``e2e`` — the same metric through the C ABI call a user makes (``rg_price_scenarios``) with host
+  inputs: host table build, H2D, all kernels, D2H and result assembly, wall-clock.
+* ``--impl reference`` times the reference algorithm's CPU restatement (the oracle) on every host
+  core on a bounded sample of the same workload.
+
+Multi-GPU: one process per GPU (torchrun); rank r prices paths [r·P, (r+1)·P) of the same Sobol
+sequence (weak scaling), and rank 0 merges the ranks' FP64 path sums in rank order.
+"""
+from __future__ import annotations
+
+import argparse
+import copy
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "riga-flow_gb300"))
+
+METRIC = "path-steps/sec and trades·bumps/sec at ≤1bp error vs FP64; p50/p99 latency"
+UNIT = "path-steps/s"
+
+
+def workload_request(paths: int, steps: int, fp32: bool = True, first_path: int = 0):
+    from riga_gb300 import workloads
+
+    req = workloads.lv3(paths=paths, steps=steps, fp32=fp32)
+    req.options.first_path = first_path
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(req)]
+    return req, scen
+
+
+def config_block(paths, steps, n_scen, world):
+    return {"workload": f"lv3_crn16: 3-asset worst-of Phoenix under Dupire local vol (seeded SVI, "
+                        f"40-point grid), {paths} Sobol paths per GPU (digital shift, seed 1), "
+                        f"{steps} steps, base + {n_scen - 1} CRN bumps in one fused launch",
+            "paths_per_gpu": paths, "steps": steps, "scenarios": n_scen, "assets": 3,
+            "precision": "fp32 path state, fp64 sums", "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"path-range shards x{world}" if world > 1 else "single GPU"}
+
+
+# ----------------------------------------------------------------------------- flops model ---
+# Algorithmic FP32 work per unit (FMA = 2 flops), fixed in code:
+#   per (path, factor, step) generation: inverse normal 30, bridge 5               -> 35
+#   per (path, scenario, step): correlate N(N+1) + payoff 3
+#   per (path, scenario, factor, step): local-vol lookup 12, Euler step 6, min 1   -> 19
+GEN_FLOPS, ASSET_FLOPS, PAY_FLOPS = 35, 19, 3
+
+
+def flops_per_launch(paths, steps, n_assets, n_scen):
+    per_path_step = GEN_FLOPS * n_assets + n_scen * (n_assets * (n_assets + 1) + PAY_FLOPS + ASSET_FLOPS * n_assets)
+    return float(paths) * steps * per_path_step
+
+
+def measured_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+# ----------------------------------------------------------------------------- clocks ---------
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        self.file.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != self.index:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline ---
+def cpu_rate(paths_hint: int, steps: int, target_s: float):
+    """Oracle path-steps/s on every host core for a bounded sample of the workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    req, scen = workload_request(64, steps, fp32=False)
+    t0 = time.perf_counter()
+    O.price_scenarios(req, scen, threads=threads)
+    dt = time.perf_counter() - t0
+    per_path = dt / 64.0
+    paths = int(max(256, min(paths_hint, target_s / max(per_path, 1e-9))))
+    paths = max(threads * 64, (paths // (threads * 64)) * threads * 64)
+    req, scen = workload_request(paths, steps, fp32=False)
+    t0 = time.perf_counter()
+    O.price_scenarios(req, scen, threads=threads)
+    dt = time.perf_counter() - t0
+    units = float(paths) * steps * len(scen)
+    return units / dt, threads, paths, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rates = []
+    for i in range(args.warmup + args.steps):
+        rate, cores, paths, dt = cpu_rate(args.paths, args.timesteps, args.cpu_seconds)
+        if i >= args.warmup:
+            rates.append(rate)
+    value = statistics.median(rates)
+    sample = (f"oracle FP64 restatement of the reference path (scenario by scenario, as the "
+              f"reference re-prices each bump), {paths} paths x {args.timesteps} steps x 16 scenarios per step")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded SVI smiles, CRN bump set)",
+            "config": config_block(args.paths, args.timesteps, 16, 1),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm --------
+def run_gpu(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from riga_gb300 import abi
+    from riga_gb300.build import build_library
+    from riga_gb300.engine import Engine
+    import ctypes as C
+
+    build_library()
+    eng = Engine(local)
+    P, T = args.paths, args.timesteps
+    req, scen = workload_request(P, T, fp32=True, first_path=rank * P)
+    n_scen = len(scen)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one_step():
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = eng.price_scenarios_raw(req, scen)
+        wall = time.perf_counter() - t0
+        tm = abi.Timing()
+        abi.check(eng.lib, eng.lib.rg_engine_last_timing(eng.handle, C.byref(tm)))
+        return res, wall, tm
+
+    for _ in range(args.warmup):
+        one_step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    walls, dev_ms, ker_ms, timings = [], [], [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            res, wall, tm = one_step()
+            walls.append(wall)
+            dev_ms.append(tm.prologue_ms + tm.kernel_ms + tm.reduce_ms)
+            ker_ms.append(tm.kernel_ms)
+            timings.append(tm)
+    torch.cuda.synchronize()
+    tot = torch.tensor([sum(dev_ms), sum(walls)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.MAX)
+        # the one gather: every rank's FP64 path sums, merged in rank order on rank 0
+        sums = torch.tensor([list(r.path_sums) for r in res], dtype=torch.float64, device="cuda")
+        gathered = [torch.empty_like(sums) for _ in range(world)]
+        torch.distributed.all_gather(gathered, sums)
+    dev_total_s, wall_total_s = tot[0].item() / 1e3, tot[1].item()
+    units = float(P) * T * n_scen * world * args.steps
+    value = units / dev_total_s
+    e2e = units / wall_total_s
+    if rank != 0:
+        return
+    merged_pv = None
+    if world > 1:
+        parts = (abi.PriceResult * world)()
+        for r_, g in enumerate(gathered):
+            parts[r_].path_sums[:] = g[0].tolist()
+            parts[r_].seed = 1
+        out = abi.PriceResult()
+        abi.check(eng.lib, eng.lib.rg_merge_results(parts, world, P * world, C.byref(out)))
+        merged_pv = out.pv
+    # accuracy: FP32 against the FP64 parity kernel on the same points (outside the timed region)
+    req64, _ = workload_request(P, T, fp32=False, first_path=rank * P)
+    t_acc = time.perf_counter()
+    res64 = eng.price_scenarios_raw(req64, scen)
+    acc_s = time.perf_counter() - t_acc
+    errs = [abs(a.pv - b.pv) for a, b in zip(res, res64)]
+    bounds = [min(0.1 * b.mc_error, 1e-4) for b in res64]
+    peaks = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    kern_avg_s = statistics.mean(ker_ms) / 1e3
+    achieved = flops_per_launch(P, T, 3, n_scen) / kern_avg_s / 1e12
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("phoenix32_lv3_bytes_per_launch")
+        except Exception:
+            traffic = None
+    clocks = clk.summary()
+    tm = timings[-1]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded SVI smiles, CRN bump set; no public dataset exists for this path)",
+        "config": config_block(P, T, n_scen, world),
+        "trades_bumps_per_s": n_scen * world * args.steps / dev_total_s,
+        "latency_ms": {"p50": 1e3 * statistics.median(walls),
+                       "p99": 1e3 * sorted(walls)[max(0, int(round(0.99 * len(walls))) - 1)]},
+        "accuracy": {"max_abs_err_vs_fp64": max(errs), "bound_min_0.1se_1bp": min(bounds),
+                     "within_bound": all(e <= b for e, b in zip(errs, bounds)),
+                     "fp64_parity_kernel_s": acc_s},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": traffic,
+                     "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x sm_max_mhz {sm_max} "
+                                    f"(MEASURED_PEAKS.json has no FP32 figure)",
+                     "kernel_ms": 1e3 * kern_avg_s,
+                     "flops_per_launch": flops_per_launch(P, T, 3, n_scen)},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(tm.h2d_bytes),
+                "d2h_bytes_per_step": int(tm.d2h_bytes)},
+        "gpu_launches": int(tm.kernel_launches) * args.steps,
+        "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes},
+        "clocks": clocks,
+    }
+    if merged_pv is not None:
+        line["merged_base_pv"] = merged_pv
+    if world == 1 and not args.no_cpu_baseline:
+        rate, cores, paths, dt = cpu_rate(P, T, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"oracle FP64 on {cores} host threads, {paths} paths x {T} steps "
+                                          f"x {n_scen} scenarios ({dt:.1f} s)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--paths", type=int, default=1 << 20)
+    ap.add_argument("--timesteps", type=int, default=756)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

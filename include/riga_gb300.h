@@ -120,6 +120,8 @@ typedef struct rg_simulation_config {
   int32_t precision;          /* RG_PRECISION_* */
   int32_t dim_mode;           /* RG_DIM_* */
   int32_t lv_grid_x;          /* Dupire log-strike points; 0 = 96 (riga-market/src/lib.rs:28) */
+  uint64_t first_path;        /* global index of this request's path 0 (path-range sharding);
+                                 path i uses QMC point first_path + i + 1 (qmc.rs:286) */
 } rg_simulation_config;
 
 /* ImpliedVolGrid, crates/riga-market/src/lib.rs:83-91 */
@@ -167,6 +169,12 @@ typedef struct rg_trace_event {
   double time;
 } rg_trace_event;
 
+/* FP64 path sums behind a result, in this slot order (pv and KO funding are shifted by -1):
+ * sum(pv-1), sum((pv-1)^2), sum(KO funding-1), sum((KO funding-1)^2), sum(KI put), sum(KI put^2),
+ * sum(coupon | paid), sum(coupon^2 | paid), sum(put), sum(funding), sum(coupon quote - memory
+ * quote), sum(memory quote), #KO, #KI, #put eligible, #paid a coupon. */
+#define RG_PATH_SUMS 16
+
 /* PriceResult, crates/riga-core/src/lib.rs:243-255 */
 typedef struct rg_price_result {
   double pv, mc_error, ki_probability;
@@ -177,6 +185,7 @@ typedef struct rg_price_result {
   uint64_t ko_count, ki_count, put_eligible_count, coupon_path_count;
   int32_t n_trace_events;
   rg_trace_event trace_events[RG_TRACE_EVENT_CAP];
+  double path_sums[RG_PATH_SUMS]; /* merged exactly by rg_merge_results */
 } rg_price_result;
 
 /* One scenario of a common-random-number batch: a complete market plus an optional parallel
@@ -282,10 +291,40 @@ int32_t rg_price_risk_batch(rg_engine* engine, const rg_price_request* request,
                             const rg_central_difference_config* config,
                             rg_batch_risk_report* out);
 
+/* Merges the results of disjoint path shards (in shard order: fixed-order FP64 sums, trace
+ * events concatenated up to the cap) into the result of all their paths — the one gather of the
+ * multi-GPU path.  `paths` is the total path count. */
+int32_t rg_merge_results(const rg_price_result* parts, int32_t n_parts, uint64_t paths,
+                         rg_price_result* out);
+
+/* Device-time breakdown of the engine's last call, from CUDA events on the engine's stream. */
+typedef struct rg_timing {
+  double h2d_ms, prologue_ms, kernel_ms, reduce_ms, d2h_ms, device_ms;
+  uint64_t h2d_bytes, d2h_bytes;
+  int32_t kernel_launches; /* kernels this call launched (prologue + fused + reduce) */
+  int32_t grid, block, smem_bytes; /* launch shape of the fused kernel */
+} rg_timing;
+int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
+
 /* explain::run_paths restricted to [first_path, first_path + count),
  * crates/riga-engine/src/explain.rs:90-316 (reconstruct_path :319-333 is count == 1). */
 int32_t rg_run_paths(rg_engine* engine, const rg_price_request* request, uint64_t first_path,
                      uint64_t count, rg_path_record* out);
+
+/* ------------------------------------------------------------------ host tables --------------- */
+/* The Sobol direction table v[dim][32] the engine uses for `dim` dimensions: dimension 0 is van
+ * der Corput, dimension d >= 1 the Joe–Kuo recurrence with unit initial values on the d-th
+ * primitive polynomial of degree >= 2 (crates/riga-engine/src/qmc.rs:247-262, 316-430). */
+int32_t rg_sobol_directions(int64_t dim, uint32_t* out /* [dim * 32] */);
+
+/* The streamed Brownian-bridge schedule for `steps` steps of length dt: node_off[steps + 1]
+ * (first node consumed at each step), node_k[steps] (the preorder index of each node, i.e. the
+ * QMC step whose normals it reads; node 0 is the terminal point) and node_c[steps] (its
+ * conditional standard deviation) — the in-order traversal of the reference's depth-first
+ * bisection (crates/riga-engine/src/qmc.rs:155-191).  Returns the anchor-stack depth in
+ * *stack_depth. */
+int32_t rg_bridge_schedule(int64_t steps, double dt, int32_t* node_off, int32_t* node_k,
+                           double* node_c, int32_t* stack_depth);
 
 /* ------------------------------------------------------------------ gpu backend drop-in ------- */
 /* gpu::worst_of, crates/riga-engine/src/gpu.rs:171-205 / :515-517 (out = min(a, b)). */

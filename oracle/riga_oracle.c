@@ -737,7 +737,7 @@ typedef struct model {
   int has_lv;
   or_lv_surface lv[NMAX];
   int vr, scrambler;
-  uint64_t seed;
+  uint64_t seed, first_path;
   uint32_t* sob_v;
   int64_t sob_dim;
   uint32_t* hal_bases;
@@ -805,6 +805,7 @@ static int32_t model_init(model* m, const rg_price_request* r, const rg_market_s
   if (st) { model_free(m); return st; }
   m->vr = r->config.variance_reduction;
   m->seed = r->config.seed;
+  m->first_path = r->config.first_path;
   m->scrambler = r->config.scrambler;
   if (m->vr == RG_VR_SOBOL) {
     int64_t d = (int64_t)r->config.qmc_dimension;
@@ -893,7 +894,7 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
   } else {
     /* per-path QMC normals, Cholesky, bridge, note.rs:83-106 */
     for (int64_t s = 0; s < T; ++s) {
-      for (int f = 0; f < n; ++f) z[f] = ladder_normal(m, path_id, (uint64_t)(s * n + f));
+      for (int f = 0; f < n; ++f) z[f] = ladder_normal(m, m->first_path + path_id, (uint64_t)(s * n + f));
       chol_apply(m->L, n, z, y);
       for (int f = 0; f < n; ++f) ws->normals[(size_t)f * T + s] = y[f];
     }
@@ -1022,7 +1023,7 @@ static void accum_path(accum* a, const model* m, uint64_t path_id, const path_ou
   if (o->ko) {
     a->ko += 1;
     if (m->trace && a->n_trace < RG_TRACE_EVENT_CAP) {
-      a->trace[a->n_trace].path_id = path_id;
+      a->trace[a->n_trace].path_id = m->first_path + path_id;
       a->trace[a->n_trace].time = o->redemption_time;
       a->n_trace++;
     }
@@ -1205,9 +1206,9 @@ int32_t or_run_paths(const rg_price_request* r, uint64_t first, uint64_t count, 
     simulate_path(&m, p, &ws, &g, &o);
     rg_path_record* rec = &out[i];
     memset(rec, 0, sizeof *rec);
-    rec->path_id = p;
+    rec->path_id = m.first_path + p;
     rec->rng_seed = r->config.seed;
-    rec->sobol_index = m.vr == RG_VR_NONE ? 0 : p + 1;
+    rec->sobol_index = m.vr == RG_VR_NONE ? 0 : m.first_path + p + 1;
     rec->worst_final = o.worst_final;
     rec->knocked_out = o.ko;
     rec->ko_step = o.ko_step;

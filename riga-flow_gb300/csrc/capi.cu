@@ -1,0 +1,726 @@
+// capi.cu — the C ABI of the engine: errors, device discovery, the engine object, pricing,
+// scenario batches, the CRN risk batch and per-path replay records.
+//
+// The pipeline of one request, all on the engine's stream:
+//   validate (host) → host tables (host_prep.cu) → one packed H2D copy → FP64 prologue kernels
+//   (Dupire calibration per distinct surface, Cholesky per scenario) → fused path kernel
+//   (FP64 parity or FP32 CRN) → fixed-order reduction → one D2H copy of the FP64 sums →
+//   PriceResult assembly on the host (note.rs:262-372).
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rg_internal.h"
+
+namespace rg {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& m) { g_last_error = m; }
+
+[[noreturn]] void raise(int32_t status, const std::string& message) { throw Error{status, message}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear a non-sticky error so the context stays usable
+    raise(RG_ERR_GPU_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+void DevBuf::ensure(size_t n) {
+  if (n <= bytes && ptr) return;
+  release();
+  size_t want = n < 256 ? 256 : n;
+  cuda_check(cudaMalloc(&ptr, want), "cudaMalloc");
+  bytes = want;
+}
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+void HostBuf::ensure(size_t n) {
+  if (n <= bytes && ptr) return;
+  release();
+  size_t want = n < 256 ? 256 : n;
+  cuda_check(cudaMallocHost(&ptr, want), "cudaMallocHost");
+  bytes = want;
+}
+void HostBuf::release() {
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+// ------------------------------------------------------------------ device guard --------------
+struct DeviceInfo {
+  int32_t status = RG_OK;
+  std::string message, name, arch;
+  int sm_count = 0;
+  int count = 0;
+};
+
+static const DeviceInfo& device_info() {
+  static std::once_flag once;
+  static DeviceInfo info;
+  std::call_once(once, [] {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+      cudaGetLastError();
+      info.status = RG_ERR_GPU_UNAVAILABLE;
+      info.message = std::string("CUDA device 0: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "no device");
+      return;
+    }
+    info.count = count;
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
+      cudaGetLastError();
+      info.status = RG_ERR_GPU_UNAVAILABLE;
+      info.message = "CUDA device 0: properties unavailable";
+      return;
+    }
+    info.name = p.name;
+    info.arch = "sm_" + std::to_string(p.major) + std::to_string(p.minor);
+    info.sm_count = p.multiProcessorCount;
+    if (!(p.major == 10 && p.minor == 3)) {
+      info.status = RG_ERR_GPU_UNAVAILABLE;
+      info.message = "this build holds sm_103a code only; device 0 is " + info.arch;
+    }
+  });
+  return info;
+}
+
+}  // namespace rg
+
+using namespace rg;
+
+int32_t rg_guard_device() {
+  const DeviceInfo& d = device_info();
+  if (d.status) set_last_error(d.message);
+  return d.status;
+}
+
+#define RG_TRY(...)                              \
+  try {                                           \
+    __VA_ARGS__;                                  \
+    return RG_OK;                                 \
+  } catch (const rg::Error& e) {                  \
+    rg::set_last_error(e.message);                \
+    return e.status;                              \
+  } catch (const std::bad_alloc&) {               \
+    rg::set_last_error("host allocation failed"); \
+    return RG_ERR_GPU_ERROR;                      \
+  }
+
+static const char* const kCodes[] = {
+    "ok", "missing_as_of", "as_of_mismatch", "invalid_paths", "invalid_schedule",
+    "invalid_market_shape", "invalid_market", "invalid_trade", "invalid_local_vol", "shape_mismatch",
+    "gpu_unavailable", "gpu_error", "no_crn_rejected", "invalid_spot_bump", "invalid_volatility_bump",
+    "invalid_rate_bump", "invalid_correlation_bump", "risk_input_shape", "risk_paths_required",
+    "path_out_of_range", "invalid_argument", "unsupported", "invalid_percentile", "cancelled",
+    "device_timeout"};
+
+extern "C" const char* rg_status_code(int32_t status) {
+  if (status < 0 || status >= (int32_t)(sizeof kCodes / sizeof kCodes[0])) return "unknown";
+  return kCodes[status];
+}
+
+extern "C" int32_t rg_last_error(char* buf, size_t len) {
+  const std::string& m = g_last_error;
+  if (buf && len) {
+    size_t n = m.size() < len - 1 ? m.size() : len - 1;
+    memcpy(buf, m.data(), n);
+    buf[n] = 0;
+  }
+  return (int32_t)m.size();
+}
+
+extern "C" int32_t rg_abi_version(void) { return RG_ABI_VERSION; }
+
+static int32_t copy_str(const std::string& s, char* buf, size_t len) {
+  if (!buf || !len) return RG_ERR_INVALID_ARGUMENT;
+  size_t n = s.size() < len - 1 ? s.size() : len - 1;
+  memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return RG_OK;
+}
+
+extern "C" int32_t rg_ensure_available(void) { return rg_guard_device(); }
+
+extern "C" int32_t rg_device_name(char* buf, size_t len) {
+  int32_t g = rg_guard_device();
+  if (g) return g;
+  return copy_str(device_info().name, buf, len);
+}
+
+extern "C" int32_t rg_arch(char* buf, size_t len) {
+  int32_t g = rg_guard_device();
+  if (g) return g;
+  return copy_str(device_info().arch, buf, len);
+}
+
+// ------------------------------------------------------------------ engine --------------------
+struct rg_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  DevBuf arena, partial, sums, kosteps, records, calib_scratch, sobol;
+  int64_t sobol_dim = -1;
+  HostBuf host_sums;
+  std::vector<uint8_t> host_pack;
+  cudaEvent_t ev[6] = {};
+  rg_timing timing{};
+};
+
+extern "C" int32_t rg_engine_create(int32_t device, rg_engine** out) {
+  RG_TRY({
+    if (!out) raise(RG_ERR_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    int32_t g = rg_guard_device();
+    if (g) raise(g, device_info().message);
+    if (device < 0 || device >= device_info().count)
+      raise(RG_ERR_INVALID_ARGUMENT, "device index out of range");
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    std::unique_ptr<rg_engine> e(new rg_engine());
+    e->device = device;
+    cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t& ev : e->ev) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
+    *out = e.release();
+  })
+}
+
+extern "C" void rg_engine_destroy(rg_engine* e) {
+  if (!e) return;
+  if (e->stream) {
+    cudaStreamSynchronize(e->stream);
+    cudaStreamDestroy(e->stream);
+  }
+  for (cudaEvent_t ev : e->ev)
+    if (ev) cudaEventDestroy(ev);
+  delete e;
+}
+
+namespace rg {
+
+// Builds the device tables of a prepared request into the engine arena.
+struct Staged {
+  DevTables tb{};
+  DevScenario* scen = nullptr;
+  DevScen32* scen32 = nullptr;
+};
+
+static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
+  Pack pk;
+  const DevTrade& tr = P.trade;
+  const int64_t T = P.T;
+  // QMC tables
+  size_t o_sobol = 0, o_hb = 0, o_ho = 0, o_hp = 0;
+  std::vector<uint32_t> hb, ho, hp;
+  if (tr.vr == RG_VR_SOBOL) {
+    const std::vector<uint32_t>& v = sobol_table(tr.sob_dim);
+    o_sobol = pk.add(v);
+  } else if (tr.vr == RG_VR_HALTON) {
+    halton_tables(tr.hal_dim, tr.seed, hb, ho, hp);
+    o_hb = pk.add(hb);
+    o_ho = pk.add(ho);
+    o_hp = pk.add(hp);
+  }
+  size_t o_flags = pk.add(P.step_flags), o_per = pk.add(P.step_period), o_acc = pk.add(P.accr_inc);
+  size_t o_noff = pk.add(P.node_off), o_nk = pk.add(P.node_k), o_nc = pk.add(P.node_c),
+         o_ncf = pk.add(P.node_cf);
+  size_t o_ti = pk.add(P.lv_ti), o_tw = pk.add(P.lv_tw), o_twf = pk.add(P.lv_twf);
+  size_t o_df = pk.add(P.df), o_dfm = pk.add(P.df_mat);
+  size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
+  // local-vol surfaces: inputs (grids) and outputs
+  const int gx = tr.gx;
+  size_t o_lv = 0, o_lvf = 0, o_logs = 0, o_jobs = 0;
+  std::vector<size_t> o_mats, o_ks, o_vs;
+  size_t cells = 0, scratch = 0;
+  std::vector<CalibJob> jobs;
+  if (tr.has_lv) {
+    for (int j = 0; j < P.n_surf; ++j) cells += (size_t)P.surf_nt[j] * gx;
+    o_lv = pk.reserve(cells * sizeof(double));
+    o_lvf = pk.reserve(cells * sizeof(float2));
+    o_logs = pk.reserve((size_t)P.n_surf * gx * sizeof(double));
+    for (int f = 0; f < P.n; ++f) {
+      const rg_implied_vol_grid& g = req->local_vol[f];
+      o_mats.push_back(pk.add(g.maturities_years, (size_t)g.n_maturities));
+      o_ks.push_back(pk.add(g.strikes, (size_t)g.n_strikes));
+      o_vs.push_back(pk.add(g.vols, (size_t)g.n_maturities * g.n_strikes));
+    }
+    for (int j = 0; j < P.n_surf; ++j) {
+      const rg_implied_vol_grid& g = req->local_vol[P.surfaces[j].asset];
+      scratch += (size_t)4 * g.n_maturities * gx + gx + (size_t)6 * g.n_maturities * g.n_strikes;
+    }
+    jobs.resize(P.n_surf);
+    o_jobs = pk.reserve(sizeof(CalibJob) * (size_t)P.n_surf);
+  }
+  E->arena.ensure(pk.host.size());
+  uint8_t* base = static_cast<uint8_t*>(E->arena.ptr);
+  if (tr.has_lv) {
+    E->calib_scratch.ensure(scratch * sizeof(double));
+    double* sc = static_cast<double*>(E->calib_scratch.ptr);
+    size_t cell_off = 0, sc_off = 0;
+    for (int j = 0; j < P.n_surf; ++j) {
+      const SurfaceKey& key = P.surfaces[j];
+      const rg_implied_vol_grid& g = req->local_vol[key.asset];
+      CalibJob& J = jobs[j];
+      J.n_t = g.n_maturities;
+      J.n_k = g.n_strikes;
+      J.gx = gx;
+      J.mats = reinterpret_cast<const double*>(base + o_mats[key.asset]);
+      J.strikes = reinterpret_cast<const double*>(base + o_ks[key.asset]);
+      J.vols = reinterpret_cast<const double*>(base + o_vs[key.asset]);
+      J.spot = key.spot;
+      J.rate = key.rate;
+      J.shift = key.shift;
+      J.out_v = reinterpret_cast<double*>(base + o_lv) + cell_off;
+      J.out_vf = reinterpret_cast<float2*>(base + o_lvf) + cell_off;
+      J.out_logs = reinterpret_cast<double*>(base + o_logs) + (size_t)j * gx;
+      J.scratch = sc + sc_off;
+      cell_off += (size_t)J.n_t * gx;
+      sc_off += (size_t)4 * J.n_t * gx + gx + (size_t)6 * J.n_t * J.n_k;
+    }
+    memcpy(pk.host.data() + o_jobs, jobs.data(), sizeof(CalibJob) * jobs.size());
+  }
+  cuda_check(cudaEventRecord(E->ev[0], E->stream), "event");
+  cuda_check(cudaMemcpyAsync(base, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, E->stream),
+             "H2D request tables");
+  cuda_check(cudaEventRecord(E->ev[1], E->stream), "event");
+  E->timing.h2d_bytes += pk.host.size();
+  Staged S;
+  DevTables& tb = S.tb;
+  tb.sobol = reinterpret_cast<const uint32_t*>(base + o_sobol);
+  tb.hal_base = reinterpret_cast<const uint32_t*>(base + o_hb);
+  tb.hal_off = reinterpret_cast<const uint32_t*>(base + o_ho);
+  tb.hal_perm = reinterpret_cast<const uint32_t*>(base + o_hp);
+  tb.step_flags = reinterpret_cast<const uint32_t*>(base + o_flags);
+  tb.step_period = reinterpret_cast<const int32_t*>(base + o_per);
+  tb.accr_inc = reinterpret_cast<const double*>(base + o_acc);
+  tb.node_off = reinterpret_cast<const int32_t*>(base + o_noff);
+  tb.node_k = reinterpret_cast<const int32_t*>(base + o_nk);
+  tb.node_c = reinterpret_cast<const double*>(base + o_nc);
+  tb.node_cf = reinterpret_cast<const float*>(base + o_ncf);
+  tb.lv_ti = reinterpret_cast<const int2*>(base + o_ti);
+  tb.lv_tw = reinterpret_cast<const double*>(base + o_tw);
+  tb.lv_twf = reinterpret_cast<const float*>(base + o_twf);
+  tb.lv_v = reinterpret_cast<const double*>(base + o_lv);
+  tb.lv_vf = reinterpret_cast<const float2*>(base + o_lvf);
+  tb.lv_logs = reinterpret_cast<const double*>(base + o_logs);
+  tb.df = reinterpret_cast<const double*>(base + o_df);
+  tb.df_mat = reinterpret_cast<const double*>(base + o_dfm);
+  tb.lv_nt = P.lv_nt_max;
+  S.scen = reinterpret_cast<DevScenario*>(base + o_scen);
+  S.scen32 = reinterpret_cast<DevScen32*>(base + o_s32);
+  if (tr.has_lv) {
+    launch_calibrate(reinterpret_cast<const CalibJob*>(base + o_jobs), P.n_surf, E->stream);
+    E->timing.kernel_launches += 1;
+  }
+  launch_cholesky(S.scen, P.n_scen, P.n, E->stream);
+  E->timing.kernel_launches += 1;
+  cuda_check(cudaEventRecord(E->ev[2], E->stream), "event");
+  return S;
+}
+
+// PriceResult from the FP64 sums (note.rs:262-372); counts are exact in FP64.
+static void finish(const double* a, uint64_t paths, uint64_t seed, rg_price_result* out) {
+  memset(out, 0, sizeof *out);
+  const double P = (double)paths;
+  auto var = [](double s1, double s2, double n) {
+    return n > 1.0 ? (s2 - s1 * s1 / n) / (n - 1.0) : 0.0;
+  };
+  const double ko = a[ACC_NKO], ki = a[ACC_NKI], pe = a[ACC_NPUT], cp = a[ACC_NCPN];
+  const double mean_put = a[ACC_PUT] / P, mean_funding = a[ACC_FUND] / P;
+  const double mean_cq = a[ACC_CQ] / P, mean_mq = a[ACC_MQ] / P;
+  const double total = mean_funding + (mean_cq + mean_mq) / 10.0 - mean_put;
+  out->pv = total;
+  out->mc_error = std::sqrt(var(a[ACC_PV], a[ACC_PV2], P) / P);
+  out->ki_probability = ki / P;
+  out->legs.coupon = mean_cq;
+  out->legs.memory_coupon = mean_mq;
+  out->legs.down_and_in_put = mean_put;
+  out->legs.funding = mean_funding;
+  out->legs.total = total;
+  rg_transition_stats* s = out->stats;
+  s[0].input_count = paths;
+  s[0].output_count = (uint64_t)ko;
+  s[0].probability = ko / P;
+  s[0].mean_payoff = ko > 0 ? 1.0 + a[ACC_KOF] / ko : 0.0;
+  s[0].variance_payoff = var(a[ACC_KOF], a[ACC_KOF2], ko);
+  s[1].input_count = paths;
+  s[1].output_count = (uint64_t)ki;
+  s[1].probability = ki / P;
+  s[1].mean_payoff = ki > 0 ? a[ACC_KIPUT] / ki : 0.0;
+  s[1].variance_payoff = var(a[ACC_KIPUT], a[ACC_KIPUT2], ki);
+  s[2].input_count = paths;
+  s[2].output_count = (uint64_t)cp;
+  s[2].probability = cp / P;
+  s[2].mean_payoff = cp > 0 ? a[ACC_CPN] / cp : 0.0;
+  s[2].variance_payoff = var(a[ACC_CPN], a[ACC_CPN2], cp);
+  rg_ledger_entry* l = out->ledger;
+  l[0].population_before = paths;
+  l[0].population_after = (uint64_t)ko;
+  l[0].pv_impact = mean_funding * (ko / P);
+  l[1].population_before = paths - (uint64_t)ko;
+  l[1].population_after = (uint64_t)pe;
+  l[1].pv_impact = -mean_put;
+  l[2].population_before = paths;
+  l[2].population_after = (uint64_t)cp;
+  l[2].pv_impact = (mean_cq + mean_mq) / 10.0;
+  out->seed = seed;
+  out->ko_count = (uint64_t)ko;
+  out->ki_count = (uint64_t)ki;
+  out->put_eligible_count = (uint64_t)pe;
+  out->coupon_path_count = (uint64_t)cp;
+  for (int k = 0; k < RG_ACC; ++k) out->path_sums[k] = a[k];
+}
+
+// First RG_TRACE_EVENT_CAP knocked-out paths in path order (note.rs:174-180), read back in
+// growing chunks of the per-path KO steps.
+static void collect_trace(rg_engine* E, const int32_t* dev_ko, uint64_t paths, uint64_t first_path,
+                          double dt, rg_price_result* out) {
+  std::vector<int32_t> buf;
+  uint64_t done = 0, chunk = 4096;
+  while (done < paths && out->n_trace_events < RG_TRACE_EVENT_CAP) {
+    uint64_t n = paths - done < chunk ? paths - done : chunk;
+    buf.resize(n);
+    cuda_check(cudaMemcpyAsync(buf.data(), dev_ko + done, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               E->stream), "D2H ko steps");
+    cuda_check(cudaStreamSynchronize(E->stream), "trace sync");
+    for (uint64_t i = 0; i < n && out->n_trace_events < RG_TRACE_EVENT_CAP; ++i)
+      if (buf[i] >= 0) {
+        out->trace_events[out->n_trace_events].path_id = first_path + done + i;
+        out->trace_events[out->n_trace_events].time = (double)(buf[i] + 1) * dt;
+        out->n_trace_events++;
+      }
+    done += n;
+    chunk *= 4;
+  }
+}
+
+static void check_lane(const rg_price_request* req) {
+  if (req->config.variance_reduction == RG_VR_NONE)
+    raise(RG_ERR_UNSUPPORTED,
+          "the pseudo-random (ChaCha8) lane is one sequential stream over all paths and has no "
+          "device implementation; use variance_reduction sobol or halton");
+}
+
+// Prices `n_scen` scenarios (0 = the request's own market) into out[max(1, n_scen)].
+static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* sc, int n_scen,
+                  rg_price_result* out) {
+  validate_request(req);
+  check_lane(req);
+  for (int i = 0; i < n_scen; ++i) {
+    rg_price_request r2 = *req;
+    r2.market = sc[i].market;
+    r2.market.as_of = req->market.as_of;
+    validate_request(&r2);
+  }
+  std::lock_guard<std::mutex> lock(E->mu);
+  cuda_check(cudaSetDevice(E->device), "cudaSetDevice");
+  const int total = n_scen ? n_scen : 1;
+  const bool fp32 = req->config.precision == RG_PRECISION_FP32;
+  const int per_launch = fp32 ? 32 : 1;
+  const uint64_t paths = req->config.paths;
+  const bool trace = req->config.trace_level != RG_TRACE_OFF;
+  E->timing = rg_timing{};
+  for (int first = 0; first < total; first += per_launch) {
+    const int cnt = total - first < per_launch ? total - first : per_launch;
+    Prepared P;
+    prepare(req, n_scen ? sc + first : nullptr, n_scen ? cnt : 0, P);
+    Staged S = stage(E, req, P);
+    LaunchOut lo{};
+    int grid;
+    Fp32Shape sh{};
+    if (fp32) {
+      sh = phoenix32_shape(P, paths, device_info().sm_count);
+      grid = sh.grid;
+    } else {
+      grid = phoenix64_grid(P, paths);
+    }
+    E->partial.ensure((size_t)grid * P.n_scen * RG_ACC * sizeof(double));
+    E->sums.ensure((size_t)P.n_scen * RG_ACC * sizeof(double));
+    lo.partial = static_cast<double*>(E->partial.ptr);
+    lo.grid = grid;
+    if (trace) {
+      // KO trace events are recorded for the first scenario of each fused launch
+      E->kosteps.ensure(paths * sizeof(int32_t));
+      lo.ko_steps = static_cast<int32_t*>(E->kosteps.ptr);
+    }
+    const uint64_t path0 = req->config.first_path;
+    if (fp32) {
+      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, E->stream);
+      E->timing.block = sh.threads;
+      E->timing.smem_bytes = sh.smem;
+    } else {
+      launch_phoenix64(P, S.tb, S.scen, path0, paths, lo, E->stream);
+      E->timing.block = 128;
+    }
+    E->timing.grid = grid;
+    cuda_check(cudaEventRecord(E->ev[3], E->stream), "event");
+    launch_reduce(lo.partial, grid, P.n_scen, static_cast<double*>(E->sums.ptr), E->stream);
+    cuda_check(cudaEventRecord(E->ev[4], E->stream), "event");
+    E->timing.kernel_launches += 2;
+    E->host_sums.ensure((size_t)P.n_scen * RG_ACC * sizeof(double));
+    cuda_check(cudaMemcpyAsync(E->host_sums.ptr, E->sums.ptr, (size_t)P.n_scen * RG_ACC * sizeof(double),
+                               cudaMemcpyDeviceToHost, E->stream), "D2H sums");
+    E->timing.d2h_bytes += (size_t)P.n_scen * RG_ACC * sizeof(double);
+    cuda_check(cudaEventRecord(E->ev[5], E->stream), "event");
+    cuda_check(cudaStreamSynchronize(E->stream), "pricing");
+    float ms[5];
+    for (int k = 0; k < 5; ++k) cuda_check(cudaEventElapsedTime(&ms[k], E->ev[k], E->ev[k + 1]), "event time");
+    E->timing.h2d_ms += ms[0];
+    E->timing.prologue_ms += ms[1];
+    E->timing.kernel_ms += ms[2];
+    E->timing.reduce_ms += ms[3];
+    E->timing.d2h_ms += ms[4];
+    E->timing.device_ms += ms[0] + ms[1] + ms[2] + ms[3] + ms[4];
+    const double* hs = static_cast<const double*>(E->host_sums.ptr);
+    for (int i = 0; i < cnt; ++i) finish(hs + (size_t)i * RG_ACC, paths, req->config.seed, &out[first + i]);
+    if (trace) collect_trace(E, lo.ko_steps, paths, req->config.first_path, P.trade.dt, &out[first]);
+  }
+}
+
+}  // namespace rg
+
+extern "C" int32_t rg_price_put_leg(rg_engine* e, const rg_price_request* req, rg_price_result* out) {
+  RG_TRY({
+    if (!e || !req || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    price(e, req, nullptr, 0, out);
+  })
+}
+
+extern "C" int32_t rg_price_scenarios(rg_engine* e, const rg_price_request* req, const rg_scenario* sc,
+                                      int32_t n, rg_price_result* out) {
+  RG_TRY({
+    if (!e || !req || !out || (n > 0 && !sc)) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n <= 0) raise(RG_ERR_INVALID_ARGUMENT, "at least one scenario is required");
+    for (int i = 0; i < n; ++i)
+      if (sc[i].market.n_assets != req->market.n_assets)
+        raise(RG_ERR_INVALID_MARKET_SHAPE, "scenario asset count differs from the request's");
+    price(e, req, sc, n, out);
+  })
+}
+
+namespace rg {
+// validate_configuration, crates/riga-risk/src/lib.rs:338-457 (N-asset form).
+static void validate_risk(const rg_price_request* r, const rg_central_difference_config* c) {
+  if (c->random_number_policy == RG_NO_CRN)
+    raise(RG_ERR_NO_CRN_REJECTED,
+          "central finite differences require CommonRandomNumbers; independent streams are rejected");
+  if (!std::isfinite(c->spot_relative_bump) || c->spot_relative_bump <= 0.0 || c->spot_relative_bump >= 1.0)
+    raise(RG_ERR_INVALID_SPOT_BUMP, "spot_relative_bump must be finite, positive, and less than one");
+  if (!std::isfinite(c->volatility_absolute_bump) || c->volatility_absolute_bump <= 0.0)
+    raise(RG_ERR_INVALID_VOLATILITY_BUMP, "volatility_absolute_bump must be finite and positive");
+  if (!std::isfinite(c->rate_absolute_bump) || c->rate_absolute_bump <= 0.0)
+    raise(RG_ERR_INVALID_RATE_BUMP, "rate_absolute_bump must be finite and positive");
+  if (!std::isfinite(c->correlation_absolute_bump) || c->correlation_absolute_bump <= 0.0)
+    raise(RG_ERR_INVALID_CORRELATION_BUMP, "correlation_absolute_bump must be finite and positive");
+  const int n = r->market.n_assets;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      if (i == j) continue;
+      double rho = r->market.correlation[i * n + j];
+      if (!std::isfinite(rho) || rho - c->correlation_absolute_bump <= -1.0 ||
+          rho + c->correlation_absolute_bump >= 1.0)
+        raise(RG_ERR_INVALID_CORRELATION_BUMP,
+              "correlation up/down scenarios must remain strictly inside (-1, 1)");
+    }
+  for (int f = 0; f < n; ++f) {
+    double s = r->market.spots[f], v = r->market.vols[f];
+    if (!std::isfinite(s) || s <= 0.0) raise(RG_ERR_INVALID_SPOT_BUMP, "spot must be finite and positive");
+    double h = s * c->spot_relative_bump;
+    if (!std::isfinite(h) || h == 0.0 || s - h <= 0.0)
+      raise(RG_ERR_INVALID_SPOT_BUMP, "spot bump is not representable and positive");
+    if (!std::isfinite(v) || v < c->volatility_absolute_bump)
+      raise(RG_ERR_INVALID_VOLATILITY_BUMP, "volatility must be finite and at least volatility_absolute_bump");
+  }
+  if (r->config.paths < 2)
+    raise(RG_ERR_RISK_PATHS_REQUIRED, "at least two paths are required to report Monte Carlo risk uncertainty");
+  for (int f = 0; f < r->n_local_vol; ++f) {
+    const rg_implied_vol_grid& g = r->local_vol[f];
+    for (int i = 0; i < g.n_maturities * g.n_strikes; ++i)
+      if (!std::isfinite(g.vols[i]) || g.vols[i] < c->volatility_absolute_bump)
+        raise(RG_ERR_INVALID_VOLATILITY_BUMP,
+              "local-vol surface must align with assets and every implied-vol node must remain "
+              "non-negative under the down bump");
+  }
+}
+}  // namespace rg
+
+// Scenario order: base, per asset {spot+, spot-, vol+, vol-}, rate+, rate-, corr+, corr-
+// (crates/riga-risk/src/lib.rs:117-186, 573-626; scenario_count = 1 + 4n + 4).
+extern "C" int32_t rg_price_risk_batch(rg_engine* e, const rg_price_request* req,
+                                       const rg_central_difference_config* cfg,
+                                       rg_batch_risk_report* out) {
+  RG_TRY({
+    if (!e || !req || !cfg || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    validate_request(req);
+    validate_risk(req, cfg);
+    const int n = req->market.n_assets;
+    const int ns = 1 + 4 * n + 4;
+    std::vector<std::vector<double>> spots(ns), vols(ns), corr(ns), shift(ns);
+    std::vector<rg_scenario> sc(ns);
+    for (int s = 0; s < ns; ++s) {
+      spots[s].assign(req->market.spots, req->market.spots + n);
+      vols[s].assign(req->market.vols, req->market.vols + n);
+      corr[s].assign(req->market.correlation, req->market.correlation + n * n);
+      shift[s].assign(n, 0.0);
+      sc[s].market = req->market;
+    }
+    for (int f = 0; f < n; ++f) {
+      double h = req->market.spots[f] * cfg->spot_relative_bump;
+      spots[1 + 4 * f][f] += h;
+      spots[2 + 4 * f][f] -= h;
+      vols[3 + 4 * f][f] += cfg->volatility_absolute_bump;
+      vols[4 + 4 * f][f] += -cfg->volatility_absolute_bump;
+      shift[3 + 4 * f][f] = cfg->volatility_absolute_bump;
+      shift[4 + 4 * f][f] = -cfg->volatility_absolute_bump;
+    }
+    const int ir = 1 + 4 * n;
+    sc[ir].market.risk_free_rate += cfg->rate_absolute_bump;
+    sc[ir + 1].market.risk_free_rate += -cfg->rate_absolute_bump;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        if (i != j) {
+          corr[ir + 2][i * n + j] += cfg->correlation_absolute_bump;
+          corr[ir + 3][i * n + j] += -cfg->correlation_absolute_bump;
+        }
+    for (int s = 0; s < ns; ++s) {
+      sc[s].market.spots = spots[s].data();
+      sc[s].market.vols = vols[s].data();
+      sc[s].market.correlation = corr[s].data();
+      sc[s].implied_vol_shift = req->n_local_vol ? shift[s].data() : nullptr;
+    }
+    std::vector<rg_price_result> res(ns);
+    price(e, req, sc.data(), ns, res.data());
+    memset(out, 0, sizeof *out);
+    out->base = res[0];
+    out->scenario_count = (uint64_t)ns;
+    out->seed = req->config.seed;
+    out->n_assets = n;
+    for (int f = 0; f < n; ++f) {
+      const rg_price_result &su = res[1 + 4 * f], &sd = res[2 + 4 * f], &vu = res[3 + 4 * f], &vd = res[4 + 4 * f];
+      const double h = req->market.spots[f] * cfg->spot_relative_bump, hv = cfg->volatility_absolute_bump;
+      rg_asset_greeks& g = out->assets[f];
+      g.asset_index = f;
+      g.spot_bump = h;
+      g.volatility_bump = hv;
+      g.delta = {(su.pv - sd.pv) / (2.0 * h), (su.mc_error + sd.mc_error) / (2.0 * h)};
+      g.gamma = {(su.pv - 2.0 * res[0].pv + sd.pv) / (h * h),
+                 (su.mc_error + 2.0 * res[0].mc_error + sd.mc_error) / (h * h)};
+      g.vega = {(vu.pv - vd.pv) / (2.0 * hv), (vu.mc_error + vd.mc_error) / (2.0 * hv)};
+      g.spot_up_pv = su.pv;
+      g.spot_down_pv = sd.pv;
+      g.vol_up_pv = vu.pv;
+      g.vol_down_pv = vd.pv;
+      g.spot_up_mc_error = su.mc_error;
+      g.spot_down_mc_error = sd.mc_error;
+      g.vol_up_mc_error = vu.mc_error;
+      g.vol_down_mc_error = vd.mc_error;
+    }
+    // transition_risk, crates/riga-risk/src/lib.rs:519-554
+    for (int k = 0; k < RG_N_TRANSITIONS; ++k) {
+      double d = 0.0, v = 0.0;
+      for (int f = 0; f < n; ++f) {
+        const double h = out->assets[f].spot_bump, hv = out->assets[f].volatility_bump;
+        if (h > 0.0) d += (res[1 + 4 * f].ledger[k].pv_impact - res[2 + 4 * f].ledger[k].pv_impact) / (2.0 * h);
+        if (hv > 0.0) v += (res[3 + 4 * f].ledger[k].pv_impact - res[4 + 4 * f].ledger[k].pv_impact) / (2.0 * hv);
+      }
+      out->transitions[k] = {res[0].ledger[k].pv_impact, d, v};
+    }
+    out->rate_up_pv = res[ir].pv;
+    out->rate_down_pv = res[ir + 1].pv;
+    out->correlation_up_pv = res[ir + 2].pv;
+    out->correlation_down_pv = res[ir + 3].pv;
+    out->rate_bump = cfg->rate_absolute_bump;
+    out->correlation_bump = cfg->correlation_absolute_bump;
+    out->pv_mc_error = res[0].mc_error;
+  })
+}
+
+extern "C" int32_t rg_run_paths(rg_engine* e, const rg_price_request* req, uint64_t first, uint64_t count,
+                                rg_path_record* out) {
+  RG_TRY({
+    if (!e || !req || (count && !out)) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    validate_request(req);
+    check_lane(req);
+    if (first > req->config.paths || count > req->config.paths - first)
+      raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
+    if (count == 0) return RG_OK;
+    std::lock_guard<std::mutex> lock(e->mu);
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    Prepared P;
+    prepare(req, nullptr, 0, P);
+    Staged S = stage(e, req, P);
+    const bool fp32 = req->config.precision == RG_PRECISION_FP32;
+    LaunchOut lo{};
+    Fp32Shape sh{};
+    lo.grid = fp32 ? (sh = phoenix32_shape(P, count, device_info().sm_count)).grid : phoenix64_grid(P, count);
+    e->partial.ensure((size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double));
+    e->records.ensure(count * sizeof(rg_path_record));
+    lo.partial = static_cast<double*>(e->partial.ptr);
+    lo.records = static_cast<rg_path_record*>(e->records.ptr);
+    const uint64_t path0 = req->config.first_path + first;
+    if (fp32)
+      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, count, sh, lo, e->stream);
+    else
+      launch_phoenix64(P, S.tb, S.scen, path0, count, lo, e->stream);
+    cuda_check(cudaMemcpyAsync(out, lo.records, count * sizeof(rg_path_record), cudaMemcpyDeviceToHost,
+                               e->stream), "D2H records");
+    cuda_check(cudaStreamSynchronize(e->stream), "run_paths");
+  })
+}
+
+extern "C" int32_t rg_sobol_directions(int64_t dim, uint32_t* out) {
+  RG_TRY({
+    if (dim < 1 || dim > (int64_t(1) << 22) || !out) raise(RG_ERR_INVALID_ARGUMENT, "dim must be 1..2^22 and out non-null");
+    const std::vector<uint32_t>& v = sobol_table(dim);
+    memcpy(out, v.data(), v.size() * sizeof(uint32_t));
+  })
+}
+
+extern "C" int32_t rg_bridge_schedule(int64_t steps, double dt, int32_t* node_off, int32_t* node_k,
+                                      double* node_c, int32_t* stack_depth) {
+  RG_TRY({
+    if (steps < 1 || steps > (int64_t(1) << 22) || !(dt > 0.0) || !node_off || !node_k || !node_c)
+      raise(RG_ERR_INVALID_ARGUMENT, "steps must be 1..2^22, dt positive, buffers non-null");
+    Prepared P;
+    bridge_schedule_into(steps, dt, P);
+    memcpy(node_off, P.node_off.data(), P.node_off.size() * sizeof(int32_t));
+    memcpy(node_k, P.node_k.data(), P.node_k.size() * sizeof(int32_t));
+    memcpy(node_c, P.node_c.data(), P.node_c.size() * sizeof(double));
+    if (stack_depth) *stack_depth = P.stack_max;
+  })
+}
+
+extern "C" int32_t rg_merge_results(const rg_price_result* parts, int32_t n, uint64_t paths,
+                                    rg_price_result* out) {
+  RG_TRY({
+    if (!parts || !out || n < 1) raise(RG_ERR_INVALID_ARGUMENT, "at least one part is required");
+    if (paths == 0) raise(RG_ERR_INVALID_PATHS, "paths must be positive");
+    double acc[RG_ACC] = {0};
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < RG_ACC; ++k) acc[k] += parts[i].path_sums[k];
+    rg_price_result r;
+    finish(acc, paths, parts[0].seed, &r);
+    for (int i = 0; i < n && r.n_trace_events < RG_TRACE_EVENT_CAP; ++i)
+      for (int j = 0; j < parts[i].n_trace_events && r.n_trace_events < RG_TRACE_EVENT_CAP; ++j)
+        r.trace_events[r.n_trace_events++] = parts[i].trace_events[j];
+    *out = r;
+  })
+}
+
+extern "C" int32_t rg_engine_last_timing(rg_engine* e, rg_timing* out) {
+  RG_TRY({
+    if (!e || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(e->mu);
+    *out = e->timing;
+  })
+}

@@ -1,0 +1,224 @@
+// prologue.cu — the FP64 device prologue of a pricing request.
+//
+// * calibrate_kernel: one CTA per Dupire surface.  Natural-spline fit of each tenor's smile in
+//   log-moneyness, total-variance Dupire on the dense log-strike axis, clamp to [0.10, 3.00]
+//   (crates/riga-market/src/lib.rs:125-299).  Writes the FP64 grid the parity kernel reads and
+//   the (v, dv) FP32 pairs the production kernel interpolates.
+// * cholesky_kernel: one thread per scenario.  Jacobi minimum eigenvalue, diagonal-loading PSD
+//   clamp and Cholesky–Banachiewicz (crates/riga-market/src/correlation.rs:95-168), in place on
+//   the scenario's correlation block.
+// Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's.
+#include "rg_internal.h"
+
+namespace rg {
+
+// Natural-spline second derivatives by the Thomas algorithm (riga-market/src/lib.rs:125-176).
+__device__ static void spline_y2(const double* x, const double* y, int n, double* y2, double* h,
+                                 double* cp, double* dp) {
+  for (int i = 0; i < n; ++i) y2[i] = 0.0;
+  if (n < 3) return;
+  bool bad = false;
+  for (int i = 0; i < n - 1; ++i) {
+    h[i] = x[i + 1] - x[i];
+    if (h[i] <= 0.0) bad = true;
+  }
+  for (int i = 0; i < n; ++i)
+    if (!isfinite(y[i])) bad = true;
+  if (bad) return;
+  // b: diagonal; a/c: sub/super diagonals; d: right-hand side (computed inline)
+  auto b = [&](int i) { return (i == 0 || i == n - 1) ? 1.0 : 2.0 * (h[i - 1] + h[i]); };
+  auto a = [&](int i) { return i < n - 1 ? h[i] : 0.0; };
+  auto c = [&](int i) { return i + 1 < n - 1 ? h[i + 1] : 0.0; };
+  auto d = [&](int i) {
+    return (i == 0 || i == n - 1) ? 0.0 : 6.0 * ((y[i + 1] - y[i]) / h[i] - (y[i] - y[i - 1]) / h[i - 1]);
+  };
+  cp[0] = c(0) / b(0);
+  dp[0] = d(0) / b(0);
+  for (int i = 1; i < n; ++i) {
+    double m = b(i) - a(i) * cp[i - 1];
+    if (fabs(m) < 1e-300) m = 1e-300;
+    cp[i] = c(i) / m;
+    dp[i] = (d(i) - a(i) * dp[i - 1]) / m;
+  }
+  y2[n - 1] = dp[n - 1];
+  for (int i = n - 2; i >= 0; --i) y2[i] = dp[i] - cp[i] * y2[i + 1];
+}
+
+// Spline value and derivatives with the reference's term placement (lib.rs:178-203).
+__device__ static void spline_at(double p, const double* x, const double* y, const double* y2, int n,
+                                 double* f, double* f1, double* f2) {
+  int seg = 0;
+  while (seg + 1 < n - 1 && p > x[seg + 1]) ++seg;
+  double h = x[seg + 1] - x[seg];
+  double t = (p - x[seg]) / h;
+  t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+  double omt = 1.0 - t;
+  *f = (1.0 - t) * y[seg] + t * y[seg + 1] +
+       (h * h / 6.0) * ((t * t * t - t) * y2[seg] + (omt * (omt * omt) - (1.0 - t)) * y2[seg + 1]);
+  *f1 = (y[seg + 1] - y[seg] +
+         (h * h / 6.0) * ((3.0 * t * t - 1.0) * y2[seg] - (3.0 * (1.0 - t) * (1.0 - t) - 1.0) * y2[seg + 1])) /
+        h;
+  *f2 = (1.0 - t) * y2[seg + 1] + t * y2[seg];
+}
+
+__global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
+  const CalibJob J = jobs[blockIdx.x];
+  const int nt = J.n_t, nk = J.n_k, gx = J.gx;
+  double* w = J.scratch;
+  double* wx = w + nt * gx;
+  double* wxx = wx + nt * gx;
+  double* xa = wxx + nt * gx;
+  double* s_axis = xa + nt * gx;             // gx
+  double* xj = s_axis + gx;                   // nt * nk
+  double* y2 = xj + nt * nk;                  // nt * nk
+  double* tmp = y2 + nt * nk;                 // 3 * nt * nk (h, cp, dp)
+  double* yv = tmp + 3 * nt * nk;             // nt * nk shifted implied vols
+  const double s_min = J.strikes[0] * 0.55, s_max = J.strikes[nk - 1] * 1.05;
+  const double log_lo = log(s_min > 1e-6 ? s_min : 1e-6), log_hi = log(s_max > 1e-6 ? s_max : 1e-6);
+  for (int i = threadIdx.x; i < gx; i += blockDim.x) {
+    double ls = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
+    J.out_logs[i] = ls;
+    s_axis[i] = exp(ls);
+  }
+  for (int i = threadIdx.x; i < nt * nk; i += blockDim.x) yv[i] = J.vols[i] + J.shift;
+  __syncthreads();
+  // one thread per tenor: log-moneyness nodes and the spline solve
+  for (int k = threadIdx.x; k < nt; k += blockDim.x) {
+    double forward = J.spot * exp(J.rate * J.mats[k]);
+    for (int j = 0; j < nk; ++j) xj[k * nk + j] = log(J.strikes[j] / forward);
+    spline_y2(xj + k * nk, yv + k * nk, nk, y2 + k * nk, tmp + 3 * k * nk, tmp + 3 * k * nk + nk,
+              tmp + 3 * k * nk + 2 * nk);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
+    int k = c / gx, i = c % gx;
+    double tk = J.mats[k];
+    double forward = J.spot * exp(J.rate * tk);
+    const double* xk = xj + k * nk;
+    double x_lo = xk[0], x_hi = xk[nk - 1];
+    double xd = log(s_axis[i] / forward);
+    xd = xd < x_lo ? x_lo : (xd > x_hi ? x_hi : xd);
+    double sg, s1, s2;
+    if (nk >= 2) {
+      spline_at(xd, xk, yv + k * nk, y2 + k * nk, nk, &sg, &s1, &s2);
+    } else {
+      sg = yv[k * nk];
+      s1 = 0.0;
+      s2 = 0.0;
+    }
+    w[c] = sg * sg * tk;
+    wx[c] = 2.0 * sg * tk * s1;
+    wxx[c] = 2.0 * tk * (s1 * s1 + sg * s2);
+    xa[c] = xd;
+  }
+  __syncthreads();
+  const double* T = J.mats;
+  const double lo2 = 0.10 * 0.10, hi2 = 3.00 * 3.00;  // LV_CLAMP_LO/HI, lib.rs:30-32
+  for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
+    int k = c / gx, i = c % gx;
+    double dw;
+    if (nt == 1) {
+      dw = w[i] / (T[0] > 1e-9 ? T[0] : 1e-9);
+    } else if (k == 0) {
+      double sp = T[1] - T[0];
+      dw = (w[gx + i] - w[i]) / (sp > 1e-9 ? sp : 1e-9);
+    } else if (k == nt - 1) {
+      double sp = T[nt - 1] - T[nt - 2];
+      dw = (w[(nt - 1) * gx + i] - w[(nt - 2) * gx + i]) / (sp > 1e-9 ? sp : 1e-9);
+    } else {
+      double sp = T[k + 1] - T[k - 1];
+      dw = (w[(k + 1) * gx + i] - w[(k - 1) * gx + i]) / (sp > 1e-9 ? sp : 1e-9);
+    }
+    double ww = w[c] > 1e-12 ? w[c] : 1e-12;
+    double denom = 1.0 - (xa[c] / ww) * wx[c] + 0.25 * (-0.25 - 1.0 / ww) * wx[c] * wx[c] + 0.5 * wxx[c];
+    double lv2 = (isfinite(denom) && fabs(denom) > 1e-12) ? dw / denom : lo2;
+    lv2 = lv2 < lo2 ? lo2 : (lv2 > hi2 ? hi2 : lv2);
+    J.out_v[c] = sqrt(lv2);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
+    int i = c % gx;
+    double v = J.out_v[c];
+    double dv = i + 1 < gx ? J.out_v[c + 1] - v : 0.0;
+    J.out_vf[c] = make_float2((float)v, (float)dv);
+  }
+}
+
+void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s) {
+  if (n_jobs <= 0) return;
+  calibrate_kernel<<<n_jobs, 128, 0, s>>>(jobs_dev);
+  cuda_check(cudaGetLastError(), "calibrate_kernel launch");
+}
+
+// ------------------------------------------------------------------ correlation ---------------
+__device__ static double min_eigenvalue(const double* c, int n) {
+  double a[RG_NMAX * RG_NMAX];
+  for (int i = 0; i < n * n; ++i) a[i] = c[i];
+  if (n == 1) return a[0];
+  for (int it = 0; it < 100; ++it) {  // cyclic Jacobi, correlation.rs:217-260
+    int p = 0, q = 0;
+    double mx = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = i + 1; j < n; ++j) {
+        double v = fabs(a[i * n + j]);
+        if (v > mx) { mx = v; p = i; q = j; }
+      }
+    if (mx < 1.0e-14) break;
+    double app = a[p * n + p], aqq = a[q * n + q], apq = a[p * n + q];
+    double theta = 0.5 * (aqq - app) / apq;
+    double t = copysign(1.0, theta) / (fabs(theta) + sqrt(theta * theta + 1.0));
+    double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+    for (int k = 0; k < n; ++k) {
+      double akp = a[k * n + p], akq = a[k * n + q];
+      a[k * n + p] = cs * akp - sn * akq;
+      a[k * n + q] = sn * akp + cs * akq;
+    }
+    for (int k = 0; k < n; ++k) {
+      double apk = a[p * n + k], aqk = a[q * n + k];
+      a[p * n + k] = cs * apk - sn * aqk;
+      a[q * n + k] = sn * apk + cs * aqk;
+    }
+  }
+  double m = INFINITY;
+  for (int i = 0; i < n; ++i) m = fmin(m, a[i * n + i]);
+  return m;
+}
+
+__global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_scen) return;
+  DevScenario& sc = scen[i];
+  double src[RG_NMAX * RG_NMAX], l[RG_NMAX * RG_NMAX];
+  for (int k = 0; k < n * n; ++k) src[k] = sc.L[k];
+  // use the matrix as is when min eig >= 1e-10, else PSD-clamp with floor 1e-8
+  // (is_positive_semidefinite(-1e-10) and psd_clamp(1e-8), correlation.rs:103-136, 144-148)
+  double mn = min_eigenvalue(src, n);
+  if (!(mn >= 1.0e-10)) {
+    double shift = 1.0e-8 - mn, inv[RG_NMAX];
+    for (int k = 0; k < n; ++k) src[k * n + k] += shift;
+    for (int k = 0; k < n; ++k) inv[k] = 1.0 / sqrt(src[k * n + k]);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) src[a * n + b] *= inv[a] * inv[b];
+  }
+  for (int k = 0; k < n * n; ++k) l[k] = 0.0;
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b <= a; ++b) {
+      double sum = src[a * n + b];
+      for (int k = 0; k < b; ++k) sum -= l[a * n + k] * l[b * n + k];
+      if (a == b) {
+        l[a * n + b] = sqrt(sum > 0.0 ? sum : 0.0);
+      } else {
+        double pivot = l[b * n + b];
+        l[a * n + b] = pivot > 0.0 ? sum / pivot : 0.0;
+      }
+    }
+  for (int k = 0; k < n * n; ++k) sc.L[k] = l[k];
+  sc.status = 0;
+}
+
+void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s) {
+  cholesky_kernel<<<(n_scen + 63) / 64, 64, 0, s>>>(scen_dev, n_scen, n);
+  cuda_check(cudaGetLastError(), "cholesky_kernel launch");
+}
+
+}  // namespace rg

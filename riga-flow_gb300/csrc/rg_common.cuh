@@ -1,0 +1,235 @@
+// rg_common.cuh — shared device definitions for the GB300 Phoenix engine (sm_103a).
+//
+// Layout of everything the fused kernels read lives here: the per-trade step schedule, the
+// per-scenario market block, the Brownian-bridge node schedule and the QMC tables.  All tables
+// are built once per request on the host (integer/FP64 work) or by the FP64 prologue kernels
+// (Cholesky, Dupire calibration) and stay resident in HBM for every kernel of the request.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/riga_gb300.h"
+
+#define RG_NMAX RG_MAX_ASSETS
+#define RG_ACC 16          // FP64 accumulators per (block, scenario)
+#define RG_STACK_MAX 24    // Brownian-bridge anchor stack depth (T <= 2^22)
+#define RG_MAX_SCEN 64     // scenarios in one fused CRN launch
+
+// Accumulator slots (per scenario).  Second moments are of shifted values so that the FP64
+// sums keep their precision: pv and KO funding are shifted by 1.
+enum {
+  ACC_PV = 0, ACC_PV2, ACC_KOF, ACC_KOF2, ACC_KIPUT, ACC_KIPUT2, ACC_CPN, ACC_CPN2,
+  ACC_PUT, ACC_FUND, ACC_CQ, ACC_MQ, ACC_NKO, ACC_NKI, ACC_NPUT, ACC_NCPN
+};
+
+// Per-step flags of the Phoenix schedule (note.rs:150-218), identical for every path.
+enum : uint32_t {
+  STEP_PERIOD_END = 1u,    // a coupon period closes at this step
+  STEP_CALL_ACTIVE = 2u,   // step >= call_start_step
+  STEP_ACCRUE = 4u,        // daily accrual allowed (not the fixed first period)
+  STEP_PERIOD_RESET = 8u,  // the period index changed at this step
+  STEP_FIXED_DUE = 16u     // the due amount is the fixed coupon (period 0, fixed first coupon)
+};
+
+struct DevTrade {
+  int32_t n, vr, scrambler, has_lv;
+  int64_t steps, periods;
+  int64_t sob_dim;     // rows of the Sobol table (the wrap modulus)
+  int32_t hal_dim;
+  int32_t gx;          // Dupire log-strike points
+  uint64_t seed;
+  double dt, sqrt_dt, inv_sqrt_dt, maturity;
+  double init[RG_NMAX];
+  double call_barrier, coupon_barrier, coupon_rate, strike, ki;
+  int32_t memory;
+  uint32_t x_lo, x_hi;  // probit branch thresholds on the 32-bit Sobol integer
+};
+
+struct DevScenario {
+  double spots[RG_NMAX], vols[RG_NMAX], q[RG_NMAX];
+  double rate;
+  double L[RG_NMAX * RG_NMAX];  // written by the FP64 Cholesky kernel
+  int32_t surf[RG_NMAX];         // calibrated Dupire surface per asset (-1 = flat vol)
+  int32_t surf_off[RG_NMAX];     // first cell of that surface in the packed local-vol grids
+  int32_t status;                // Cholesky status
+};
+
+// Device pointers of one request's resident tables.
+struct DevTables {
+  const uint32_t* sobol;       // [sob_dim][32]
+  const uint32_t* hal_base;    // [hal_dim]
+  const uint32_t* hal_off;     // [hal_dim] offsets into hal_perm
+  const uint32_t* hal_perm;
+  const uint32_t* step_flags;  // [T]
+  const int32_t* step_period;  // [T]
+  const double* accr_inc;      // [periods] coupon_rate / period_steps
+  const int32_t* node_off;     // [T+1] first bridge node consumed at step t
+  const int32_t* node_k;       // [T] preorder index (QMC step) of each node, consumption order
+  const double* node_c;        // [T] bridge standard deviation of each node
+  const float* node_cf;        // [T] the same in FP32
+  const int2* lv_ti;           // [n][T] (tenor row at or below step t's time, next row)
+  const double* lv_tw;         // [n][T] tenor weight
+  const float* lv_twf;         // [n][T] tenor weight in FP32
+  const double* lv_v;          // [surfaces][n_t][gx] FP64 local vol
+  const float2* lv_vf;         // [surfaces][n_t][gx] (v, v[j+1]-v[j]) FP32
+  const double* lv_logs;       // [surfaces][gx] log-strike axis
+  const double* df;            // [scenarios][T] exp(-r_s * (t+1) dt)
+  const double* df_mat;        // [scenarios] exp(-r_s * maturity)
+  int32_t lv_nt;
+};
+
+// ------------------------------------------------------------------ integer QMC primitives ----
+__host__ __device__ __forceinline__ uint64_t rg_mix64(uint64_t z) {
+  // SplitMix64 finaliser (crates/riga-engine/src/qmc.rs:310-314)
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// Nested (Owen) scramble keyed on the scrambled prefix (qmc.rs:292-308).  The loop-invariant key
+// part seed ^ dim*C1 is hoisted; bit*C2 is a running sum.
+__device__ __forceinline__ uint32_t rg_owen(uint32_t x, uint64_t dim, uint64_t seed) {
+  const uint64_t base = seed ^ (dim * 0x9E3779B97F4A7C15ULL);
+  uint32_t result = 0, prefix = 0;
+#pragma unroll 4
+  for (int bit = 31; bit >= 0; --bit) {
+    uint32_t b = (x >> bit) & 1u;
+    uint64_t h = rg_mix64(base ^ ((uint64_t)bit * 0xD6E8FEB86659FD93ULL) ^
+                          ((uint64_t)prefix * 0xA24BAED4963EE407ULL));
+    uint32_t s = b ^ (uint32_t)(h >> 63);
+    result |= s << bit;
+    prefix = (prefix << 1) | s;
+  }
+  return result;
+}
+
+// Digital shift: the engine's production scrambler (one XOR mask per dimension).
+__host__ __device__ __forceinline__ uint32_t rg_digital_shift(uint64_t dim, uint64_t seed) {
+  return (uint32_t)(rg_mix64(seed ^ ((dim + 1) * 0xD1B54A32D192ED03ULL)) >> 32);
+}
+
+// Gray-code Sobol integer of 1-based point n: XOR of row[k] over the set bits of n ^ (n >> 1)
+// (qmc.rs:269-279: an odd count (n>>k)-(n>>(k+1)) is exactly bit k of the Gray code).
+__device__ __forceinline__ uint32_t rg_sobol_gray(const uint32_t* __restrict__ row, uint64_t n) {
+  uint64_t g = n ^ (n >> 1);
+  uint32_t x = 0;
+  uint32_t gl = (uint32_t)g;
+  while (gl) {
+    int k = __ffs(gl) - 1;
+    x ^= __ldg(row + k);
+    gl &= gl - 1;
+  }
+  return x;
+}
+
+// ------------------------------------------------------------------ inverse normal ------------
+// Acklam's rational approximation (qmc.rs:37-91), FP64, reference operation order.
+__device__ __forceinline__ double rg_probit64(double p) {
+  const double a0 = -3.969683028665376e1, a1 = 2.209460984245205e2, a2 = -2.759285104469687e2,
+               a3 = 1.383577518672690e2, a4 = -3.066479806614716e1, a5 = 2.506628277459239e0;
+  const double b0 = -5.447609879822406e1, b1 = 1.615858368580409e2, b2 = -1.556989798598866e2,
+               b3 = 6.680131188771972e1, b4 = -1.328068155288572e1;
+  const double c0 = -7.784894002430293e-3, c1 = -3.223964580411365e-1, c2 = -2.400758277161838e0,
+               c3 = -2.549732539343734e0, c4 = 4.374664141464968e0, c5 = 2.938163982698783e0;
+  const double d0 = 7.784695709041462e-3, d1 = 3.224671290700398e-1, d2 = 2.445134137142996e0,
+               d3 = 3.754408661907416e0;
+  if (p <= 0.0) return -INFINITY;
+  if (p >= 1.0) return INFINITY;
+  const double plow = 0.02425, phigh = 1.0 - plow;
+  if (p < plow) {
+    double q = sqrt(-2.0 * log(p));
+    return (((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
+           ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
+  } else if (p <= phigh) {
+    double q = p - 0.5, r = q * q;
+    return (((((a0 * r + a1) * r + a2) * r + a3) * r + a4) * r + a5) * q /
+           (((((b0 * r + b1) * r + b2) * r + b3) * r + b4) * r + 1.0);
+  } else {
+    double q = sqrt(-2.0 * log(1.0 - p));
+    return -(((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
+           ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
+  }
+}
+
+// The same approximation in FP32, taking the 32-bit scrambled integer x (u = (x + 1/2) / 2^32).
+// The branch is decided on x against integer thresholds computed in FP64 on the host, so every
+// coordinate takes the same branch as the FP64 reference.  Tail probabilities are formed from x
+// or ~x so that no 1 - u cancellation occurs.
+__device__ __forceinline__ float rg_probit32(uint32_t x, uint32_t x_lo, uint32_t x_hi) {
+  const float a0 = -3.969683028665376e1f, a1 = 2.209460984245205e2f, a2 = -2.759285104469687e2f,
+              a3 = 1.383577518672690e2f, a4 = -3.066479806614716e1f, a5 = 2.506628277459239e0f;
+  const float b0 = -5.447609879822406e1f, b1 = 1.615858368580409e2f, b2 = -1.556989798598866e2f,
+              b3 = 6.680131188771972e1f, b4 = -1.328068155288572e1f;
+  const float c0 = -7.784894002430293e-3f, c1 = -3.223964580411365e-1f, c2 = -2.400758277161838e0f,
+              c3 = -2.549732539343734e0f, c4 = 4.374664141464968e0f, c5 = 2.938163982698783e0f;
+  const float d0 = 7.784695709041462e-3f, d1 = 3.224671290700398e-1f, d2 = 2.445134137142996e0f,
+              d3 = 3.754408661907416e0f;
+  if (x >= x_lo && x <= x_hi) {
+    float q = fmaf((float)(int32_t)(x ^ 0x80000000u), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+    float r = q * q;
+    float num = fmaf(fmaf(fmaf(fmaf(fmaf(a0, r, a1), r, a2), r, a3), r, a4), r, a5) * q;
+    float den = fmaf(fmaf(fmaf(fmaf(fmaf(b0, r, b1), r, b2), r, b3), r, b4), r, 1.0f);
+    return __fdividef(num, den);
+  }
+  const bool lower = x < x_lo;
+  const uint32_t t = lower ? x : ~x;
+  float p = fmaf((float)t, 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+  float q = sqrtf(-2.0f * logf(p));
+  float num = fmaf(fmaf(fmaf(fmaf(fmaf(c0, q, c1), q, c2), q, c3), q, c4), q, c5);
+  float den = fmaf(fmaf(fmaf(fmaf(d0, q, d1), q, d2), q, d3), q, 1.0f);
+  float z = __fdividef(num, den);
+  return lower ? z : -z;
+}
+
+// ------------------------------------------------------------------ Halton -------------------
+// Digit-permuted radical inverse (qmc.rs:143-153) in FP64.
+__device__ __forceinline__ double rg_halton_u(uint64_t index, uint32_t base, const uint32_t* perm) {
+  double inv = 1.0 / (double)base, factor = inv, result = 0.0;
+  while (index > 0) {
+    result += factor * (double)__ldg(perm + (index % base));
+    index /= base;
+    factor *= inv;
+  }
+  return result;
+}
+
+// The QMC integer for (point, dim) before the probit: scrambled Sobol (Owen or digital shift).
+__device__ __forceinline__ uint32_t rg_sobol_scrambled(const DevTrade& tr, const uint32_t* __restrict__ sobol,
+                                                       uint64_t point, uint64_t dim) {
+  const uint32_t* row = sobol + 32 * (dim % (uint64_t)tr.sob_dim);
+  uint32_t x = rg_sobol_gray(row, point + 1);
+  return tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT ? x ^ rg_digital_shift(dim, tr.seed)
+                                                   : rg_owen(x, dim, tr.seed);
+}
+
+// FP64 normal of the QMC lanes (Ladder::normal, qmc.rs:119-125, 284-289).
+__device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevTables& tb,
+                                                  uint64_t point, uint64_t dim) {
+  double u;
+  if (tr.vr == RG_VR_SOBOL) {
+    uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
+    u = ((double)x + 0.5) / 4294967296.0;
+  } else {
+    uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
+    u = rg_halton_u(point + 1, __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx));
+  }
+  u = u < 1.0e-12 ? 1.0e-12 : (u > 1.0 - 1.0e-12 ? 1.0 - 1.0e-12 : u);
+  return rg_probit64(u);
+}
+
+// FP32 normal of the QMC lanes.
+__device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTables& tb,
+                                                 uint64_t point, uint64_t dim) {
+  if (tr.vr == RG_VR_SOBOL) {
+    uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
+    return rg_probit32(x, tr.x_lo, tr.x_hi);
+  }
+  return (float)rg_qmc_normal64(tr, tb, point, dim);
+}
+
+// ------------------------------------------------------------------ kernels (launchers) -------
+struct DevRecordOut;  // forward
+
+// Status word a kernel raises instead of trapping.
+enum { KSTAT_OK = 0, KSTAT_BAD_LAUNCH = 1 };

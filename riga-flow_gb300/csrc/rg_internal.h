@@ -1,0 +1,161 @@
+// rg_internal.h — host-side structures shared by the C ABI, the request preparation and the
+// kernel launchers.  Nothing here crosses the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rg_common.cuh"
+
+namespace rg {
+
+// Error raised inside the host layer; converted to a status code at the ABI boundary.
+struct Error {
+  int32_t status;
+  std::string message;
+};
+
+[[noreturn]] void raise(int32_t status, const std::string& message);
+void set_last_error(const std::string& message);
+void cuda_check(cudaError_t e, const char* what);
+
+// A device buffer that only grows.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n);
+  void release();
+  ~DevBuf() { release(); }
+};
+
+// A pinned host buffer that only grows.
+struct HostBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n);
+  void release();
+  ~HostBuf() { release(); }
+};
+
+// Packs many small tables into one host staging area, copied to the device in one transfer.
+struct Pack {
+  std::vector<uint8_t> host;
+  template <class T>
+  size_t add(const T* data, size_t count) {
+    size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + sizeof(T) * count);
+    if (count) memcpy(host.data() + off, data, sizeof(T) * count);
+    return off;
+  }
+  template <class T>
+  size_t add(const std::vector<T>& v) { return add(v.data(), v.size()); }
+  size_t reserve(size_t bytes) {
+    size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + bytes);
+    return off;
+  }
+};
+
+// One Dupire surface to calibrate: asset index, the market spot and rate it is calibrated
+// against and the parallel implied-vol shift (crates/riga-risk/src/lib.rs:260-279).
+struct SurfaceKey {
+  int asset;
+  double spot, rate, shift;
+  bool operator==(const SurfaceKey& o) const {
+    return asset == o.asset && spot == o.spot && rate == o.rate && shift == o.shift;
+  }
+};
+
+// FP32 scenario constants for the CRN kernel, one per scenario.
+struct DevScen32 {
+  float x0[RG_NMAX];      // ln(spot / initial_spot)
+  float mu_dt[RG_NMAX];   // (r - q) dt
+  float sig[RG_NMAX];     // flat vol
+  float a_u[RG_NMAX];     // (ln initial_spot - log_lo) / h
+  float inv_h[RG_NMAX];   // 1 / h on the Dupire log-strike axis
+  int32_t surf_off[RG_NMAX];
+};
+
+// Everything one request needs on the device, after preparation.
+struct Prepared {
+  DevTrade trade{};
+  int n = 0;
+  int64_t T = 0;
+  int n_scen = 0;
+  int n_surf = 0;
+  int lv_nt_max = 0;
+  int stack_max = 0;
+  double ln_ko = 0, ln_cb = 0, ln_ki = 0;  // log barriers for the FP32 kernel
+  std::vector<uint32_t> step_flags;
+  std::vector<int32_t> step_period;
+  std::vector<double> accr_inc;
+  std::vector<int32_t> node_off, node_k;
+  std::vector<double> node_c;
+  std::vector<float> node_cf;
+  std::vector<int32_t> lv_ti;   // [n][T][2] (row, next row)
+  std::vector<double> lv_tw;    // [n][T]
+  std::vector<float> lv_twf;    // [n][T]
+  std::vector<DevScenario> scen;
+  std::vector<DevScen32> scen32;
+  std::vector<double> df, df_mat;
+  std::vector<SurfaceKey> surfaces;
+  std::vector<int32_t> surf_nt;  // tenor count of each surface
+  std::vector<double> asset_log_lo, asset_log_hi;
+  // host copies of the request inputs the calibration kernel reads
+  std::vector<const rg_implied_vol_grid*> grids;
+};
+
+struct Engine;
+
+// Request preparation (host, FP64): validation already done.
+void prepare(const rg_price_request* req, const rg_scenario* scen, int n_scen, Prepared& P);
+// The streamed bridge schedule (node_off, node_k, node_c, stack_max) of T steps.
+void bridge_schedule_into(int64_t T, double dt, Prepared& P);
+// The Sobol direction table for `dim` dimensions (process-wide cache).
+const std::vector<uint32_t>& sobol_table(int64_t dim);
+// Halton bases and permutations.
+void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vector<uint32_t>& off,
+                   std::vector<uint32_t>& perm);
+
+// Validation of lib.rs:209-321, generalised to N assets.
+void validate_request(const rg_price_request* r);
+
+// Kernel launchers (defined in the .cu files).
+struct CalibJob {
+  int32_t n_t, n_k, gx, pad;
+  const double* mats;
+  const double* strikes;
+  const double* vols;
+  double spot, rate, shift;
+  double* out_v;
+  float2* out_vf;
+  double* out_logs;
+  double* scratch;  // 4 * n_t * gx + gx + 6 * n_t * n_k doubles
+};
+void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s);
+void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s);
+
+struct LaunchOut {
+  double* partial;      // [grid][n_scen][RG_ACC]
+  int32_t* ko_steps;    // [npaths] (scenario 0) or null
+  rg_path_record* records;  // [npaths] or null
+  int grid;
+};
+int phoenix64_grid(const Prepared& P, uint64_t npaths);
+void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
+                      uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);
+struct Fp32Shape {
+  int Sb, Pb, TT, threads, grid, smem;
+};
+Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count);
+void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
+                      const DevScen32* scen32_dev, uint64_t path0, uint64_t npaths,
+                      const Fp32Shape& shape, const LaunchOut& out, cudaStream_t s);
+void launch_reduce(const double* partial, int grid, int n_scen, double* out, cudaStream_t s);
+
+}  // namespace rg

@@ -104,6 +104,7 @@ class SimConfig(C.Structure):
         ("precision", C.c_int32),
         ("dim_mode", C.c_int32),
         ("lv_grid_x", C.c_int32),
+        ("first_path", C.c_uint64),
     ]
 
 
@@ -175,7 +176,16 @@ class PriceResult(C.Structure):
         ("coupon_path_count", C.c_uint64),
         ("n_trace_events", C.c_int32),
         ("trace_events", TraceEvent * RG_TRACE_EVENT_CAP),
+        ("path_sums", C.c_double * 16),
     ]
+
+
+class Timing(C.Structure):
+    _fields_ = [("h2d_ms", C.c_double), ("prologue_ms", C.c_double), ("kernel_ms", C.c_double),
+                ("reduce_ms", C.c_double), ("d2h_ms", C.c_double), ("device_ms", C.c_double),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("kernel_launches", C.c_int32), ("grid", C.c_int32), ("block", C.c_int32),
+                ("smem_bytes", C.c_int32)]
 
 
 class Scenario(C.Structure):
@@ -285,6 +295,11 @@ SIGNATURES = {
                                    C.POINTER(CentralDifferenceConfig),
                                    C.POINTER(BatchRiskReport)]),
     "rg_run_paths": (_i32, [_vp, C.POINTER(PriceRequest), _u64, _u64, C.POINTER(PathRecord)]),
+    "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
+    "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
+    "rg_sobol_directions": (_i32, [_i64, C.POINTER(C.c_uint32)]),
+    "rg_bridge_schedule": (_i32, [_i64, C.c_double, C.POINTER(_i32), C.POINTER(_i32),
+                                  C.POINTER(C.c_double), C.POINTER(_i32)]),
     "rg_worst_of": (_i32, [_fp, _fp, _fp, _i64]),
     "rg_lv_terminal_spots": (_i32, [_fp, _fp, _fp, _i64, _fp, _fp, C.c_float, _i64, _i64,
                                     C.c_float, C.c_float, _fp, _fp, C.POINTER(_i32)]),

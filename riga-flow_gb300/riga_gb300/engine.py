@@ -1,0 +1,121 @@
+"""The reference's public pricing API over the engine's C ABI.
+
+* ``price_put_leg`` — ``riga_engine::price_put_leg`` (crates/riga-engine/src/lib.rs:183-186)
+* ``price_scenarios`` — a CRN scenario batch in one fused launch (crates/riga-risk/src/lib.rs:253-258)
+* ``price_risk_batch`` — ``riga_risk::price_risk_batch`` (crates/riga-risk/src/lib.rs:573-626)
+* ``run_paths`` / ``reconstruct_path`` / ``query_worst_percentile`` —
+  crates/riga-engine/src/explain.rs:90-372
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import threading
+from typing import Optional
+
+from . import abi
+from .abi import RigaError, check, load_library
+from .types import PriceRequest, market_to_abi, record_to_dict, result_to_json
+
+
+class Engine:
+    """One engine handle: a CUDA stream plus its resident device workspace."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        check(self.lib, self.lib.rg_engine_create(device, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.rg_engine_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- pricing ---------------
+    def price_raw(self, request: PriceRequest) -> abi.PriceResult:
+        a = request.to_abi()
+        out = abi.PriceResult()
+        check(self.lib, self.lib.rg_price_put_leg(self.handle, a.ptr, C.byref(out)))
+        return out
+
+    def price_put_leg(self, request: PriceRequest) -> dict:
+        return result_to_json(self.price_raw(request), request)
+
+    def price_scenarios_raw(self, request: PriceRequest, scenarios) -> list:
+        """``scenarios``: list of (MarketSnapshot, implied-vol shift list or None)."""
+        a = request.to_abi()
+        keep = []
+        arr = (abi.Scenario * len(scenarios))()
+        for i, (mk, shift) in enumerate(scenarios):
+            arr[i].market = market_to_abi(mk, lambda x: (keep.append(x), x)[1])
+            if shift is not None:
+                buf = (C.c_double * len(shift))(*shift)
+                keep.append(buf)
+                arr[i].implied_vol_shift = C.cast(buf, C.POINTER(C.c_double))
+        out = (abi.PriceResult * len(scenarios))()
+        check(self.lib, self.lib.rg_price_scenarios(self.handle, a.ptr, arr, len(scenarios), out))
+        return list(out)
+
+    def price_risk_batch_raw(self, request: PriceRequest, config: Optional[abi.CentralDifferenceConfig] = None):
+        cfg = config or abi.CentralDifferenceConfig(0.01, 0.01, 1e-4, 0.01, abi.CRN)
+        a = request.to_abi()
+        out = abi.BatchRiskReport()
+        check(self.lib, self.lib.rg_price_risk_batch(self.handle, a.ptr, C.byref(cfg), C.byref(out)))
+        return out
+
+    def run_paths_raw(self, request: PriceRequest, first: int = 0, count: Optional[int] = None):
+        count = request.config.paths - first if count is None else count
+        a = request.to_abi()
+        out = (abi.PathRecord * max(1, count))()
+        check(self.lib, self.lib.rg_run_paths(self.handle, a.ptr, first, count, out))
+        return out
+
+    def run_paths(self, request: PriceRequest, first: int = 0, count: Optional[int] = None) -> list:
+        n = request.config.paths - first if count is None else count
+        return [record_to_dict(r) for r in self.run_paths_raw(request, first, n)][:n]
+
+    def reconstruct_path(self, request: PriceRequest, path_id: int) -> dict:
+        """explain.rs:319-333: one path re-simulated from its identity alone."""
+        if path_id >= request.config.paths:
+            raise RigaError("path_out_of_range",
+                            f"path_id {path_id} is outside the configured path count {request.config.paths}")
+        return record_to_dict(self.run_paths_raw(request, path_id, 1)[0])
+
+    def query_worst_percentile(self, request: PriceRequest, percentile: float, max_sample: int) -> dict:
+        """explain.rs:336-372"""
+        if not (0.0 <= percentile <= 1.0):
+            raise RigaError("invalid_percentile", "percentile must be within [0, 1]")
+        recs = [record_to_dict(r) for r in self.run_paths_raw(request)]
+        recs.sort(key=lambda r: r["worst_final"])
+        total = len(recs)
+        selected = math.ceil(total * percentile)
+        return {"percentile": percentile,
+                "threshold_worst_final": recs[selected - 1]["worst_final"] if selected else 0.0,
+                "selected": selected, "total": total, "sample": recs[: min(selected, max_sample)]}
+
+
+_default: Optional[Engine] = None
+_lock = threading.Lock()
+
+
+def default_engine() -> Engine:
+    global _default
+    with _lock:
+        if _default is None:
+            _default = Engine(0)
+        return _default
+
+
+def price_put_leg(request: PriceRequest) -> dict:
+    return default_engine().price_put_leg(request)
+
+
+def price_risk_batch(request: PriceRequest, config=None):
+    return default_engine().price_risk_batch_raw(request, config)

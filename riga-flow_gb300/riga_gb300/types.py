@@ -167,6 +167,7 @@ class EngineOptions:
     precision: int = abi.PRECISION_FP64_PARITY
     dim_mode: int = abi.DIM_WRAP_REFERENCE
     lv_grid_x: int = 0
+    first_path: int = 0
 
 
 @dataclass
@@ -259,6 +260,7 @@ class AbiRequest:
         cfg.qmc_dimension = c.variance_reduction.dimension
         cfg.scrambler, cfg.precision, cfg.dim_mode, cfg.lv_grid_x = (
             o.scrambler, o.precision, o.dim_mode, o.lv_grid_x)
+        cfg.first_path = o.first_path
 
         r = abi.PriceRequest()
         r.trade = tr

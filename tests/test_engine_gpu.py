@@ -1,0 +1,323 @@
+"""GPU parity tests: the CUDA engine, called through the C ABI, against the CPU oracle.
+
+Bars (each written into the assertion that checks it):
+* FP64 parity mode — per path, the knock-out step, the qualifying-coupon count and the number of
+  paid periods equal the oracle's exactly; discounted payoffs agree within 1e-12 relative; the
+  aggregate PriceResult within the reference's own 1e-12 (crates/riga-engine/src/lib.rs:453).
+* FP32 production mode — every price within min(0.1 × MC standard error, 1bp of notional) of the
+  FP64 oracle on the same scrambled points; the same bound for the CRN bump differences.
+"""
+from __future__ import annotations
+
+import copy
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import json_close
+from riga_gb300 import abi, gpu, workloads
+from riga_gb300.build import build_library
+from riga_gb300.engine import Engine
+from riga_gb300.types import EngineOptions, VarianceReduction, result_to_json
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    build_library()
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+def _lane(req, kind, dim=None, **opts):
+    r = copy.deepcopy(req)
+    r.config.variance_reduction = VarianceReduction(kind, dim if dim is not None else r.trade.steps * len(r.market.spots))
+    r.options = EngineOptions(**opts)
+    return r
+
+
+def _termsheet(termsheet1, paths=2048, kind="sobol", **opts):
+    r = _lane(termsheet1.request, kind, **opts)
+    r.config.paths = paths
+    return r
+
+
+def assert_records_match(gpu_recs, cpu_recs, rel=1e-12):
+    mism = []
+    for g, c in zip(gpu_recs, cpu_recs):
+        assert g.path_id == c.path_id
+        if (g.ko_step, g.qualified_steps, g.paid_periods, g.ki_hit) != (c.ko_step, c.qualified_steps, c.paid_periods, c.ki_hit):
+            mism.append((g.path_id, (g.ko_step, c.ko_step), (g.qualified_steps, c.qualified_steps),
+                         (g.paid_periods, c.paid_periods), g.worst_final))
+            continue
+        for f in ("pv", "put_payoff", "coupon_pv", "memory_coupon_pv", "funding", "worst_final"):
+            a, b = getattr(g, f), getattr(c, f)
+            assert abs(a - b) <= rel * max(abs(b), 1e-300) or a == b, (g.path_id, f, a, b)
+    assert mism == [], f"event mismatches (path, ko, qualified, paid, worst): {mism[:5]}"
+
+
+# ------------------------------------------------------------------ device ---------------------
+def test_device_is_a_gb300(engine):
+    """gpu.rs:500-512 and lib.rs:618-629"""
+    gpu.ensure_available()
+    assert gpu.arch() == "sm_103"
+    assert gpu.device_name()
+
+
+# ------------------------------------------------------------------ FP64 parity ---------------
+@pytest.mark.parametrize("kind,extra", [("sobol", {}), ("halton", {}),
+                                        ("sobol", {"scrambler": abi.SCRAMBLE_DIGITAL_SHIFT,
+                                                   "dim_mode": abi.DIM_FULL})])
+def test_fp64_parity_termsheet1_per_path(engine, termsheet1, kind, extra):
+    """Reference two-asset Dupire-LV trade on the QMC lanes: per-path events exact, payoffs to
+    1e-12 relative (note.rs:81-259, explain.rs:90-316)."""
+    r = _termsheet(termsheet1, 2048, kind, **extra)
+    g = engine.run_paths_raw(r, 0, 2048)
+    c = O.run_paths(r, 0, 2048)
+    assert_records_match(g, c)
+
+
+@pytest.mark.parametrize("kind", ["sobol", "halton"])
+def test_fp64_parity_termsheet1_price_result(engine, termsheet1, kind):
+    """The whole PriceResult within the reference's 1e-12 (lib.rs:430-457)."""
+    r = _termsheet(termsheet1, 4096, kind)
+    r.config.trace_level = "aggregated"
+    got = result_to_json(engine.price_raw(r), r)
+    exp = result_to_json(O.price_put_leg(r, threads=1), r)
+    assert json_close(got, exp, tol=1e-12) == []
+
+
+def test_fp64_parity_three_asset_flat_vol(engine):
+    """The 3-asset plain configuration (756 steps, digital shift) at 2048 paths."""
+    r = workloads.plain3(2048)
+    assert_records_match(engine.run_paths_raw(r, 0, 2048), O.run_paths(r, 0, 2048))
+    got = result_to_json(engine.price_raw(r), r)
+    exp = result_to_json(O.price_put_leg(r, threads=8), r)
+    assert json_close(got, exp, tol=1e-12) == []
+
+
+def test_fp64_parity_three_asset_local_vol(engine):
+    """The 3-asset Dupire configuration (SVI smiles, 40-point grid) at 512 paths."""
+    r = workloads.lv3(512, fp32=False)
+    assert_records_match(engine.run_paths_raw(r, 0, 512), O.run_paths(r, 0, 512))
+
+
+@pytest.mark.parametrize("n", [1, 4, 5])
+def test_fp64_parity_other_asset_counts(engine, n):
+    r = workloads.plain3(512, steps=126)
+    r.trade.initial_spots = [100.0] * n
+    r.market.spots = [100.0 + 3 * i for i in range(n)]
+    r.market.vols = [0.2 + 0.03 * i for i in range(n)]
+    r.market.dividend_yields = [0.01] * n
+    r.market.correlation = [[1.0 if i == j else 0.3 for j in range(n)] for i in range(n)]
+    r.config.variance_reduction = VarianceReduction("sobol", n * 126)
+    assert_records_match(engine.run_paths_raw(r, 0, 512), O.run_paths(r, 0, 512))
+
+
+def test_path_ranges_shard_exactly(engine):
+    """Points come from the path index alone (qmc.rs:269-290): records of [a, b) ∪ [b, c) equal
+    the records of [a, c) — the sharding property of the multi-rank path."""
+    r = workloads.plain3(4096, steps=63)
+    whole = engine.run_paths_raw(r, 0, 4096)
+    lo = engine.run_paths_raw(r, 0, 1500)
+    hi = engine.run_paths_raw(r, 1500, 2596)
+    for a, b in zip(list(lo) + list(hi), whole):
+        assert (a.path_id, a.pv, a.ko_step) == (b.path_id, b.pv, b.ko_step)
+
+
+def test_repeated_launches_are_bit_identical(engine):
+    r = workloads.plain3(1 << 14, steps=126)
+    a = engine.price_raw(r)
+    b = engine.price_raw(r)
+    assert bytes(a) == bytes(b)
+    r.options = workloads.production_options()
+    assert bytes(engine.price_raw(r)) == bytes(engine.price_raw(r))
+
+
+def test_ko_gates_the_put_but_not_ki(engine, termsheet1):
+    """note.rs:381-401"""
+    r = _termsheet(termsheet1, 1024)
+    r.trade.knock_out_barrier = None
+    e = copy.deepcopy(r)
+    e.trade.knock_out_barrier = 1.0e-6
+    a, b = engine.price_raw(r), engine.price_raw(e)
+    assert a.ki_probability == b.ki_probability
+    assert a.legs.down_and_in_put > 0.0 and b.legs.down_and_in_put == 0.0
+
+
+# ------------------------------------------------------------------ FP32 production ------------
+def _fp32_bound(res64: abi.PriceResult) -> float:
+    return min(0.1 * res64.mc_error, 1e-4)
+
+
+def test_fp32_matches_fp64_within_a_tenth_of_the_standard_error(engine):
+    r = workloads.plain3(1 << 14)
+    r64 = copy.deepcopy(r)
+    r.options = workloads.production_options()
+    res32 = engine.price_raw(r)
+    res64 = O.price_put_leg(r64, threads=8)
+    bound = _fp32_bound(res64)
+    assert abs(res32.pv - res64.pv) <= bound, (res32.pv, res64.pv, bound)
+    assert abs(res32.legs.down_and_in_put - res64.legs.down_and_in_put) <= bound
+    assert abs(res32.ki_probability - res64.ki_probability) <= 2.0 / r.config.paths
+
+
+def test_fp32_crn_batch_matches_fp64_scenarios(engine):
+    """16 scenarios (base + 15 CRN bumps) of the 3-asset Dupire configuration in one fused FP32
+    launch against the FP64 oracle priced scenario by scenario."""
+    r = workloads.lv3(2048, steps=126, fp32=True)
+    scen = workloads.crn15_scenarios(r)
+    got = engine.price_scenarios_raw(r, [(m, s) for _, m, s in scen])
+    r64 = workloads.lv3(2048, steps=126, fp32=False)
+    exp = O.price_scenarios(r64, [(m, s) for _, m, s in scen], threads=8)
+    for (label, _, _), g, e in zip(scen, got, exp):
+        bound = _fp32_bound(e)
+        assert abs(g.pv - e.pv) <= bound, (label, g.pv, e.pv, bound)
+    # the CRN differences (delta numerators) keep the same bound
+    for i in (1, 3, 5):
+        dg, de = got[i].pv - got[i + 1].pv, exp[i].pv - exp[i + 1].pv
+        assert abs(dg - de) <= _fp32_bound(exp[0]), (i, dg, de)
+
+
+def test_fp64_risk_batch_matches_the_oracle(engine, termsheet1):
+    """crates/riga-risk/src/lib.rs:573-626 on the device: every scenario price within 1e-12."""
+    r = _termsheet(termsheet1, 512)
+    cfg = abi.CentralDifferenceConfig(0.01, 0.01, 1e-4, 0.01, abi.CRN)
+    g = engine.price_risk_batch_raw(r, cfg)
+    c = O.price_risk_batch(r, cfg, threads=8)
+    assert g.scenario_count == c.scenario_count == 13
+    for f in ("rate_up_pv", "rate_down_pv", "correlation_up_pv", "correlation_down_pv"):
+        assert abs(getattr(g, f) - getattr(c, f)) <= 1e-12, f
+    for i in range(2):
+        for f in ("spot_up_pv", "spot_down_pv", "vol_up_pv", "vol_down_pv"):
+            assert abs(getattr(g.assets[i], f) - getattr(c.assets[i], f)) <= 1e-12, (i, f)
+    assert abs(g.base.pv - c.base.pv) <= 1e-12
+
+
+# ------------------------------------------------------------------ errors --------------------
+def test_invalid_requests_keep_the_reference_error_codes(engine, termsheet1):
+    """lib.rs:595-607 and the validate() branches (lib.rs:209-321) through the C ABI."""
+    def code(mut, kind="sobol"):
+        r = _termsheet(termsheet1, 64, kind)
+        mut(r)
+        with pytest.raises(abi.RigaError) as e:
+            engine.price_raw(r)
+        return e.value.code
+
+    def corr(r):
+        r.market.correlation = [[1.0, 2.0], [2.0, 1.0]]
+    assert code(corr) == "invalid_market"
+    assert code(lambda r: setattr(r, "as_of", "")) == "missing_as_of"
+    assert code(lambda r: setattr(r.config, "paths", 0)) == "invalid_paths"
+    assert code(lambda r: setattr(r.trade, "steps", 0)) == "invalid_schedule"
+    assert code(lambda r: setattr(r.market, "spots", [1.0])) == "invalid_market_shape"
+    assert code(lambda r: None, kind="none") == "unsupported"
+    with pytest.raises(abi.RigaError) as e:
+        engine.run_paths_raw(_termsheet(termsheet1, 64), 60, 10)
+    assert e.value.code == "path_out_of_range"
+
+
+# ------------------------------------------------------------------ gpu backend drop-ins --------
+def test_gpu_worst_of_is_bit_identical_to_scalar():
+    """gpu.rs:595-621: the same LCG inputs, compared bit for bit with the scalar minimum."""
+    n = 4096
+    seed = 0x12345678
+    a = np.empty(n, np.float32)
+    b = np.empty(n, np.float32)
+    for i in range(n):
+        seed = (seed * 1664525 + 1013904223) & 0xFFFFFFFF
+        a[i] = np.float32(seed >> 8) / np.float32(1 << 24) * np.float32(1.8) + np.float32(0.2)
+        seed = (seed * 1664525 + 1013904223) & 0xFFFFFFFF
+        b[i] = np.float32(seed >> 8) / np.float32(1 << 24) * np.float32(1.8) + np.float32(0.2)
+    out = gpu.worst_of(a, b)
+    assert np.array_equal(out.view(np.uint32), np.minimum(a, b).view(np.uint32))
+    w = gpu.resident_worst_of(a, b)
+    w.reduce()
+    assert np.array_equal(w.download(), out)
+
+
+def _lv_inputs(termsheet1, paths=2048):
+    req = termsheet1.request
+    steps = req.trade.steps
+    dt = np.float32(req.trade.maturity_years / steps)
+    gx = 96
+    rows = np.zeros(2 * steps * gx, np.float32)
+    axes = []
+    for f in range(2):
+        t_axis, log_s, v, surf = O.lv_calibrate(req.local_vol[f], req.market.spots[f], req.market.risk_free_rate)
+        for s in range(steps):
+            t = s * float(dt)
+            tc = min(max(t, t_axis[0]), t_axis[-1])
+            i = 0
+            while i + 1 < len(t_axis) - 1 and tc > t_axis[i + 1]:
+                i += 1
+            w = (tc - t_axis[i]) / (t_axis[i + 1] - t_axis[i])
+            rows[(f * steps + s) * gx:(f * steps + s + 1) * gx] = [(1 - w) * v[i][j] + w * v[i + 1][j] for j in range(gx)]
+        axes += log_s
+    seed = 0x9E3779B9
+    normals = np.empty(paths * steps * 2, np.float32)
+    for i in range(normals.size):
+        seed = (seed * 1664525 + 1013904223) & 0xFFFFFFFF
+        normals[i] = (np.float32(seed >> 8) / np.float32(1 << 24) - np.float32(0.5)) * np.float32(2.0)
+    return normals, rows, np.asarray(axes, np.float32), steps, float(dt)
+
+
+def _lv_reference(normals, rows, axes, s0, refs, bar, paths, steps, dt, rate, divs):
+    """numpy float32 restatement of lv_propagate (gpu.rs:37-75)."""
+    gx = axes.size // 2
+    f32 = np.float32
+    ls = np.array([np.log(f32(s0[0])), np.log(f32(s0[1]))], f32)
+    ls = np.tile(ls, (paths, 1))
+    nz = normals.reshape(paths, steps, 2)
+    ko = np.full(paths, -1, np.int32)
+    sq = np.sqrt(f32(dt))
+    for s in range(steps):
+        sig = []
+        for f in range(2):
+            lo, hi = axes[f * gx], axes[f * gx + gx - 1]
+            x = np.clip((ls[:, f] - lo) * (f32(1) / (hi - lo)) * f32(gx - 1), 0, gx - 1)
+            j = np.minimum(x.astype(np.int32), gx - 2)
+            w = x - j.astype(f32)
+            row = rows[(f * steps + s) * gx:(f * steps + s + 1) * gx]
+            sig.append(row[j] * (f32(1) - w) + row[j + 1] * w)
+        for f in range(2):
+            ls[:, f] += (f32(rate) - f32(divs[f]) - f32(0.5) * sig[f] * sig[f]) * f32(dt) + sig[f] * sq * nz[:, s, f]
+        hit = (ko < 0) & (np.exp(ls[:, 0]) / f32(refs[0]) >= f32(bar)) & (np.exp(ls[:, 1]) / f32(refs[1]) >= f32(bar))
+        ko[hit] = s
+    return np.exp(ls).reshape(-1), ko
+
+
+def test_lv_terminal_spots_matches_the_float32_restatement(termsheet1):
+    normals, rows, axes, steps, dt = _lv_inputs(termsheet1, 1024)
+    req = termsheet1.request
+    s0 = np.asarray(req.market.spots, np.float32)
+    refs = np.asarray(req.trade.initial_spots, np.float32)
+    divs = np.asarray(req.market.dividend_yields, np.float32)
+    out, ko = gpu.lv_terminal_spots(normals, rows, axes, s0, refs, 1.1, 1024, steps, dt,
+                                    req.market.risk_free_rate, divs)
+    ref_out, ref_ko = _lv_reference(normals, rows, axes, s0, refs, 1.1, 1024, steps, dt,
+                                    req.market.risk_free_rate, divs)
+    assert np.max(np.abs(out - ref_out) / ref_out) < 1e-4
+    assert np.mean(ko == ref_ko) > 0.995
+
+
+def test_resident_lv_multi_scenario_matches_per_call(termsheet1):
+    """gpu.rs:625-697: each resident run is bit-identical to a fresh per-call run."""
+    normals, rows, axes, steps, dt = _lv_inputs(termsheet1, 2048)
+    req = termsheet1.request
+    base = np.asarray(req.market.spots, np.float32)
+    refs = np.asarray(req.trade.initial_spots, np.float32)
+    divs = np.asarray(req.market.dividend_yields, np.float32)
+    rate = np.float32(req.market.risk_free_rate)
+    res = gpu.resident_lv(normals, rows, axes, 2048, steps, dt)
+    for bump in (np.float32(1.0), np.float32(1.005), np.float32(0.99)):
+        s0 = base * bump
+        res.run(s0, refs, 1.1, rate, divs)
+        rt, rk = res.download()
+        t, k = gpu.lv_terminal_spots(normals, rows, axes, s0, refs, 1.1, 2048, steps, dt, rate, divs)
+        assert np.array_equal(rt.view(np.uint32), t.view(np.uint32))
+        assert np.array_equal(rk, k)
