@@ -60,12 +60,31 @@ def lib() -> C.CDLL:
             "or_price_risk_batch": (i32, [P(abi.PriceRequest), P(abi.CentralDifferenceConfig),
                                           i32, P(abi.BatchRiskReport)]),
             "or_last_error": (C.c_char_p, []),
+            "or_set_portable_math": (None, [i32]),
+            "or_pexp": (d, [d]),
+            "or_plog": (d, [d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
         _lib = L
     return _lib
+
+
+def set_portable_math(on: bool) -> None:
+    """Select the portable deterministic exp/log (bit-identical to the GPU parity kernel) or the
+    platform libm (default; reproduces the reference golden bit for bit)."""
+    lib().or_set_portable_math(1 if on else 0)
+
+
+class portable_math:
+    """Context manager: run the oracle with the portable exp/log."""
+
+    def __enter__(self):
+        set_portable_math(True)
+
+    def __exit__(self, *exc):
+        set_portable_math(False)
 
 
 class OracleError(abi.RigaError):

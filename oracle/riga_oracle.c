@@ -35,6 +35,65 @@ static int32_t fail(int32_t status, const char* fmt, ...) {
 
 const char* or_last_error(void) { return g_err; }
 
+
+/* ============================================================ elementary functions =========== */
+/* Two modes.  Default: the platform libm, which is what the reference's Rust f64::exp/ln call —
+ * the golden vector is reproduced bit for bit in this mode.  Portable: a deterministic exp/log
+ * built only from IEEE-754 +, -, *, / and exact power-of-two scaling (Cody–Waite reduction by a
+ * split ln 2 and the degree-13 Taylor polynomial; log by the artanh series through s^23), the
+ * same published method and coefficients the engine's FP64 parity kernel uses, so the two agree
+ * bit for bit.  Compiled with -ffp-contract=off. */
+static int g_portable = 0;
+void or_set_portable_math(int on) { g_portable = on != 0; }
+
+static double bits_to_double(uint64_t u) { double x; memcpy(&x, &u, sizeof x); return x; }
+static uint64_t double_to_bits(double x) { uint64_t u; memcpy(&u, &x, sizeof u); return u; }
+static double pow2i(int k) { return bits_to_double((uint64_t)(k + 1023) << 52); }
+
+double or_pexp(double x) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return INFINITY;
+  if (x < -745.1332191019412) return 0.0;
+  const double hi = 0x1.62e42ffp-1, lo = -0x1.718432a1b0e26p-35;
+  double k = floor(x * 0x1.71547652b82fep+0 + 0.5);
+  double r = (x + -(k * hi)) + -(k * lo);
+  static const double c[14] = {0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26,
+                               0x1.27e4fb7789f5cp-22, 0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16,
+                               0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7,
+                               0x1.5555555555555p-5,  0x1.5555555555555p-3,  0.5, 1.0, 1.0};
+  double p = c[0];
+  for (int i = 1; i < 14; ++i) p = p * r + c[i];
+  int ki = (int)k;
+  if (ki >= -1022) return ki <= 1023 ? p * pow2i(ki) : (p * pow2i(1023)) * pow2i(ki - 1023);
+  return (p * pow2i(ki + 54)) * pow2i(-54);
+}
+
+double or_plog(double x) {
+  if (x != x) return x;
+  if (x < 0.0) return NAN;
+  if (x == 0.0) return -INFINITY;
+  if (x == INFINITY) return x;
+  int e = 0;
+  if (x < 0x1p-1022) { x = x * 0x1p54; e = -54; }
+  uint64_t b = double_to_bits(x);
+  e += (int)((b >> 52) & 0x7ff) - 1023;
+  double m = bits_to_double((b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
+  if (m > 0x1.6a09e667f3bcdp+0) { m = m * 0.5; e += 1; }
+  double f = m - 1.0, s = f / (2.0 + f), z = s * s;
+  static const double c[11] = {0x1.642c8590b2164p-5, 0x1.8618618618618p-5, 0x1.af286bca1af28p-5,
+                               0x1.e1e1e1e1e1e1ep-5, 0x1.1111111111111p-4, 0x1.3b13b13b13b14p-4,
+                               0x1.745d1745d1746p-4, 0x1.c71c71c71c71cp-4, 0x1.2492492492492p-3,
+                               0x1.999999999999ap-3, 0x1.5555555555555p-2};
+  double R = c[0];
+  for (int i = 1; i < 11; ++i) R = R * z + c[i];
+  R = R * z;
+  double lm = 2.0 * (s + s * R), ed = (double)e;
+  return ed * 0x1.62e42ffp-1 + (lm + ed * -0x1.718432a1b0e26p-35);
+}
+
+#define OEXP(x) (g_portable ? or_pexp(x) : exp(x))
+#define OLOG(x) (g_portable ? or_plog(x) : log(x))
+
 /* ============================================================ qmc.rs ========================= */
 
 /* Acklam's rational inverse normal CDF, crates/riga-engine/src/qmc.rs:37-91.  The coefficients
@@ -52,7 +111,7 @@ double or_probit(double p) {
   if (p >= 1.0) return INFINITY;
   const double plow = 0.02425, phigh = 1.0 - plow;
   if (p < plow) {
-    double q = sqrt(-2.0 * log(p));
+    double q = sqrt(-2.0 * OLOG(p));
     return (((((C[0] * q + C[1]) * q + C[2]) * q + C[3]) * q + C[4]) * q + C[5]) /
            ((((D[0] * q + D[1]) * q + D[2]) * q + D[3]) * q + 1.0);
   } else if (p <= phigh) {
@@ -60,7 +119,7 @@ double or_probit(double p) {
     return (((((A[0] * r + A[1]) * r + A[2]) * r + A[3]) * r + A[4]) * r + A[5]) * q /
            (((((B[0] * r + B[1]) * r + B[2]) * r + B[3]) * r + B[4]) * r + 1.0);
   } else {
-    double q = sqrt(-2.0 * log(1.0 - p));
+    double q = sqrt(-2.0 * OLOG(1.0 - p));
     return -(((((C[0] * q + C[1]) * q + C[2]) * q + C[3]) * q + C[4]) * q + C[5]) /
            ((((D[0] * q + D[1]) * q + D[2]) * q + D[3]) * q + 1.0);
   }
@@ -428,7 +487,7 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   int nt = grid->n_maturities, nk = grid->n_strikes;
   const double* K = grid->strikes;
   double s_min = K[0] * 0.55, s_max = K[nk - 1] * 1.05;
-  double log_lo = log(s_min > 1e-6 ? s_min : 1e-6), log_hi = log(s_max > 1e-6 ? s_max : 1e-6);
+  double log_lo = OLOG(s_min > 1e-6 ? s_min : 1e-6), log_hi = OLOG(s_max > 1e-6 ? s_max : 1e-6);
   out->n_t = nt;
   out->gx = gx;
   out->t_axis = (double*)malloc(sizeof(double) * (size_t)nt);
@@ -438,7 +497,7 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   double* s_axis = (double*)malloc(sizeof(double) * (size_t)gx);
   for (int i = 0; i < gx; ++i) {
     out->log_s[i] = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
-    s_axis[i] = exp(out->log_s[i]);
+    s_axis[i] = OEXP(out->log_s[i]);
   }
   size_t cells = (size_t)nt * (size_t)gx;
   double *w = (double*)malloc(sizeof(double) * cells), *wx = (double*)malloc(sizeof(double) * cells),
@@ -446,13 +505,13 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   double *xj = (double*)malloc(sizeof(double) * (size_t)nk), *y2 = (double*)malloc(sizeof(double) * (size_t)nk);
   for (int k = 0; k < nt; ++k) {
     double tk = grid->maturities_years[k];
-    double forward = spot * exp(rate * tk);
-    for (int j = 0; j < nk; ++j) xj[j] = log(K[j] / forward);
+    double forward = spot * OEXP(rate * tk);
+    for (int j = 0; j < nk; ++j) xj[j] = OLOG(K[j] / forward);
     const double* y = grid->vols + (size_t)k * nk;
     natural_second_derivatives(xj, y, nk, y2);
     double x_lo = xj[0], x_hi = xj[nk - 1];
     for (int i = 0; i < gx; ++i) {
-      double xd = log(s_axis[i] / forward);
+      double xd = OLOG(s_axis[i] / forward);
       xd = xd < x_lo ? x_lo : (xd > x_hi ? x_hi : xd);
       double sg, s1, s2;
       if (nk >= 2) {
@@ -502,7 +561,7 @@ void or_lv_free(or_lv_surface* s) {
 
 /* DupireLocalVol::sigma, crates/riga-market/src/lib.rs:301-343 */
 double or_lv_sigma(const or_lv_surface* s, double t, double spot) {
-  double x = log(spot > 1e-12 ? spot : 1e-12);
+  double x = OLOG(spot > 1e-12 ? spot : 1e-12);
   int n = s->gx, lo, hi;
   if (x <= s->log_s[0]) { lo = 0; hi = 0; }
   else if (x >= s->log_s[n - 1]) { lo = n - 1; hi = n - 1; }
@@ -918,7 +977,7 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
     for (int f = 0; f < n; ++f) {
       double vol = m->has_lv ? or_lv_sigma(&m->lv[f], (double)step * dt, spots[f]) : m->vols[f];
       double drift = (m->rate - m->q[f] - 0.5 * vol * vol) * dt;
-      spots[f] *= exp(drift + vol * sqrt(dt) * ws->incr[(size_t)f * T + step]);
+      spots[f] *= OEXP(drift + vol * sqrt(dt) * ws->incr[(size_t)f * T + step]);
     }
     double worst = spots[0] / m->init[0];
     for (int f = 1; f < n; ++f) worst = fmin(worst, spots[f] / m->init[f]);
@@ -944,7 +1003,7 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
       double due = (period == 0 && m->fixed_first) ? m->coupon_rate : accrual;
       double carry = due > 0.0 ? unpaid : 0.0;
       if (due + carry > 0.0) {
-        double df = exp(-m->rate * time);
+        double df = OEXP(-m->rate * time);
         coupon_pv += due * df;
         memory_pv += carry * df;
         received = 1;
@@ -961,7 +1020,7 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
     if (step + 1 == T || next_period != period) {
       double due = (period == 0 && m->fixed_first) ? m->coupon_rate : accrual;
       if (due > 0.0) {
-        double df = exp(-m->rate * time);
+        double df = OEXP(-m->rate * time);
         coupon_pv += due * df;
         memory_pv += unpaid * df;
         received = 1;
@@ -973,10 +1032,10 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
     }
   }
   /* path close, note.rs:221-258 */
-  double funding = exp(-m->rate * redemption_time);
+  double funding = OEXP(-m->rate * redemption_time);
   int hit_ki = final_worst <= m->ki;
   int put_eligible = hit_ki && !ko;
-  double put = put_eligible ? fmax(m->strike - final_worst, 0.0) * exp(-m->rate * m->maturity) : 0.0;
+  double put = put_eligible ? fmax(m->strike - final_worst, 0.0) * OEXP(-m->rate * m->maturity) : 0.0;
   double coupon_nominal = coupon_pv + memory_pv;
   o->worst_final = final_worst;
   o->redemption_time = redemption_time;

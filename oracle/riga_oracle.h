@@ -23,6 +23,12 @@
 extern "C" {
 #endif
 
+/* --- elementary functions: libm (default, reproduces the golden) or the portable deterministic
+ * exp/log the engine's FP64 parity kernel uses (bit-identical on CPU and GPU) --- */
+void or_set_portable_math(int on);
+double or_pexp(double x);
+double or_plog(double x);
+
 /* --- qmc.rs restatement --- */
 double or_probit(double p);
 double or_radical_inverse(uint64_t index, uint32_t base);

@@ -404,8 +404,8 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
       }
       // Dupire log-strike axis [0.55 K_min, 1.05 K_max] (riga-market/src/lib.rs:217-224)
       double s_min = g.strikes[0] * 0.55, s_max = g.strikes[g.n_strikes - 1] * 1.05;
-      P.asset_log_lo[f] = std::log(std::max(s_min, 1e-6));
-      P.asset_log_hi[f] = std::log(std::max(s_max, 1e-6));
+      P.asset_log_lo[f] = rg_log64(std::max(s_min, 1e-6));
+      P.asset_log_hi[f] = rg_log64(std::max(s_max, 1e-6));
     }
   }
 
@@ -447,9 +447,9 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
     // discount factors exp(-r * (step + 1) dt) and exp(-r * T) (note.rs:189, 210, 221, 238)
     for (int64_t s = 0; s < T; ++s) {
       double time = (double)(s + 1) * tr.dt;
-      P.df[size_t(i) * T + s] = std::exp(-m.risk_free_rate * time);
+      P.df[size_t(i) * T + s] = rg_exp64(-m.risk_free_rate * time);
     }
-    P.df_mat[i] = std::exp(-m.risk_free_rate * t.maturity_years);
+    P.df_mat[i] = rg_exp64(-m.risk_free_rate * t.maturity_years);
   }
   P.n_surf = (int)P.surfaces.size();
   // surface row offsets in the packed local-vol tables

@@ -8,7 +8,8 @@
 // node schedule (which preorder index and standard deviation each step consumes) is a host table
 // shared by every thread, so the traversal is warp-uniform.
 //
-// Compiled with -fmad=false: products and sums round separately, as in the reference.
+// Compiled with -fmad=false: products and sums round separately, as in the reference; exp and
+// log are the deterministic rg_exp64/rg_log64 shared with the host tables.
 #include "rg_internal.h"
 
 namespace rg {
@@ -16,7 +17,7 @@ namespace rg {
 // DupireLocalVol::sigma with a precomputed tenor row/weight (riga-market/src/lib.rs:305-343).
 __device__ __forceinline__ double lv_sigma64(const double* __restrict__ v, const double* __restrict__ ls,
                                              int gx, int ti, int ti1, double wt, double spot) {
-  double x = log(spot > 1e-12 ? spot : 1e-12);
+  double x = rg_log64(spot > 1e-12 ? spot : 1e-12);
   int lo, hi;
   if (x <= __ldg(ls)) {
     lo = 0; hi = 0;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables t
                                      tix[f].y, tw[f], spots[f])
                         : vol[f];
           double drift = (rate - qd[f] - 0.5 * v * v) * dt;
-          spots[f] *= exp(drift + v * sqrt_dt * shock[f]);
+          spots[f] *= rg_exp64(drift + v * sqrt_dt * shock[f]);
         }
         double worst = spots[0] / tr.init[0];
 #pragma unroll

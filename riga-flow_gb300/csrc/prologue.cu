@@ -7,7 +7,8 @@
 // * cholesky_kernel: one thread per scenario.  Jacobi minimum eigenvalue, diagonal-loading PSD
 //   clamp and Cholesky–Banachiewicz (crates/riga-market/src/correlation.rs:95-168), in place on
 //   the scenario's correlation block.
-// Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's.
+// Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's; exp and log are
+// the deterministic rg_exp64/rg_log64, so the grid is bit-identical to a host calibration.
 #include "rg_internal.h"
 
 namespace rg {
@@ -74,18 +75,18 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
   double* tmp = y2 + nt * nk;                 // 3 * nt * nk (h, cp, dp)
   double* yv = tmp + 3 * nt * nk;             // nt * nk shifted implied vols
   const double s_min = J.strikes[0] * 0.55, s_max = J.strikes[nk - 1] * 1.05;
-  const double log_lo = log(s_min > 1e-6 ? s_min : 1e-6), log_hi = log(s_max > 1e-6 ? s_max : 1e-6);
+  const double log_lo = rg_log64(s_min > 1e-6 ? s_min : 1e-6), log_hi = rg_log64(s_max > 1e-6 ? s_max : 1e-6);
   for (int i = threadIdx.x; i < gx; i += blockDim.x) {
     double ls = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
     J.out_logs[i] = ls;
-    s_axis[i] = exp(ls);
+    s_axis[i] = rg_exp64(ls);
   }
   for (int i = threadIdx.x; i < nt * nk; i += blockDim.x) yv[i] = J.vols[i] + J.shift;
   __syncthreads();
   // one thread per tenor: log-moneyness nodes and the spline solve
   for (int k = threadIdx.x; k < nt; k += blockDim.x) {
-    double forward = J.spot * exp(J.rate * J.mats[k]);
-    for (int j = 0; j < nk; ++j) xj[k * nk + j] = log(J.strikes[j] / forward);
+    double forward = J.spot * rg_exp64(J.rate * J.mats[k]);
+    for (int j = 0; j < nk; ++j) xj[k * nk + j] = rg_log64(J.strikes[j] / forward);
     spline_y2(xj + k * nk, yv + k * nk, nk, y2 + k * nk, tmp + 3 * k * nk, tmp + 3 * k * nk + nk,
               tmp + 3 * k * nk + 2 * nk);
   }
@@ -93,10 +94,10 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
   for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
     int k = c / gx, i = c % gx;
     double tk = J.mats[k];
-    double forward = J.spot * exp(J.rate * tk);
+    double forward = J.spot * rg_exp64(J.rate * tk);
     const double* xk = xj + k * nk;
     double x_lo = xk[0], x_hi = xk[nk - 1];
-    double xd = log(s_axis[i] / forward);
+    double xd = rg_log64(s_axis[i] / forward);
     xd = xd < x_lo ? x_lo : (xd > x_hi ? x_hi : xd);
     double sg, s1, s2;
     if (nk >= 2) {

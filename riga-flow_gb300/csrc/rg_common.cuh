@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "../../include/riga_gb300.h"
+#include "rg_math.cuh"
 
 #define RG_NMAX RG_MAX_ASSETS
 #define RG_ACC 16          // FP64 accumulators per (block, scenario)
@@ -138,7 +139,7 @@ __device__ __forceinline__ double rg_probit64(double p) {
   if (p >= 1.0) return INFINITY;
   const double plow = 0.02425, phigh = 1.0 - plow;
   if (p < plow) {
-    double q = sqrt(-2.0 * log(p));
+    double q = sqrt(-2.0 * rg_log64(p));
     return (((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
            ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
   } else if (p <= phigh) {
@@ -146,7 +147,7 @@ __device__ __forceinline__ double rg_probit64(double p) {
     return (((((a0 * r + a1) * r + a2) * r + a3) * r + a4) * r + a5) * q /
            (((((b0 * r + b1) * r + b2) * r + b3) * r + b4) * r + 1.0);
   } else {
-    double q = sqrt(-2.0 * log(1.0 - p));
+    double q = sqrt(-2.0 * rg_log64(1.0 - p));
     return -(((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
            ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
   }

@@ -17,7 +17,8 @@ from .abi import LIB_PATH, ROOT_DIR
 CSRC = ROOT_DIR / "csrc"
 BUILD = ROOT_DIR / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
 NO_FMA = {"phoenix64.cu", "prologue.cu"}
 

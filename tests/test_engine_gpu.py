@@ -4,6 +4,10 @@ Bars (each written into the assertion that checks it):
 * FP64 parity mode — per path, the knock-out step, the qualifying-coupon count and the number of
   paid periods equal the oracle's exactly; discounted payoffs agree within 1e-12 relative; the
   aggregate PriceResult within the reference's own 1e-12 (crates/riga-engine/src/lib.rs:453).
+  The oracle runs with the portable deterministic exp/log the parity kernel uses: the Dupire
+  calibration amplifies last-ulp differences between elementary-function libraries about a
+  million-fold, so both sides must share one exp/log (the oracle's libm mode is pinned to the
+  reference golden separately, in test_oracle.py).
 * FP32 production mode — every price within min(0.1 × MC standard error, 1bp of notional) of the
   FP64 oracle on the same scrambled points; the same bound for the CRN bump differences.
 """
@@ -33,6 +37,13 @@ def engine():
     e.close()
 
 
+@pytest.fixture(autouse=True)
+def portable_oracle():
+    O.set_portable_math(True)
+    yield
+    O.set_portable_math(False)
+
+
 def _lane(req, kind, dim=None, **opts):
     r = copy.deepcopy(req)
     r.config.variance_reduction = VarianceReduction(kind, dim if dim is not None else r.trade.steps * len(r.market.spots))
@@ -44,6 +55,16 @@ def _termsheet(termsheet1, paths=2048, kind="sobol", **opts):
     r = _lane(termsheet1.request, kind, **opts)
     r.config.paths = paths
     return r
+
+
+def max_rel_dev(gpu_recs, cpu_recs):
+    worst = 0.0
+    for g, c in zip(gpu_recs, cpu_recs):
+        for f in ("pv", "put_payoff", "coupon_pv", "memory_coupon_pv", "funding", "worst_final"):
+            a, b = getattr(g, f), getattr(c, f)
+            if a != b:
+                worst = max(worst, abs(a - b) / max(abs(b), 1e-300))
+    return worst
 
 
 def assert_records_match(gpu_recs, cpu_recs, rel=1e-12):
@@ -104,6 +125,20 @@ def test_fp64_parity_three_asset_local_vol(engine):
     """The 3-asset Dupire configuration (SVI smiles, 40-point grid) at 512 paths."""
     r = workloads.lv3(512, fp32=False)
     assert_records_match(engine.run_paths_raw(r, 0, 512), O.run_paths(r, 0, 512))
+
+
+@pytest.mark.parametrize("case", ["plain3", "lv3", "termsheet1"])
+def test_fp64_parity_is_bit_level(engine, termsheet1, case):
+    """Same algorithm, operation order and exp/log on both sides: per-path outputs agree to the
+    last bit (reported as the largest relative deviation, required to be 0)."""
+    if case == "plain3":
+        r = workloads.plain3(1024)
+    elif case == "lv3":
+        r = workloads.lv3(256, fp32=False)
+    else:
+        r = _termsheet(termsheet1, 1024)
+    dev = max_rel_dev(engine.run_paths_raw(r, 0, r.config.paths), O.run_paths(r, 0, r.config.paths))
+    assert dev == 0.0, dev
 
 
 @pytest.mark.parametrize("n", [1, 4, 5])

@@ -397,3 +397,42 @@ def test_risk_batch_follows_the_reference_scenario_set(termsheet1):
     with pytest.raises(abi.RigaError) as e:
         O.price_risk_batch(r, cfg_vol)
     assert e.value.code == "invalid_volatility_bump"
+
+
+# ----------------------------------------------------------------------- portable exp/log -----
+def _ulp_diff(a: float, b: float) -> int:
+    import struct
+
+    ia = struct.unpack("<q", struct.pack("<d", a))[0]
+    ib = struct.unpack("<q", struct.pack("<d", b))[0]
+    return abs(ia - ib)
+
+
+def test_portable_exp_log_are_within_two_ulp_of_libm():
+    """The deterministic exp/log shared with the GPU parity kernel (Cody–Waite + Taylor; artanh
+    series) stay within 2 ulp of the platform libm over the ranges the path uses."""
+    import random
+
+    rng = random.Random(7)
+    L = lib()
+    worst_e = worst_l = 0
+    for _ in range(100_000):
+        x = rng.uniform(-40.0, 10.0)
+        worst_e = max(worst_e, _ulp_diff(L.or_pexp(x), math.exp(x)))
+        y = math.exp(rng.uniform(-40.0, 12.0))
+        worst_l = max(worst_l, _ulp_diff(L.or_plog(y), math.log(y)) if abs(math.log(y)) > 1e-3 else 0)
+    assert worst_e <= 2 and worst_l <= 2, (worst_e, worst_l)
+    assert L.or_pexp(0.0) == 1.0 and L.or_plog(1.0) == 0.0
+    assert L.or_pexp(-800.0) == 0.0 and L.or_pexp(800.0) == math.inf
+    assert L.or_plog(0.0) == -math.inf and math.isnan(L.or_plog(-1.0))
+    for x in (1e-300, 5e-324, 2.0 ** -1030, 0.1, 0.5, 2.0, 1e300):
+        assert _ulp_diff(L.or_plog(x), math.log(x)) <= 2, x
+
+
+def test_portable_math_oracle_stays_close_to_the_libm_oracle(termsheet1, golden_result):
+    """Replacing libm's exp/log by the portable ones moves the golden PriceResult by far less than
+    the reference's 1e-12 tolerance would allow for the MC lane's aggregates."""
+    with O.portable_math():
+        res = O.price_put_leg(termsheet1.request, threads=1)
+    got = result_to_json(res, termsheet1.request)
+    assert json_close(got, golden_result, tol=1e-10) == []
