@@ -233,7 +233,7 @@ static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
   }
   size_t o_flags = pk.add(P.step_flags), o_per = pk.add(P.step_period), o_acc = pk.add(P.accr_inc);
   size_t o_noff = pk.add(P.node_off), o_nk = pk.add(P.node_k), o_nc = pk.add(P.node_c),
-         o_ncf = pk.add(P.node_cf);
+         o_ncf = pk.add(P.node_cf), o_nfr = pk.add(P.nf_row), o_nfs = pk.add(P.nf_shift);
   size_t o_ti = pk.add(P.lv_ti), o_tw = pk.add(P.lv_tw), o_twf = pk.add(P.lv_twf);
   size_t o_df = pk.add(P.df), o_dfm = pk.add(P.df_mat);
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
@@ -307,6 +307,8 @@ static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
   tb.node_k = reinterpret_cast<const int32_t*>(base + o_nk);
   tb.node_c = reinterpret_cast<const double*>(base + o_nc);
   tb.node_cf = reinterpret_cast<const float*>(base + o_ncf);
+  tb.nf_row = reinterpret_cast<const int32_t*>(base + o_nfr);
+  tb.nf_shift = reinterpret_cast<const uint32_t*>(base + o_nfs);
   tb.lv_ti = reinterpret_cast<const int2*>(base + o_ti);
   tb.lv_tw = reinterpret_cast<const double*>(base + o_tw);
   tb.lv_twf = reinterpret_cast<const float*>(base + o_twf);

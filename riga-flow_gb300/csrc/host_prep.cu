@@ -97,8 +97,10 @@ void validate_request(const rg_price_request* r) {
   if (c.lv_grid_x < 0 || c.lv_grid_x == 1 || c.lv_grid_x > 4096)
     raise(RG_ERR_INVALID_ARGUMENT, "lv_grid_x must be 0 or 2..4096");
   if (t.steps > (int64_t(1) << 22)) raise(RG_ERR_INVALID_SCHEDULE, "at most 2^22 steps are supported");
-  if (c.paths >= (uint64_t(1) << 32))
-    raise(RG_ERR_INVALID_PATHS, "the 32-bit Sobol net supports fewer than 2^32 paths");
+  // Sobol points are 32-bit: every point index first_path + i + 1 (and the up to 7 extra points a
+  // generation run computes past the last path) must stay below 2^32.
+  if (c.paths >= (uint64_t(1) << 32) - 16 || c.first_path >= (uint64_t(1) << 32) - 16 - c.paths)
+    raise(RG_ERR_INVALID_PATHS, "first_path + paths must stay below 2^32 - 16 (32-bit Sobol points)");
   // implied-vol grid shape (ImpliedVolGrid::validate, riga-market/src/lib.rs:94-111)
   for (int f = 0; f < r->n_local_vol; ++f) {
     const rg_implied_vol_grid& g = r->local_vol[f];
@@ -357,6 +359,18 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
   }
 
   bridge_schedule_into(T, tr.dt, P);
+  // per (node, factor): the QMC dimension n·k + f reduced to its table row, and its shift mask
+  P.nf_row.resize(size_t(T) * n);
+  P.nf_shift.resize(size_t(T) * n);
+  for (int64_t nd = 0; nd < T; ++nd)
+    for (int f = 0; f < n; ++f) {
+      const uint64_t dim = (uint64_t)P.node_k[nd] * (uint64_t)n + (uint64_t)f;
+      int32_t row = 0;
+      if (tr.vr == RG_VR_SOBOL) row = (int32_t)(dim % (uint64_t)tr.sob_dim);
+      else if (tr.vr == RG_VR_HALTON) row = (int32_t)(dim % (uint64_t)tr.hal_dim);
+      P.nf_row[size_t(nd) * n + f] = row;
+      P.nf_shift[size_t(nd) * n + f] = rg_digital_shift(dim, tr.seed);
+    }
 
   // Scenarios: the request's own market when none are given.
   std::vector<rg_scenario> own;

@@ -1,56 +1,83 @@
 // phoenix32.cu — the FP32 production kernel: one fused launch prices S common-random-number
 // scenarios of one trade.
 //
-// A CTA owns Pb paths × Sb scenario lanes (Sb = S rounded up to a power of two, Sb·Pb = 256) and
-// walks time in tiles of TT steps:
-//   1. chain phase — one "chain" per (path, factor) generates the Sobol coordinates of the bridge
-//      nodes the tile consumes, maps them through the inverse normal and advances the streamed
-//      Brownian bridge of that factor; the uncorrelated increments dW[tile][factor][path] land in
-//      shared memory.  Generation is paid once per path, not once per scenario.
-//   2. scenario phase — every (path, scenario) thread correlates the increments with its own
-//      Cholesky factor (the bridge is linear, so L·bridge(z) = bridge(L·z)), steps ln(S/S0) under
-//      flat vol or its scenario's Dupire surface and runs the Phoenix state machine.
-// Path state is FP32; event cash flows, discount factors and every reduction are FP64.
-// Reductions are fixed-order (shuffle butterfly, then warps in index order, then blocks in the
-// final reduce kernel), so results are bit-reproducible for a given launch shape.
+// A CTA owns Pb consecutive paths × Sb scenario slots (Sb = S rounded up to a power of two); thread
+// t serves scenario t / Pb and path t % Pb, so a warp is 32 paths of one scenario and its
+// local-vol lookups all read one surface.  Time is walked in tiles of TT steps, each in three
+// phases separated by CTA barriers:
+//   G. generation — every thread takes (bridge node, factor, 8-path run) tasks: the Sobol integer
+//      of the run's first point from its Gray code, the next seven by the Gray recurrence
+//      x(n) = x(n-1) ^ v[ctz(n)] (one load each), the digital shift (or Owen scramble) and the
+//      FP32 inverse normal; the standard normals of every node the tile consumes land in shared
+//      memory.  The step schedule of the tile is staged next to them.
+//   B. bridge — one chain per (path, factor) walks the tile's steps through the streamed
+//      Brownian bridge and writes the uncorrelated increments dW[step][factor][path].
+//   S. scenario stepping — every (path, scenario) thread correlates dW with its own Cholesky
+//      factor (the bridge is linear, so L·bridge(z) = bridge(L·z)), steps ln(S/S0) under flat vol
+//      or its scenario's Dupire surface and runs the Phoenix state machine.
+// Generation is paid once per path, not once per scenario.  Path state is FP32; event cash flows,
+// discount factors and every reduction are FP64, in a fixed order (shuffle butterfly within a
+// scenario's warps, warps in index order, blocks in the final reduce kernel), so a launch of a
+// given shape is bit-reproducible.
 #include "rg_internal.h"
 
 namespace rg {
 
-template <int N, bool LV>
-__global__ void __launch_bounds__(256, 2) phoenix32_kernel(
+#define GEN_CH 8  // consecutive paths per generation task (one Gray-code run)
+
+template <int N, bool LV, bool REC>
+__global__ void __launch_bounds__(512, 2) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
-    const DevScen32* __restrict__ scen32, int S, int Sb, int Pb, int TT, int stack_max, float ln_ko,
-    float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths, double* __restrict__ partial,
-    int32_t* __restrict__ ko_steps, rg_path_record* __restrict__ records) {
+    const DevScen32* __restrict__ scen32, int S, int Pb, int TT, int NNmax, int stack_max,
+    float ln_ko, float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths,
+    double* __restrict__ partial, int32_t* __restrict__ ko_steps, rg_path_record* __restrict__ records) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = blockDim.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int PbN = Pb * N;
-  double* acc = reinterpret_cast<double*>(smem_raw);                  // [S][RG_ACC]
-  unsigned char* region = smem_raw + (((size_t)S * RG_ACC * 8 + 15) & ~(size_t)15);
-  float* wcur = reinterpret_cast<float*>(region);                    // [N*Pb]
-  float* stack = wcur + PbN;                                         // [stack_max][N*Pb]
-  float* dW = stack + (size_t)stack_max * PbN;                       // [TT][N][Pb]
-  double* red = reinterpret_cast<double*>(region);                   // [nwarps][Sb][RG_ACC]
+  const int nch = Pb / GEN_CH;
+  const int T = (int)tr.steps;
+  // ---- shared-memory carve-up
+  unsigned char* ptr = smem_raw;
+  auto carve = [&](size_t bytes) {
+    unsigned char* p = ptr;
+    ptr += (bytes + 15) & ~(size_t)15;
+    return p;
+  };
+  double* acc = reinterpret_cast<double*>(carve((size_t)S * RG_ACC * 8));
+  float4* s_lv = reinterpret_cast<float4*>(carve((size_t)S * N * 16));  // (a_u, inv_h, surface offset, x0)
+  uint32_t* s_flags = reinterpret_cast<uint32_t*>(carve((size_t)TT * 4));
+  int32_t* s_per = reinterpret_cast<int32_t*>(carve((size_t)TT * 4));
+  int2* s_ti = reinterpret_cast<int2*>(carve((size_t)N * TT * 8));
+  float* s_tw = reinterpret_cast<float*>(carve((size_t)N * TT * 4));
+  int32_t* s_noff = reinterpret_cast<int32_t*>(carve((size_t)(TT + 1) * 4));
+  float* s_ncf = reinterpret_cast<float*>(carve((size_t)NNmax * 4));
+  float* wcur = reinterpret_cast<float*>(carve((size_t)PbN * 4));
+  float* stack = reinterpret_cast<float*>(carve((size_t)stack_max * PbN * 4));
+  float* Z = reinterpret_cast<float*>(carve((size_t)NNmax * PbN * 4));
+  float* dW = reinterpret_cast<float*>(carve((size_t)TT * PbN * 4));
+  double* red = reinterpret_cast<double*>(Z);  // reduction scratch, reused after the time loop
 
   for (int k = tid; k < S * RG_ACC; k += blockDim.x) acc[k] = 0.0;
 
-  const int s = tid % Sb, pl = tid / Sb;
+  const int s = tid / Pb, pl = tid % Pb;
   const bool lane_ok = s < S;
-  const int T = (int)tr.steps;
   const int gx = tr.gx;
   const float gxm1 = (float)(gx - 1);
   const float nhdt = (float)(-0.5 * tr.dt);
+  const uint32_t x_lo = tr.x_lo, x_hi = tr.x_hi;
 
-  // scenario constants in registers
-  float Lf[N * (N + 1) / 2], mu[N], sig[N], x0[N], a_u[N], inv_h[N];
-  int soff[N];
-  const double* df_s = tb.df;
-  double df_mat = 1.0;
-  if (lane_ok) {
-    const DevScenario& sc = scen[s];
-    const DevScen32& s3 = scen32[s];
+  // scenario constants: the Cholesky factor and drifts in registers; the per-asset local-vol
+  // constants (warp-uniform) in shared memory
+  for (int i = tid; i < S * N; i += blockDim.x) {
+    const DevScen32& s3 = scen32[i / N];
+    const int f = i % N;
+    s_lv[i] = make_float4(s3.a_u[f], s3.inv_h[f], __int_as_float(s3.surf_off[f]), s3.x0[f]);
+  }
+  float Lf[N * (N + 1) / 2], mu[N], sig[N];
+  const int ss = lane_ok ? s : 0;
+  {
+    const DevScenario& sc = scen[ss];
+    const DevScen32& s3 = scen32[ss];
     int q = 0;
 #pragma unroll
     for (int a = 0; a < N; ++a)
@@ -60,14 +87,10 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
     for (int f = 0; f < N; ++f) {
       mu[f] = s3.mu_dt[f];
       sig[f] = s3.sig[f];
-      x0[f] = s3.x0[f];
-      a_u[f] = s3.a_u[f];
-      inv_h[f] = s3.inv_h[f];
-      soff[f] = s3.surf_off[f];
     }
-    df_s = tb.df + (size_t)s * T;
-    df_mat = tb.df_mat[s];
   }
+  const float4* lvc = s_lv + ss * N;
+  __syncthreads();
 
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -77,48 +100,97 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
     const bool ok = lane_ok && gi < npaths;
     float x[N];
 #pragma unroll
-    for (int f = 0; f < N; ++f) x[f] = x0[f];
+    for (int f = 0; f < N; ++f) x[f] = lvc[f].w;
     bool alive = true, received = false;
     int qual = 0, unpaid = 0, ko_step = -1, qualified = 0, paid = 0;
-    double cpv = 0.0, mpv = 0.0;
+    float cpv = 0.0f, mpv = 0.0f;
     float worst = 0.0f;
     int sp = 0;
-    __syncthreads();
     for (int t0 = 0; t0 < T; t0 += TT) {
       const int tn = min(TT, T - t0);
-      // ---- chain phase: Sobol → inverse normal → streamed bridge, one chain per (path, factor)
-      for (int c = tid; c < PbN; c += blockDim.x) {
-        const int p = c % Pb, f = c / Pb;
-        const uint64_t cgi = tile0 + p;
-        if (cgi < npaths) {
-          const uint64_t path = path0 + cgi;
-          float wc = wcur[c];
-          int lsp = sp;
-          for (int tt = 0; tt < tn; ++tt) {
-            const int t = t0 + tt;
-            const int n0 = __ldg(tb.node_off + t), n1 = __ldg(tb.node_off + t + 1);
-            for (int nd = n0; nd < n1; ++nd) {
-              const int k = __ldg(tb.node_k + nd);
-              const float cf = __ldg(tb.node_cf + nd);
-              const float z = rg_qmc_normal32(tr, tb, path, (uint64_t)k * N + f);
-              const float w = nd == 0 ? z * cf : fmaf(z, cf, 0.5f * (wc + stack[(lsp - 1) * PbN + c]));
-              stack[lsp * PbN + c] = w;
-              ++lsp;
-            }
-            --lsp;
-            const float wn = stack[lsp * PbN + c];
-            dW[(tt * N + f) * Pb + p] = wn - wc;
-            wc = wn;
+      const int n0 = __ldg(tb.node_off + t0), n1 = __ldg(tb.node_off + t0 + tn);
+      const int nn = n1 - n0;
+      // ---- G: standard normals of the tile's bridge nodes, and the tile's step schedule
+      for (int i = tid; i < tn; i += blockDim.x) {
+        s_flags[i] = __ldg(tb.step_flags + t0 + i);
+        s_per[i] = __ldg(tb.step_period + t0 + i);
+        if (LV) {
+#pragma unroll
+          for (int f = 0; f < N; ++f) {
+            s_ti[f * TT + i] = __ldg(tb.lv_ti + f * T + t0 + i);
+            s_tw[f * TT + i] = __ldg(tb.lv_twf + f * T + t0 + i);
           }
-          wcur[c] = wc;
         }
       }
-      sp += (__ldg(tb.node_off + t0 + tn) - __ldg(tb.node_off + t0)) - tn;
+      for (int i = tid; i <= tn; i += blockDim.x) s_noff[i] = __ldg(tb.node_off + t0 + i);
+      for (int i = tid; i < nn; i += blockDim.x) s_ncf[i] = __ldg(tb.node_cf + n0 + i);
+      const int ntask = nn * N * nch;
+      for (int task = tid; task < ntask; task += blockDim.x) {
+        const int c = task % nch, rem = task / nch, f = rem % N, j = rem / N;
+        const int nd = n0 + j;
+        const uint64_t g0 = tile0 + (uint64_t)c * GEN_CH;
+        if (g0 >= npaths) continue;  // these paths are never read
+        float* zo = Z + (size_t)(j * N + f) * GEN_CH * nch + c;
+        if (tr.vr == RG_VR_SOBOL) {
+          const uint32_t* row = tb.sobol + 32 * (size_t)__ldg(tb.nf_row + nd * N + f);
+          uint64_t n = path0 + g0 + 1;
+          uint32_t xs = rg_sobol_gray(row, n);
+          if (tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT) {
+            const uint32_t shift = __ldg(tb.nf_shift + nd * N + f);
+#pragma unroll
+            for (int q = 0; q < GEN_CH; ++q) {
+              if (q) {
+                ++n;
+                xs ^= __ldg(row + (__ffsll((long long)n) - 1));
+              }
+              zo[q * nch] = rg_probit32(xs ^ shift, x_lo, x_hi);
+            }
+          } else {
+            const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
+            for (int q = 0; q < GEN_CH; ++q) {
+              if (q) {
+                ++n;
+                xs ^= __ldg(row + (__ffsll((long long)n) - 1));
+              }
+              zo[q * nch] = rg_probit32(rg_owen(xs, dim, tr.seed), x_lo, x_hi);
+            }
+          }
+        } else {
+          const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
+          for (int q = 0; q < GEN_CH; ++q)
+            zo[q * nch] = (float)rg_qmc_normal64(tr, tb, path0 + g0 + q, dim);
+        }
+      }
       __syncthreads();
-      // ---- scenario phase
+      // ---- B: streamed bridge, one chain per (path, factor)
+      for (int c = tid; c < PbN; c += blockDim.x) {
+        const int p = c % Pb, f = c / Pb;
+        if (tile0 + p >= npaths) continue;
+        const int pc = p / GEN_CH, pq = p % GEN_CH;
+        float wc = wcur[c];
+        int lsp = sp;
+        for (int tt = 0; tt < tn; ++tt) {
+          const int e0 = s_noff[tt], e1 = s_noff[tt + 1];
+          for (int nd = e0; nd < e1; ++nd) {
+            const int j = nd - n0;
+            const float z = Z[((size_t)(j * N + f) * GEN_CH + pq) * nch + pc];
+            const float cf = s_ncf[j];
+            const float w = nd == 0 ? z * cf : fmaf(z, cf, 0.5f * (wc + stack[(lsp - 1) * PbN + c]));
+            stack[lsp * PbN + c] = w;
+            ++lsp;
+          }
+          --lsp;
+          const float wn = stack[lsp * PbN + c];
+          dW[(tt * N + f) * Pb + p] = wn - wc;
+          wc = wn;
+        }
+        wcur[c] = wc;
+      }
+      sp += nn - tn;
+      __syncthreads();
+      // ---- S: scenario stepping
       if (ok) {
         for (int tt = 0; tt < tn; ++tt) {
-          const int t = t0 + tt;
           float d[N], y[N];
 #pragma unroll
           for (int f = 0; f < N; ++f) d[f] = dW[(tt * N + f) * Pb + pl];
@@ -135,13 +207,14 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
           for (int f = 0; f < N; ++f) {
             float sg;
             if (LV) {
-              const int2 ti = __ldg(tb.lv_ti + f * T + t);
-              const float wt = __ldg(tb.lv_twf + f * T + t);
-              float u = fmaf(x[f], inv_h[f], a_u[f]);
+              const int2 ti = s_ti[f * TT + tt];
+              const float wt = s_tw[f * TT + tt];
+              const float4 c4 = lvc[f];
+              float u = fmaf(x[f], c4.y, c4.x);
               u = fminf(fmaxf(u, 0.0f), gxm1);
-              const int j = min((int)u, gx - 2);
-              const float w = u - (float)j;
-              const float2* base = tb.lv_vf + soff[f] + j;
+              const int jj = min((int)u, gx - 2);
+              const float w = u - (float)jj;
+              const float2* base = tb.lv_vf + __float_as_int(c4.z) + jj;
               const float2 lo = __ldg(base + ti.x * gx), hi = __ldg(base + ti.y * gx);
               const float v0 = fmaf(w, lo.y, lo.x), v1 = fmaf(w, hi.y, hi.x);
               sg = fmaf(wt, v1 - v0, v0);
@@ -153,35 +226,36 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
           }
           worst = wmin;
           if (alive) {
-            const uint32_t fl = __ldg(tb.step_flags + t);
+            const uint32_t fl = s_flags[tt];
+            const int t = t0 + tt;
             if (fl & STEP_PERIOD_RESET) qual = 0;
             if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
               ++qual;
-              ++qualified;
+              if (REC) ++qualified;
             }
             if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
               alive = false;
               ko_step = t;
-              const double due = (fl & STEP_FIXED_DUE) ? tr.coupon_rate
-                                                       : (double)qual * __ldg(tb.accr_inc + __ldg(tb.step_period + t));
-              const double carry = due > 0.0 ? (double)unpaid * tr.coupon_rate : 0.0;
-              if (due + carry > 0.0) {
-                const double df = __ldg(df_s + t);
-                cpv += due * df;
-                mpv += carry * df;
+              const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                                      : (float)qual * (float)__ldg(tb.accr_inc + s_per[tt]);
+              const float carry = due > 0.0f ? (float)unpaid * (float)tr.coupon_rate : 0.0f;
+              if (due + carry > 0.0f) {
+                const float df = (float)__ldg(tb.df + (size_t)ss * T + t);
+                cpv = fmaf(due, df, cpv);
+                mpv = fmaf(carry, df, mpv);
                 received = true;
-                ++paid;
+                if (REC) ++paid;
               }
             } else if (fl & STEP_PERIOD_END) {
-              const double due = (fl & STEP_FIXED_DUE) ? tr.coupon_rate
-                                                       : (double)qual * __ldg(tb.accr_inc + __ldg(tb.step_period + t));
-              if (due > 0.0) {
-                const double df = __ldg(df_s + t);
-                cpv += due * df;
-                mpv += (double)unpaid * tr.coupon_rate * df;
+              const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                                      : (float)qual * (float)__ldg(tb.accr_inc + s_per[tt]);
+              if (due > 0.0f) {
+                const float df = (float)__ldg(tb.df + (size_t)ss * T + t);
+                cpv = fmaf(due, df, cpv);
+                mpv = fmaf((float)unpaid * (float)tr.coupon_rate, df, mpv);
                 unpaid = 0;
                 received = true;
-                ++paid;
+                if (REC) ++paid;
               } else if (tr.memory) {
                 ++unpaid;
               }
@@ -197,12 +271,13 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
     for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0;
     if (ok) {
       const bool ko = ko_step >= 0;
-      const double funding = ko ? __ldg(df_s + ko_step) : df_mat;
+      const double df_mat = __ldg(tb.df_mat + ss);
+      const double funding = ko ? __ldg(tb.df + (size_t)ss * T + ko_step) : df_mat;
       const bool hit_ki = worst <= ln_ki;
       const bool put_ok = hit_ki && !ko;
       const double wf = exp((double)worst);
       const double put = put_ok ? fmax(tr.strike - wf, 0.0) * df_mat : 0.0;
-      const double cn = cpv + mpv;
+      const double cn = (double)cpv + (double)mpv;
       const double pv = funding + cn - put;
       out[ACC_PV] = pv - 1.0;
       out[ACC_PV2] = (pv - 1.0) * (pv - 1.0);
@@ -223,11 +298,11 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
       }
       out[ACC_PUT] = put;
       out[ACC_FUND] = funding;
-      out[ACC_CQ] = cn * 10.0 - mpv * 10.0;
-      out[ACC_MQ] = mpv * 10.0;
+      out[ACC_CQ] = cn * 10.0 - (double)mpv * 10.0;
+      out[ACC_MQ] = (double)mpv * 10.0;
       out[ACC_NPUT] = put_ok ? 1.0 : 0.0;
       if (s == 0 && ko_steps) ko_steps[gi] = ko_step;
-      if (s == 0 && records) {
+      if (REC && s == 0 && records) {
         rg_path_record r;
         r.path_id = path0 + gi;
         r.rng_seed = tr.seed;
@@ -241,46 +316,51 @@ __global__ void __launch_bounds__(256, 2) phoenix32_kernel(
         r.paid_periods = paid;
         r.put_payoff = put;
         r.coupon_pv = cn;
-        r.memory_coupon_pv = mpv;
+        r.memory_coupon_pv = (double)mpv;
         r.funding = funding;
         r.pv = pv;
         records[gi] = r;
       }
     }
-    // butterfly across the paths of this warp that share a scenario lane
-    for (int off = Sb; off < 32; off <<= 1)
+    // butterfly within each group of lanes that share a scenario (g = min(32, Pb) lanes)
+    const int g = Pb < 32 ? Pb : 32;
+    for (int off = g >> 1; off > 0; off >>= 1)
 #pragma unroll
       for (int k = 0; k < RG_ACC; ++k) out[k] += __shfl_xor_sync(0xffffffffu, out[k], off);
-    if (lane < Sb)
+    if ((lane % g) == 0)
 #pragma unroll
-      for (int k = 0; k < RG_ACC; ++k) red[((size_t)warp * Sb + lane) * RG_ACC + k] = out[k];
+      for (int k = 0; k < RG_ACC; ++k) red[(size_t)(tid / g) * RG_ACC + k] = out[k];
     __syncthreads();
-    for (int j = tid; j < S * RG_ACC; j += blockDim.x) {
-      const int ss = j / RG_ACC, k = j % RG_ACC;
+    const int groups_per_scen = Pb / g;
+    for (int jx = tid; jx < S * RG_ACC; jx += blockDim.x) {
+      const int ss = jx / RG_ACC, k = jx % RG_ACC;
       double v = 0.0;
-      for (int w = 0; w < nwarps; ++w) v += red[((size_t)w * Sb + ss) * RG_ACC + k];
-      acc[j] += v;
+      for (int w = 0; w < groups_per_scen; ++w) v += red[(size_t)(ss * groups_per_scen + w) * RG_ACC + k];
+      acc[jx] += v;
     }
     __syncthreads();
   }
-  for (int j = tid; j < S * RG_ACC; j += blockDim.x) partial[(size_t)blockIdx.x * S * RG_ACC + j] = acc[j];
+  for (int jx = tid; jx < S * RG_ACC; jx += blockDim.x) partial[(size_t)blockIdx.x * S * RG_ACC + jx] = acc[jx];
 }
 
 template <int N, bool LV>
-static const void* kernel_ptr() {
-  return reinterpret_cast<const void*>(&phoenix32_kernel<N, LV>);
+static const void* kernel_ptr(bool rec) {
+  return rec ? reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, true>)
+             : reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, false>);
 }
 
-static const void* select_kernel(int n, bool lv) {
+static const void* select_kernel(int n, bool lv, bool rec) {
   switch (n) {
-    case 1: return lv ? kernel_ptr<1, true>() : kernel_ptr<1, false>();
-    case 2: return lv ? kernel_ptr<2, true>() : kernel_ptr<2, false>();
-    case 3: return lv ? kernel_ptr<3, true>() : kernel_ptr<3, false>();
-    case 4: return lv ? kernel_ptr<4, true>() : kernel_ptr<4, false>();
-    case 5: return lv ? kernel_ptr<5, true>() : kernel_ptr<5, false>();
+    case 1: return lv ? kernel_ptr<1, true>(rec) : kernel_ptr<1, false>(rec);
+    case 2: return lv ? kernel_ptr<2, true>(rec) : kernel_ptr<2, false>(rec);
+    case 3: return lv ? kernel_ptr<3, true>(rec) : kernel_ptr<3, false>(rec);
+    case 4: return lv ? kernel_ptr<4, true>(rec) : kernel_ptr<4, false>(rec);
+    case 5: return lv ? kernel_ptr<5, true>(rec) : kernel_ptr<5, false>(rec);
     default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
   }
 }
+
+static size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
@@ -288,23 +368,32 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   int sb = 1;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
-  sh.threads = 256;
-  sh.Pb = 256 / sb;
-  const int PbN = sh.Pb * P.n;
-  int tt = 8192 / PbN;
+  sh.threads = sb >= 8 ? 512 : 256;
+  sh.Pb = sh.threads / sb;
+  const int N = P.n, PbN = sh.Pb * N;
+  int tt = (12288 / PbN - P.stack_max) / 2;
   tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
   sh.TT = tt;
-  size_t acc_bytes = ((size_t)P.n_scen * RG_ACC * 8 + 15) & ~(size_t)15;
-  size_t chain = ((size_t)(1 + P.stack_max) * PbN + (size_t)tt * PbN) * 4;
-  size_t red = (size_t)(256 / 32) * sb * RG_ACC * 8;
-  sh.smem = (int)(acc_bytes + (chain > red ? chain : red));
-  const void* k = select_kernel(P.n, P.trade.has_lv != 0);
-  cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),
-             "phoenix32 smem attribute");
+  const int NNmax = tt + P.stack_max;
+  size_t bytes = align16((size_t)P.n_scen * RG_ACC * 8) + align16((size_t)P.n_scen * N * 16) +
+                 align16((size_t)tt * 4) * 2 +
+                 align16((size_t)N * tt * 8) + align16((size_t)N * tt * 4) + align16((size_t)(tt + 1) * 4) +
+                 align16((size_t)NNmax * 4) + align16((size_t)PbN * 4) + align16((size_t)P.stack_max * PbN * 4);
+  size_t zbytes = align16((size_t)NNmax * PbN * 4);
+  const int g = sh.Pb < 32 ? sh.Pb : 32;
+  size_t red = (size_t)(sh.threads / g) * RG_ACC * 8;
+  if (zbytes < red) zbytes = align16(red);
+  bytes += zbytes + align16((size_t)tt * PbN * 4);
+  sh.smem = (int)bytes;
+  for (int rec = 0; rec < 2; ++rec)
+    cuda_check(cudaFuncSetAttribute(select_kernel(P.n, P.trade.has_lv != 0, rec != 0),
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),
+               "phoenix32 smem attribute");
+  const void* k = select_kernel(P.n, P.trade.has_lv != 0, false);
   int per_sm = 0;
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, sh.threads, sh.smem),
              "phoenix32 occupancy");
-  if (per_sm < 1) per_sm = 1;
+  if (per_sm < 1) raise(RG_ERR_GPU_ERROR, "phoenix32: launch shape does not fit on an SM");
   uint64_t tiles = (npaths + sh.Pb - 1) / sh.Pb;
   uint64_t cap = (uint64_t)sm_count * per_sm;
   sh.grid = (int)(tiles < cap ? tiles : cap);
@@ -316,20 +405,24 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
                       const DevScen32* scen32, uint64_t path0, uint64_t npaths, const Fp32Shape& sh,
                       const LaunchOut& out, cudaStream_t st) {
   const float ln_ko = (float)P.ln_ko, ln_cb = (float)P.ln_cb, ln_ki = (float)P.ln_ki;
-#define RG_LAUNCH(NN, LVV)                                                                       \
-  phoenix32_kernel<NN, LVV><<<sh.grid, sh.threads, sh.smem, st>>>(                               \
-      P.trade, tb, scen, scen32, P.n_scen, sh.Sb, sh.Pb, sh.TT, P.stack_max, ln_ko, ln_cb, ln_ki, \
-      path0, npaths, out.partial, out.ko_steps, out.records)
+  const int NNmax = sh.TT + P.stack_max;
+#define RG_LAUNCH(NN, LVV)                                                                        \
+  if (out.records) RG_LAUNCH_R(NN, LVV, true) else RG_LAUNCH_R(NN, LVV, false)
+#define RG_LAUNCH_R(NN, LVV, REC)                                                                 \
+  phoenix32_kernel<NN, LVV, REC><<<sh.grid, sh.threads, sh.smem, st>>>(                           \
+      P.trade, tb, scen, scen32, P.n_scen, sh.Pb, sh.TT, NNmax, P.stack_max, ln_ko, ln_cb, ln_ki, \
+      path0, npaths, out.partial, out.ko_steps, out.records);
   const bool lv = P.trade.has_lv != 0;
   switch (P.n) {
-    case 1: if (lv) RG_LAUNCH(1, true); else RG_LAUNCH(1, false); break;
-    case 2: if (lv) RG_LAUNCH(2, true); else RG_LAUNCH(2, false); break;
-    case 3: if (lv) RG_LAUNCH(3, true); else RG_LAUNCH(3, false); break;
-    case 4: if (lv) RG_LAUNCH(4, true); else RG_LAUNCH(4, false); break;
-    case 5: if (lv) RG_LAUNCH(5, true); else RG_LAUNCH(5, false); break;
+    case 1: if (lv) { RG_LAUNCH(1, true) } else { RG_LAUNCH(1, false) } break;
+    case 2: if (lv) { RG_LAUNCH(2, true) } else { RG_LAUNCH(2, false) } break;
+    case 3: if (lv) { RG_LAUNCH(3, true) } else { RG_LAUNCH(3, false) } break;
+    case 4: if (lv) { RG_LAUNCH(4, true) } else { RG_LAUNCH(4, false) } break;
+    case 5: if (lv) { RG_LAUNCH(5, true) } else { RG_LAUNCH(5, false) } break;
     default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
   }
 #undef RG_LAUNCH
+#undef RG_LAUNCH_R
   cuda_check(cudaGetLastError(), "phoenix32_kernel launch");
 }
 

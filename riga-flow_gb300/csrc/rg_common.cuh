@@ -69,6 +69,8 @@ struct DevTables {
   const int32_t* node_k;       // [T] preorder index (QMC step) of each node, consumption order
   const double* node_c;        // [T] bridge standard deviation of each node
   const float* node_cf;        // [T] the same in FP32
+  const int32_t* nf_row;       // [T][n] Sobol table row of (node, factor)
+  const uint32_t* nf_shift;    // [T][n] digital-shift mask of (node, factor)
   const int2* lv_ti;           // [n][T] (tenor row at or below step t's time, next row)
   const double* lv_tw;         // [n][T] tenor weight
   const float* lv_twf;         // [n][T] tenor weight in FP32

@@ -97,6 +97,8 @@ struct Prepared {
   std::vector<int32_t> node_off, node_k;
   std::vector<double> node_c;
   std::vector<float> node_cf;
+  std::vector<int32_t> nf_row;   // [node][n] Sobol row (dim % sob_dim) or Halton base index
+  std::vector<uint32_t> nf_shift;  // [node][n] digital-shift mask of that dimension
   std::vector<int32_t> lv_ti;   // [n][T][2] (row, next row)
   std::vector<double> lv_tw;    // [n][T]
   std::vector<float> lv_twf;    // [n][T]
