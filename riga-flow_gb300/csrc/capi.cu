@@ -170,8 +170,7 @@ struct rg_engine {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::mutex mu;
-  DevBuf arena, partial, sums, kosteps, records, calib_scratch, sobol;
-  int64_t sobol_dim = -1;
+  DevBuf bufs[WS_NSLOTS];
   HostBuf host_sums;
   std::vector<uint8_t> host_pack;
   cudaEvent_t ev[6] = {};
@@ -215,7 +214,7 @@ struct Staged {
   DevScen32* scen32 = nullptr;
 };
 
-static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
+static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   Pack pk;
   const DevTrade& tr = P.trade;
   const int64_t T = P.T;
@@ -261,11 +260,9 @@ static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
     jobs.resize(P.n_surf);
     o_jobs = pk.reserve(sizeof(CalibJob) * (size_t)P.n_surf);
   }
-  E->arena.ensure(pk.host.size());
-  uint8_t* base = static_cast<uint8_t*>(E->arena.ptr);
+  uint8_t* base = static_cast<uint8_t*>(W.device(WS_ARENA, pk.host.size()));
   if (tr.has_lv) {
-    E->calib_scratch.ensure(scratch * sizeof(double));
-    double* sc = static_cast<double*>(E->calib_scratch.ptr);
+    double* sc = static_cast<double*>(W.device(WS_CALIB, scratch * sizeof(double)));
     size_t cell_off = 0, sc_off = 0;
     for (int j = 0; j < P.n_surf; ++j) {
       const SurfaceKey& key = P.surfaces[j];
@@ -289,11 +286,11 @@ static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
     }
     memcpy(pk.host.data() + o_jobs, jobs.data(), sizeof(CalibJob) * jobs.size());
   }
-  cuda_check(cudaEventRecord(E->ev[0], E->stream), "event");
-  cuda_check(cudaMemcpyAsync(base, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, E->stream),
+  if (W.ev) cuda_check(cudaEventRecord(W.ev[0], W.stream), "event");
+  cuda_check(cudaMemcpyAsync(base, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, W.stream),
              "H2D request tables");
-  cuda_check(cudaEventRecord(E->ev[1], E->stream), "event");
-  E->timing.h2d_bytes += pk.host.size();
+  if (W.ev) cuda_check(cudaEventRecord(W.ev[1], W.stream), "event");
+  if (W.timing) W.timing->h2d_bytes += pk.host.size();
   Staged S;
   DevTables& tb = S.tb;
   tb.sobol = reinterpret_cast<const uint32_t*>(base + o_sobol);
@@ -321,12 +318,12 @@ static Staged stage(rg_engine* E, const rg_price_request* req, Prepared& P) {
   S.scen = reinterpret_cast<DevScenario*>(base + o_scen);
   S.scen32 = reinterpret_cast<DevScen32*>(base + o_s32);
   if (tr.has_lv) {
-    launch_calibrate(reinterpret_cast<const CalibJob*>(base + o_jobs), P.n_surf, E->stream);
-    E->timing.kernel_launches += 1;
+    launch_calibrate(reinterpret_cast<const CalibJob*>(base + o_jobs), P.n_surf, W.stream);
+    if (W.timing) W.timing->kernel_launches += 1;
   }
-  launch_cholesky(S.scen, P.n_scen, P.n, E->stream);
-  E->timing.kernel_launches += 1;
-  cuda_check(cudaEventRecord(E->ev[2], E->stream), "event");
+  launch_cholesky(S.scen, P.n_scen, P.n, W.stream);
+  if (W.timing) W.timing->kernel_launches += 1;
+  if (W.ev) cuda_check(cudaEventRecord(W.ev[2], W.stream), "event");
   return S;
 }
 
@@ -385,7 +382,7 @@ static void finish(const double* a, uint64_t paths, uint64_t seed, rg_price_resu
 
 // First RG_TRACE_EVENT_CAP knocked-out paths in path order (note.rs:174-180), read back in
 // growing chunks of the per-path KO steps.
-static void collect_trace(rg_engine* E, const int32_t* dev_ko, uint64_t paths, uint64_t first_path,
+static void collect_trace(Workspace& W, const int32_t* dev_ko, uint64_t paths, uint64_t first_path,
                           double dt, rg_price_result* out) {
   std::vector<int32_t> buf;
   uint64_t done = 0, chunk = 4096;
@@ -393,8 +390,8 @@ static void collect_trace(rg_engine* E, const int32_t* dev_ko, uint64_t paths, u
     uint64_t n = paths - done < chunk ? paths - done : chunk;
     buf.resize(n);
     cuda_check(cudaMemcpyAsync(buf.data(), dev_ko + done, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                               E->stream), "D2H ko steps");
-    cuda_check(cudaStreamSynchronize(E->stream), "trace sync");
+                               W.stream), "D2H ko steps");
+    cuda_check(cudaStreamSynchronize(W.stream), "trace sync");
     for (uint64_t i = 0; i < n && out->n_trace_events < RG_TRACE_EVENT_CAP; ++i)
       if (buf[i] >= 0) {
         out->trace_events[out->n_trace_events].path_id = first_path + done + i;
@@ -414,8 +411,8 @@ static void check_lane(const rg_price_request* req) {
 }
 
 // Prices `n_scen` scenarios (0 = the request's own market) into out[max(1, n_scen)].
-static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* sc, int n_scen,
-                  rg_price_result* out) {
+void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc, int n_scen,
+                rg_price_result* out) {
   validate_request(req);
   check_lane(req);
   for (int i = 0; i < n_scen; ++i) {
@@ -424,69 +421,97 @@ static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* 
     r2.market.as_of = req->market.as_of;
     validate_request(&r2);
   }
-  std::lock_guard<std::mutex> lock(E->mu);
-  cuda_check(cudaSetDevice(E->device), "cudaSetDevice");
   const int total = n_scen ? n_scen : 1;
   const bool fp32 = req->config.precision == RG_PRECISION_FP32;
   const int per_launch = fp32 ? 32 : 1;
   const uint64_t paths = req->config.paths;
   const bool trace = req->config.trace_level != RG_TRACE_OFF;
-  E->timing = rg_timing{};
+  if (W.timing) *W.timing = rg_timing{};
   for (int first = 0; first < total; first += per_launch) {
     const int cnt = total - first < per_launch ? total - first : per_launch;
     Prepared P;
     prepare(req, n_scen ? sc + first : nullptr, n_scen ? cnt : 0, P);
-    Staged S = stage(E, req, P);
+    W.begin_launch();
+    Staged S = stage(W, req, P);
     LaunchOut lo{};
     int grid;
     Fp32Shape sh{};
     if (fp32) {
-      sh = phoenix32_shape(P, paths, device_info().sm_count);
+      sh = phoenix32_shape(P, paths, W.sm_count);
       grid = sh.grid;
     } else {
       grid = phoenix64_grid(P, paths);
     }
-    E->partial.ensure((size_t)grid * P.n_scen * RG_ACC * sizeof(double));
-    E->sums.ensure((size_t)P.n_scen * RG_ACC * sizeof(double));
-    lo.partial = static_cast<double*>(E->partial.ptr);
+    const size_t sums_bytes = (size_t)P.n_scen * RG_ACC * sizeof(double);
+    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)grid * P.n_scen * RG_ACC * sizeof(double)));
+    double* dsums = static_cast<double*>(W.device(WS_SUMS, sums_bytes));
     lo.grid = grid;
     if (trace) {
       // KO trace events are recorded for the first scenario of each fused launch
-      E->kosteps.ensure(paths * sizeof(int32_t));
-      lo.ko_steps = static_cast<int32_t*>(E->kosteps.ptr);
+      lo.ko_steps = static_cast<int32_t*>(W.device(WS_KOSTEPS, paths * sizeof(int32_t)));
     }
     const uint64_t path0 = req->config.first_path;
     if (fp32) {
-      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, E->stream);
-      E->timing.block = sh.threads;
-      E->timing.smem_bytes = sh.smem;
+      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.stream);
     } else {
-      launch_phoenix64(P, S.tb, S.scen, path0, paths, lo, E->stream);
-      E->timing.block = 128;
+      launch_phoenix64(P, S.tb, S.scen, path0, paths, lo, W.stream);
     }
-    E->timing.grid = grid;
-    cuda_check(cudaEventRecord(E->ev[3], E->stream), "event");
-    launch_reduce(lo.partial, grid, P.n_scen, static_cast<double*>(E->sums.ptr), E->stream);
-    cuda_check(cudaEventRecord(E->ev[4], E->stream), "event");
-    E->timing.kernel_launches += 2;
-    E->host_sums.ensure((size_t)P.n_scen * RG_ACC * sizeof(double));
-    cuda_check(cudaMemcpyAsync(E->host_sums.ptr, E->sums.ptr, (size_t)P.n_scen * RG_ACC * sizeof(double),
-                               cudaMemcpyDeviceToHost, E->stream), "D2H sums");
-    E->timing.d2h_bytes += (size_t)P.n_scen * RG_ACC * sizeof(double);
-    cuda_check(cudaEventRecord(E->ev[5], E->stream), "event");
-    cuda_check(cudaStreamSynchronize(E->stream), "pricing");
-    float ms[5];
-    for (int k = 0; k < 5; ++k) cuda_check(cudaEventElapsedTime(&ms[k], E->ev[k], E->ev[k + 1]), "event time");
-    E->timing.h2d_ms += ms[0];
-    E->timing.prologue_ms += ms[1];
-    E->timing.kernel_ms += ms[2];
-    E->timing.reduce_ms += ms[3];
-    E->timing.d2h_ms += ms[4];
-    E->timing.device_ms += ms[0] + ms[1] + ms[2] + ms[3] + ms[4];
-    const double* hs = static_cast<const double*>(E->host_sums.ptr);
+    if (W.timing) {
+      W.timing->block = fp32 ? sh.threads : 128;
+      W.timing->smem_bytes = fp32 ? sh.smem : 0;
+      W.timing->grid = grid;
+      W.timing->kernel_launches += 2;
+      W.timing->d2h_bytes += sums_bytes;
+    }
+    if (W.ev) cuda_check(cudaEventRecord(W.ev[3], W.stream), "event");
+    launch_reduce(lo.partial, grid, P.n_scen, dsums, W.stream);
+    if (W.ev) cuda_check(cudaEventRecord(W.ev[4], W.stream), "event");
+    double* hs = static_cast<double*>(W.host(sums_bytes));
+    cuda_check(cudaMemcpyAsync(hs, dsums, sums_bytes, cudaMemcpyDeviceToHost, W.stream), "D2H sums");
+    if (W.ev) cuda_check(cudaEventRecord(W.ev[5], W.stream), "event");
+    cuda_check(cudaStreamSynchronize(W.stream), "pricing");
+    if (W.ev && W.timing) {
+      float ms[5];
+      for (int k = 0; k < 5; ++k) cuda_check(cudaEventElapsedTime(&ms[k], W.ev[k], W.ev[k + 1]), "event time");
+      W.timing->h2d_ms += ms[0];
+      W.timing->prologue_ms += ms[1];
+      W.timing->kernel_ms += ms[2];
+      W.timing->reduce_ms += ms[3];
+      W.timing->d2h_ms += ms[4];
+      W.timing->device_ms += ms[0] + ms[1] + ms[2] + ms[3] + ms[4];
+    }
     for (int i = 0; i < cnt; ++i) finish(hs + (size_t)i * RG_ACC, paths, req->config.seed, &out[first + i]);
-    if (trace) collect_trace(E, lo.ko_steps, paths, req->config.first_path, P.trade.dt, &out[first]);
+    if (trace) collect_trace(W, lo.ko_steps, paths, req->config.first_path, P.trade.dt, &out[first]);
   }
+}
+
+int device_sm_count() { return device_info().sm_count; }
+
+// The engine's workspace: growable device buffers, pinned host sums, timing events.
+struct EngineWorkspace : Workspace {
+  rg_engine* E;
+  explicit EngineWorkspace(rg_engine* e) : E(e) {
+    stream = e->stream;
+    ev = e->ev;
+    timing = &e->timing;
+    sm_count = device_info().sm_count;
+  }
+  void* device(int slot, size_t bytes) override {
+    E->bufs[slot].ensure(bytes);
+    return E->bufs[slot].ptr;
+  }
+  void* host(size_t bytes) override {
+    E->host_sums.ensure(bytes);
+    return E->host_sums.ptr;
+  }
+};
+
+static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* sc, int n_scen,
+                  rg_price_result* out) {
+  std::lock_guard<std::mutex> lock(E->mu);
+  cuda_check(cudaSetDevice(E->device), "cudaSetDevice");
+  EngineWorkspace W(E);
+  price_with(W, req, sc, n_scen, out);
 }
 
 }  // namespace rg
@@ -660,15 +685,14 @@ extern "C" int32_t rg_run_paths(rg_engine* e, const rg_price_request* req, uint6
     cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
     Prepared P;
     prepare(req, nullptr, 0, P);
-    Staged S = stage(e, req, P);
+    EngineWorkspace W(e);
+    Staged S = stage(W, req, P);
     const bool fp32 = req->config.precision == RG_PRECISION_FP32;
     LaunchOut lo{};
     Fp32Shape sh{};
     lo.grid = fp32 ? (sh = phoenix32_shape(P, count, device_info().sm_count)).grid : phoenix64_grid(P, count);
-    e->partial.ensure((size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double));
-    e->records.ensure(count * sizeof(rg_path_record));
-    lo.partial = static_cast<double*>(e->partial.ptr);
-    lo.records = static_cast<rg_path_record*>(e->records.ptr);
+    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));
+    lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, count * sizeof(rg_path_record)));
     const uint64_t path0 = req->config.first_path + first;
     if (fp32)
       launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, count, sh, lo, e->stream);

@@ -114,6 +114,24 @@ struct Prepared {
 
 struct Engine;
 
+// The device and host memory one pricing call draws on: the engine's growable buffers, or a fixed
+// region.  Slots are requested in this order within each fused launch.
+enum WsSlot { WS_ARENA = 0, WS_CALIB, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS, WS_NSLOTS };
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t* ev = nullptr;    // six events for the timing breakdown, or null
+  rg_timing* timing = nullptr;  // or null
+  int sm_count = 0;
+  virtual void begin_launch() {}
+  virtual void* device(int slot, size_t bytes) = 0;
+  virtual void* host(size_t bytes) = 0;  // landing area of the FP64 sums
+  virtual ~Workspace() = default;
+};
+// validate → host tables → H2D → prologue → fused kernel → reduce → D2H → PriceResults
+void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc, int n_scen,
+                rg_price_result* out);
+int device_sm_count();
+
 // Request preparation (host, FP64): validation already done.
 void prepare(const rg_price_request* req, const rg_scenario* scen, int n_scen, Prepared& P);
 // The streamed bridge schedule (node_off, node_k, node_c, stack_max) of T steps.

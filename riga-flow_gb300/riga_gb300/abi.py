@@ -289,6 +289,7 @@ SIGNATURES = {
     "rg_engine_create": (_i32, [_i32, C.POINTER(_vp)]),
     "rg_engine_destroy": (None, [_vp]),
     "rg_price_put_leg": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(PriceResult)]),
+    "rg_price_put_leg_static": (_i32, [C.POINTER(PriceRequest), C.POINTER(PriceResult)]),
     "rg_price_scenarios": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32,
                                   C.POINTER(PriceResult)]),
     "rg_price_risk_batch": (_i32, [_vp, C.POINTER(PriceRequest),
