@@ -238,7 +238,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
   // local-vol surfaces: inputs (grids) and outputs
   const int gx = tr.gx;
-  size_t o_lv = 0, o_lvf = 0, o_logs = 0, o_jobs = 0;
+  size_t o_lv = 0, o_lvf = 0, o_logs = 0, o_jobs = 0, o_celloff = 0, o_sasset = 0;
   std::vector<size_t> o_mats, o_ks, o_vs;
   size_t cells = 0, scratch = 0;
   std::vector<CalibJob> jobs;
@@ -259,6 +259,15 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
     }
     jobs.resize(P.n_surf);
     o_jobs = pk.reserve(sizeof(CalibJob) * (size_t)P.n_surf);
+    std::vector<int32_t> cell_off(P.n_surf), sasset(P.n_surf);
+    int32_t co = 0;
+    for (int j = 0; j < P.n_surf; ++j) {
+      cell_off[j] = co;
+      co += P.surf_nt[j] * gx;
+      sasset[j] = P.surfaces[j].asset;
+    }
+    o_celloff = pk.add(cell_off);
+    o_sasset = pk.add(sasset);
   }
   uint8_t* base = static_cast<uint8_t*>(W.device(WS_ARENA, pk.host.size()));
   if (tr.has_lv) {
@@ -320,6 +329,14 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   if (tr.has_lv) {
     launch_calibrate(reinterpret_cast<const CalibJob*>(base + o_jobs), P.n_surf, W.stream);
     if (W.timing) W.timing->kernel_launches += 1;
+    if (req->config.precision == RG_PRECISION_FP32) {
+      float2* rows = static_cast<float2*>(W.device(WS_LVROWS, (size_t)P.n_surf * P.T * gx * sizeof(float2)));
+      launch_lvrows(tb.lv_v, reinterpret_cast<const int32_t*>(base + o_celloff),
+                    reinterpret_cast<const int32_t*>(base + o_sasset), tb.lv_ti, tb.lv_tw, P.n_surf,
+                    (int)P.T, gx, rows, W.stream);
+      tb.lv_rows = rows;
+      if (W.timing) W.timing->kernel_launches += 1;
+    }
   }
   launch_cholesky(S.scen, P.n_scen, P.n, W.stream);
   if (W.timing) W.timing->kernel_launches += 1;

@@ -476,9 +476,11 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
     }
     for (int i = 0; i < n_scen; ++i)
       for (int f = 0; f < n; ++f) {
-        P.scen32[i].surf_off[f] = surf_off[P.scen[i].surf[f]];
+        P.scen32[i].surf_off[f] = P.scen[i].surf[f] * (int32_t)T * gx;
         P.scen[i].surf_off[f] = surf_off[P.scen[i].surf[f]];
       }
+    if ((double)P.n_surf * (double)T * (double)gx >= 2147483647.0)
+      raise(RG_ERR_INVALID_ARGUMENT, "too many local-vol surfaces x steps x grid points for one request");
   }
 }
 

@@ -47,8 +47,6 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
   float4* s_lv = reinterpret_cast<float4*>(carve((size_t)S * N * 16));  // (a_u, inv_h, surface offset, x0)
   uint32_t* s_flags = reinterpret_cast<uint32_t*>(carve((size_t)TT * 4));
   int32_t* s_per = reinterpret_cast<int32_t*>(carve((size_t)TT * 4));
-  int2* s_ti = reinterpret_cast<int2*>(carve((size_t)N * TT * 8));
-  float* s_tw = reinterpret_cast<float*>(carve((size_t)N * TT * 4));
   int32_t* s_noff = reinterpret_cast<int32_t*>(carve((size_t)(TT + 1) * 4));
   float* s_ncf = reinterpret_cast<float*>(carve((size_t)NNmax * 4));
   float* wcur = reinterpret_cast<float*>(carve((size_t)PbN * 4));
@@ -114,13 +112,6 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
       for (int i = tid; i < tn; i += blockDim.x) {
         s_flags[i] = __ldg(tb.step_flags + t0 + i);
         s_per[i] = __ldg(tb.step_period + t0 + i);
-        if (LV) {
-#pragma unroll
-          for (int f = 0; f < N; ++f) {
-            s_ti[f * TT + i] = __ldg(tb.lv_ti + f * T + t0 + i);
-            s_tw[f * TT + i] = __ldg(tb.lv_twf + f * T + t0 + i);
-          }
-        }
       }
       for (int i = tid; i <= tn; i += blockDim.x) s_noff[i] = __ldg(tb.node_off + t0 + i);
       for (int i = tid; i < nn; i += blockDim.x) s_ncf[i] = __ldg(tb.node_cf + n0 + i);
@@ -191,6 +182,7 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
       // ---- S: scenario stepping
       if (ok) {
         for (int tt = 0; tt < tn; ++tt) {
+          const int tg = (t0 + tt) * gx;
           float d[N], y[N];
 #pragma unroll
           for (int f = 0; f < N; ++f) d[f] = dW[(tt * N + f) * Pb + pl];
@@ -207,17 +199,16 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
           for (int f = 0; f < N; ++f) {
             float sg;
             if (LV) {
-              const int2 ti = s_ti[f * TT + tt];
-              const float wt = s_tw[f * TT + tt];
+              // sigma at the step's time row, linear in log-spot: u on the grid, floor(u) by a
+              // round-down add of 2^23 (exact for 0 <= u < 2^23), one (value, slope) gather
               const float4 c4 = lvc[f];
               float u = fmaf(x[f], c4.y, c4.x);
               u = fminf(fmaxf(u, 0.0f), gxm1);
-              const int jj = min((int)u, gx - 2);
-              const float w = u - (float)jj;
-              const float2* base = tb.lv_vf + __float_as_int(c4.z) + jj;
-              const float2 lo = __ldg(base + ti.x * gx), hi = __ldg(base + ti.y * gx);
-              const float v0 = fmaf(w, lo.y, lo.x), v1 = fmaf(w, hi.y, hi.x);
-              sg = fmaf(wt, v1 - v0, v0);
+              const float fl = __fadd_rd(u, 8388608.0f);
+              const int jj = __float_as_int(fl) - 0x4B000000;
+              const float w = u - (fl - 8388608.0f);
+              const float2 r = __ldg(tb.lv_rows + (__float_as_int(c4.z) + tg + jj));
+              sg = fmaf(w, r.y, r.x);
             } else {
               sg = sig[f];
             }
@@ -376,8 +367,7 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   sh.TT = tt;
   const int NNmax = tt + P.stack_max;
   size_t bytes = align16((size_t)P.n_scen * RG_ACC * 8) + align16((size_t)P.n_scen * N * 16) +
-                 align16((size_t)tt * 4) * 2 +
-                 align16((size_t)N * tt * 8) + align16((size_t)N * tt * 4) + align16((size_t)(tt + 1) * 4) +
+                 align16((size_t)tt * 4) * 2 + align16((size_t)(tt + 1) * 4) +
                  align16((size_t)NNmax * 4) + align16((size_t)PbN * 4) + align16((size_t)P.stack_max * PbN * 4);
   size_t zbytes = align16((size_t)NNmax * PbN * 4);
   const int g = sh.Pb < 32 ? sh.Pb : 32;
@@ -385,10 +375,13 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   if (zbytes < red) zbytes = align16(red);
   bytes += zbytes + align16((size_t)tt * PbN * 4);
   sh.smem = (int)bytes;
-  for (int rec = 0; rec < 2; ++rec)
-    cuda_check(cudaFuncSetAttribute(select_kernel(P.n, P.trade.has_lv != 0, rec != 0),
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),
+  for (int rec = 0; rec < 2; ++rec) {
+    const void* kr = select_kernel(P.n, P.trade.has_lv != 0, rec != 0);
+    cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),
                "phoenix32 smem attribute");
+    cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+               "phoenix32 carveout");
+  }
   const void* k = select_kernel(P.n, P.trade.has_lv != 0, false);
   int per_sm = 0;
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, sh.threads, sh.smem),

@@ -145,6 +145,34 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
   }
 }
 
+// One CTA per (surface, step): the FP64 row sigma(step·dt, ·) of the surface, linear in tenor
+// (riga-market/src/lib.rs:345-364), stored as FP32 (value, slope to the next node).
+__global__ void lvrows_kernel(const double* __restrict__ lv_v, const int32_t* __restrict__ cell_off,
+                              const int32_t* __restrict__ surf_asset, const int2* __restrict__ lv_ti,
+                              const double* __restrict__ lv_tw, int T, int gx, float2* __restrict__ rows) {
+  const int sfc = blockIdx.x, t = blockIdx.y;
+  const int f = surf_asset[sfc];
+  const int2 ti = lv_ti[f * T + t];
+  const double wt = lv_tw[f * T + t];
+  const double* v0 = lv_v + cell_off[sfc] + ti.x * gx;
+  const double* v1 = lv_v + cell_off[sfc] + ti.y * gx;
+  float2* out = rows + ((size_t)sfc * T + t) * gx;
+  for (int j = threadIdx.x; j < gx; j += blockDim.x) {
+    const double a = (1.0 - wt) * v0[j] + wt * v1[j];
+    const double b = j + 1 < gx ? (1.0 - wt) * v0[j + 1] + wt * v1[j + 1] : a;
+    out[j] = make_float2((float)a, (float)(b - a));
+  }
+}
+
+void launch_lvrows(const double* lv_v, const int32_t* surf_cell_off, const int32_t* surf_asset,
+                   const int2* lv_ti, const double* lv_tw, int n_surf, int T, int gx, float2* rows,
+                   cudaStream_t s) {
+  if (n_surf <= 0) return;
+  lvrows_kernel<<<dim3(n_surf, T), gx < 128 ? 64 : 128, 0, s>>>(lv_v, surf_cell_off, surf_asset, lv_ti,
+                                                                lv_tw, T, gx, rows);
+  cuda_check(cudaGetLastError(), "lvrows_kernel launch");
+}
+
 void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s) {
   if (n_jobs <= 0) return;
   calibrate_kernel<<<n_jobs, 128, 0, s>>>(jobs_dev);

@@ -78,7 +78,7 @@ struct DevScen32 {
   float sig[RG_NMAX];     // flat vol
   float a_u[RG_NMAX];     // (ln initial_spot - log_lo) / h
   float inv_h[RG_NMAX];   // 1 / h on the Dupire log-strike axis
-  int32_t surf_off[RG_NMAX];
+  int32_t surf_off[RG_NMAX];  // first FP32 step row of the scenario's surface: surface·T·gx
 };
 
 // Everything one request needs on the device, after preparation.
@@ -116,7 +116,7 @@ struct Engine;
 
 // The device and host memory one pricing call draws on: the engine's growable buffers, or a fixed
 // region.  Slots are requested in this order within each fused launch.
-enum WsSlot { WS_ARENA = 0, WS_CALIB, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS, WS_NSLOTS };
+enum WsSlot { WS_ARENA = 0, WS_CALIB, WS_LVROWS, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS, WS_NSLOTS };
 struct Workspace {
   cudaStream_t stream = nullptr;
   cudaEvent_t* ev = nullptr;    // six events for the timing breakdown, or null
@@ -159,6 +159,10 @@ struct CalibJob {
 };
 void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s);
 void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s);
+// Per surface and step, the Dupire row interpolated to the step's time, as FP32 (v_j, v_j+1 - v_j).
+void launch_lvrows(const double* lv_v, const int32_t* surf_cell_off, const int32_t* surf_asset,
+                   const int2* lv_ti, const double* lv_tw, int n_surf, int T, int gx, float2* rows,
+                   cudaStream_t s);
 
 struct LaunchOut {
   double* partial;      // [grid][n_scen][RG_ACC]
