@@ -36,11 +36,10 @@ METRIC = "path-steps/sec and trades·bumps/sec at ≤1bp error vs FP64; p50/p99 
 UNIT = "path-steps/s"
 
 
-def workload_request(paths: int, steps: int, fp32: bool = True, first_path: int = 0):
-    from riga_gb300 import workloads
+def workload_request(paths: int, steps: int, fp32: bool = True, rank: int = 0, world: int = 1):
+    from riga_gb300 import sharding, workloads
 
-    req = workloads.lv3(paths=paths, steps=steps, fp32=fp32)
-    req.options.first_path = first_path
+    req = sharding.shard_request(workloads.lv3(paths=paths, steps=steps, fp32=fp32), rank, world)
     scen = [(m, s) for _, m, s in workloads.crn15_scenarios(req)]
     return req, scen
 
@@ -180,7 +179,7 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from riga_gb300 import abi
+    from riga_gb300 import abi, sharding
     from riga_gb300.build import build_library
     from riga_gb300.engine import Engine
     import ctypes as C
@@ -188,7 +187,7 @@ def run_gpu(args):
     build_library()
     eng = Engine(local)
     P, T = args.paths, args.timesteps
-    req, scen = workload_request(P, T, fp32=True, first_path=rank * P)
+    req, scen = workload_request(P, T, fp32=True, rank=rank, world=world)
     n_scen = len(scen)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -220,9 +219,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.MAX)
         # the one gather: every rank's FP64 path sums, merged in rank order on rank 0
-        sums = torch.tensor([list(r.path_sums) for r in res], dtype=torch.float64, device="cuda")
-        gathered = [torch.empty_like(sums) for _ in range(world)]
-        torch.distributed.all_gather(gathered, sums)
+        gathered = sharding.gather_path_sums(res, device=torch.device("cuda", local))
     dev_total_s, wall_total_s = tot[0].item() / 1e3, tot[1].item()
     units = float(P) * T * n_scen * world * args.steps
     value = units / dev_total_s
@@ -231,15 +228,9 @@ def run_gpu(args):
         return
     merged_pv = None
     if world > 1:
-        parts = (abi.PriceResult * world)()
-        for r_, g in enumerate(gathered):
-            parts[r_].path_sums[:] = g[0].tolist()
-            parts[r_].seed = 1
-        out = abi.PriceResult()
-        abi.check(eng.lib, eng.lib.rg_merge_results(parts, world, P * world, C.byref(out)))
-        merged_pv = out.pv
+        merged_pv = sharding.merge_gathered(eng.lib, gathered, P, req.config.seed)[0].pv
     # accuracy: FP32 against the FP64 parity kernel on the same points (outside the timed region)
-    req64, _ = workload_request(P, T, fp32=False, first_path=rank * P)
+    req64, _ = workload_request(P, T, fp32=False, rank=rank, world=world)
     t_acc = time.perf_counter()
     res64 = eng.price_scenarios_raw(req64, scen)
     acc_s = time.perf_counter() - t_acc
@@ -297,7 +288,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--paths", type=int, default=1 << 20)

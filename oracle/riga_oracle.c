@@ -1074,6 +1074,8 @@ typedef struct accum {
   moments pv, ko_funding, ki_put, coupon;
   double put_sum, funding_sum, coupon_sum, coupon_memory_sum;
   uint64_t ko, ki, put_eligible, coupon_paths;
+  /* plain FP64 sums in the slot order rg_price_result.path_sums documents (for shard merges) */
+  double ps[RG_PATH_SUMS];
   int n_trace;
   rg_trace_event trace[RG_TRACE_EVENT_CAP];
 } accum;
@@ -1098,6 +1100,30 @@ static void accum_path(accum* a, const model* m, uint64_t path_id, const path_ou
   a->coupon_sum += coupon_quote - memory_quote;
   a->coupon_memory_sum += memory_quote;
   mom_observe(&a->pv, o->pv);
+  const double pv1 = o->pv - 1.0;
+  a->ps[0] += pv1;
+  a->ps[1] += pv1 * pv1;
+  if (o->ko) {
+    const double f1 = o->funding - 1.0;
+    a->ps[2] += f1;
+    a->ps[3] += f1 * f1;
+    a->ps[12] += 1.0;
+  }
+  if (o->hit_ki) {
+    a->ps[4] += o->put;
+    a->ps[5] += o->put * o->put;
+    a->ps[13] += 1.0;
+  }
+  if (o->received) {
+    a->ps[6] += o->coupon_pv;
+    a->ps[7] += o->coupon_pv * o->coupon_pv;
+    a->ps[15] += 1.0;
+  }
+  a->ps[8] += o->put;
+  a->ps[9] += o->funding;
+  a->ps[10] += coupon_quote - memory_quote;
+  a->ps[11] += memory_quote;
+  if (o->put_eligible) a->ps[14] += 1.0;
 }
 
 static void accum_merge(accum* a, const accum* b) {
@@ -1113,6 +1139,7 @@ static void accum_merge(accum* a, const accum* b) {
   a->ki += b->ki;
   a->put_eligible += b->put_eligible;
   a->coupon_paths += b->coupon_paths;
+  for (int k = 0; k < RG_PATH_SUMS; ++k) a->ps[k] += b->ps[k];
   for (int i = 0; i < b->n_trace && a->n_trace < RG_TRACE_EVENT_CAP; ++i) a->trace[a->n_trace++] = b->trace[i];
 }
 
@@ -1152,6 +1179,7 @@ static void finish_result(const accum* a, uint64_t paths, uint64_t seed, rg_pric
   out->coupon_path_count = a->coupon_paths;
   out->n_trace_events = a->n_trace;
   memcpy(out->trace_events, a->trace, sizeof(rg_trace_event) * (size_t)a->n_trace);
+  memcpy(out->path_sums, a->ps, sizeof a->ps);
 }
 
 /* ---------------------------------------------------------------- threading ----------------- */

@@ -497,6 +497,11 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
       W.timing->d2h_ms += ms[4];
       W.timing->device_ms += ms[0] + ms[1] + ms[2] + ms[3] + ms[4];
     }
+    if (fp32) {
+      // the FP32 kernel poisons its sums with NaN when it was given too little shared memory
+      for (size_t k = 0; k < (size_t)cnt * RG_ACC; ++k)
+        if (!std::isfinite(hs[k])) raise(RG_ERR_GPU_ERROR, "phoenix32: non-finite path sums (launch shape check failed)");
+    }
     for (int i = 0; i < cnt; ++i) finish(hs + (size_t)i * RG_ACC, paths, req->config.seed, &out[first + i]);
     if (trace) collect_trace(W, lo.ko_steps, paths, req->config.first_path, P.trade.dt, &out[first]);
   }

@@ -25,6 +25,38 @@ namespace rg {
 
 #define GEN_CH 8  // consecutive paths per generation task (one Gray-code run)
 
+// Byte offsets of the kernel's dynamic shared-memory regions, 16-byte aligned, and their total.
+// Computed by the same function on the host (to size the launch) and in the kernel (to carve).
+struct P32Layout {
+  uint32_t acc, lv, flags, per, noff, ncf, wcur, stack, z, dw, total;
+};
+
+__host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, int NNmax, int stack_max,
+                                                int threads) {
+  P32Layout L;
+  uint32_t o = 0;
+  auto put = [&o](uint32_t& field, uint32_t bytes) {
+    field = o;
+    o += (bytes + 15u) & ~15u;
+  };
+  const uint32_t PbN = (uint32_t)(Pb * N);
+  const int g = Pb < 32 ? Pb : 32;
+  const uint32_t zb = (uint32_t)NNmax * PbN * 4u;           // normals of the tile's bridge nodes
+  const uint32_t rb = (uint32_t)(threads / g) * RG_ACC * 8u;  // per-tile reduction, aliases Z
+  put(L.acc, (uint32_t)S * RG_ACC * 8u);
+  put(L.lv, (uint32_t)(S * N) * 16u);
+  put(L.flags, (uint32_t)TT * 4u);
+  put(L.per, (uint32_t)TT * 4u);
+  put(L.noff, (uint32_t)(TT + 1) * 4u);
+  put(L.ncf, (uint32_t)NNmax * 4u);
+  put(L.wcur, PbN * 4u);
+  put(L.stack, (uint32_t)stack_max * PbN * 4u);
+  put(L.z, zb > rb ? zb : rb);
+  put(L.dw, (uint32_t)TT * PbN * 4u);
+  L.total = o;
+  return L;
+}
+
 template <int N, bool LV, bool REC>
 __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
@@ -36,23 +68,27 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
   const int PbN = Pb * N;
   const int nch = Pb / GEN_CH;
   const int T = (int)tr.steps;
-  // ---- shared-memory carve-up
-  unsigned char* ptr = smem_raw;
-  auto carve = [&](size_t bytes) {
-    unsigned char* p = ptr;
-    ptr += (bytes + 15) & ~(size_t)15;
-    return p;
-  };
-  double* acc = reinterpret_cast<double*>(carve((size_t)S * RG_ACC * 8));
-  float4* s_lv = reinterpret_cast<float4*>(carve((size_t)S * N * 16));  // (a_u, inv_h, surface offset, x0)
-  uint32_t* s_flags = reinterpret_cast<uint32_t*>(carve((size_t)TT * 4));
-  int32_t* s_per = reinterpret_cast<int32_t*>(carve((size_t)TT * 4));
-  int32_t* s_noff = reinterpret_cast<int32_t*>(carve((size_t)(TT + 1) * 4));
-  float* s_ncf = reinterpret_cast<float*>(carve((size_t)NNmax * 4));
-  float* wcur = reinterpret_cast<float*>(carve((size_t)PbN * 4));
-  float* stack = reinterpret_cast<float*>(carve((size_t)stack_max * PbN * 4));
-  float* Z = reinterpret_cast<float*>(carve((size_t)NNmax * PbN * 4));
-  float* dW = reinterpret_cast<float*>(carve((size_t)TT * PbN * 4));
+  // ---- shared-memory carve-up (the host sizes the launch from the same layout)
+  const P32Layout L = p32_layout(S, N, Pb, TT, NNmax, stack_max, (int)blockDim.x);
+  uint32_t dyn_bytes;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
+  if (L.total > dyn_bytes) {
+    // launched with less shared memory than the layout needs: touch none of it, poison this
+    // block's sums so the host reports the launch as failed
+    for (int k = tid; k < S * RG_ACC; k += blockDim.x)
+      partial[(size_t)blockIdx.x * S * RG_ACC + k] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  double* acc = reinterpret_cast<double*>(smem_raw + L.acc);
+  float4* s_lv = reinterpret_cast<float4*>(smem_raw + L.lv);  // (a_u, inv_h, surface offset, x0)
+  uint32_t* s_flags = reinterpret_cast<uint32_t*>(smem_raw + L.flags);
+  int32_t* s_per = reinterpret_cast<int32_t*>(smem_raw + L.per);
+  int32_t* s_noff = reinterpret_cast<int32_t*>(smem_raw + L.noff);
+  float* s_ncf = reinterpret_cast<float*>(smem_raw + L.ncf);
+  float* wcur = reinterpret_cast<float*>(smem_raw + L.wcur);
+  float* stack = reinterpret_cast<float*>(smem_raw + L.stack);
+  float* Z = reinterpret_cast<float*>(smem_raw + L.z);
+  float* dW = reinterpret_cast<float*>(smem_raw + L.dw);
   double* red = reinterpret_cast<double*>(Z);  // reduction scratch, reused after the time loop
 
   for (int k = tid; k < S * RG_ACC; k += blockDim.x) acc[k] = 0.0;
@@ -351,8 +387,6 @@ static const void* select_kernel(int n, bool lv, bool rec) {
   }
 }
 
-static size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
-
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
   if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
@@ -365,16 +399,7 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   int tt = (12288 / PbN - P.stack_max) / 2;
   tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
   sh.TT = tt;
-  const int NNmax = tt + P.stack_max;
-  size_t bytes = align16((size_t)P.n_scen * RG_ACC * 8) + align16((size_t)P.n_scen * N * 16) +
-                 align16((size_t)tt * 4) * 2 + align16((size_t)(tt + 1) * 4) +
-                 align16((size_t)NNmax * 4) + align16((size_t)PbN * 4) + align16((size_t)P.stack_max * PbN * 4);
-  size_t zbytes = align16((size_t)NNmax * PbN * 4);
-  const int g = sh.Pb < 32 ? sh.Pb : 32;
-  size_t red = (size_t)(sh.threads / g) * RG_ACC * 8;
-  if (zbytes < red) zbytes = align16(red);
-  bytes += zbytes + align16((size_t)tt * PbN * 4);
-  sh.smem = (int)bytes;
+  sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
   for (int rec = 0; rec < 2; ++rec) {
     const void* kr = select_kernel(P.n, P.trade.has_lv != 0, rec != 0);
     cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),

@@ -164,6 +164,28 @@ def test_path_ranges_shard_exactly(engine):
         assert (a.path_id, a.pv, a.ko_step) == (b.path_id, b.pv, b.ko_step)
 
 
+@pytest.mark.parametrize("fp32", [False, True])
+def test_sharded_fused_launches_merge_to_one_launch(engine, fp32):
+    """Two ranks' shards (first_path = rank × paths) of a CRN batch, merged by rg_merge_results,
+    against one launch over both ranges: event counts exact, every price within 1e-12 relative
+    (the shards only reorder FP64 additions)."""
+    from riga_gb300 import sharding
+
+    req = workloads.lv3(paths=1 << 14, steps=126, fp32=fp32)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(req)]
+    parts = [engine.price_scenarios_raw(sharding.shard_request(req, r, 2), scen) for r in range(2)]
+    whole_req = copy.deepcopy(req)
+    whole_req.config.paths *= 2
+    whole = engine.price_scenarios_raw(whole_req, scen)
+    for s in range(len(scen)):
+        m = sharding.merge(engine.lib, [parts[0][s], parts[1][s]], whole_req.config.paths)
+        w = whole[s]
+        assert (m.ko_count, m.ki_count, m.put_eligible_count, m.coupon_path_count) == \
+            (w.ko_count, w.ki_count, w.put_eligible_count, w.coupon_path_count)
+        assert m.pv == pytest.approx(w.pv, rel=1e-12)
+        assert m.mc_error == pytest.approx(w.mc_error, rel=1e-9)
+
+
 def test_repeated_launches_are_bit_identical(engine):
     r = workloads.plain3(1 << 14, steps=126)
     a = engine.price_raw(r)
