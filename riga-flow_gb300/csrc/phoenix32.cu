@@ -15,10 +15,12 @@
 //   S. scenario stepping — every (path, scenario) thread correlates dW with its own Cholesky
 //      factor (the bridge is linear, so L·bridge(z) = bridge(L·z)), steps ln(S/S0) under flat vol
 //      or its scenario's Dupire surface and runs the Phoenix state machine.
-// Generation is paid once per path, not once per scenario.  Path state is FP32; event cash flows,
-// discount factors and every reduction are FP64, in a fixed order (shuffle butterfly within a
-// scenario's warps, warps in index order, blocks in the final reduce kernel), so a launch of a
-// given shape is bit-reproducible.
+// Generation is paid once per path, not once per scenario.  Path state and a path's payoff values
+// are FP32; the 32 paths of a warp are summed in FP32 by a fixed shuffle butterfly, and every
+// sum above that (warps in index order, tiles, blocks in the final reduce kernel) is FP64, so a
+// launch of a given shape is bit-reproducible.  With 16 scenarios a CTA is 1024 threads (64 paths
+// × 16 scenarios, one CTA per SM): each scenario has two warps on the same paths, which share
+// its local-vol rows in L1.
 #include "rg_internal.h"
 
 namespace rg {
@@ -41,7 +43,9 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
   };
   const uint32_t PbN = (uint32_t)(Pb * N);
   const int g = Pb < 32 ? Pb : 32;
-  const uint32_t zb = (uint32_t)NNmax * PbN * 4u;           // normals of the tile's bridge nodes
+  // normals of the tile's bridge nodes, one row of Pb + 4 floats per (node, factor): the padding
+  // spreads a generation pass's stores (lanes stride GEN_CH·nch apart) over distinct banks
+  const uint32_t zb = (uint32_t)NNmax * (uint32_t)N * (uint32_t)(Pb + 4) * 4u;
   const uint32_t rb = (uint32_t)(threads / g) * RG_ACC * 8u;  // per-tile reduction, aliases Z
   put(L.acc, (uint32_t)S * RG_ACC * 8u);
   put(L.lv, (uint32_t)(S * N) * 16u);
@@ -58,7 +62,7 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
 }
 
 template <int N, bool LV, bool REC>
-__global__ void __launch_bounds__(512, 2) phoenix32_kernel(
+__global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
     const DevScen32* __restrict__ scen32, int S, int Pb, int TT, int NNmax, int stack_max,
     float ln_ko, float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths,
@@ -80,7 +84,8 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
     return;
   }
   double* acc = reinterpret_cast<double*>(smem_raw + L.acc);
-  float4* s_lv = reinterpret_cast<float4*>(smem_raw + L.lv);  // (a_u, inv_h, surface offset, x0)
+  // per (scenario, asset): (a_u/(gx-1), inv_h/(gx-1), row offset - 0x4B000000 as bits, x0)
+  float4* s_lv = reinterpret_cast<float4*>(smem_raw + L.lv);
   uint32_t* s_flags = reinterpret_cast<uint32_t*>(smem_raw + L.flags);
   int32_t* s_per = reinterpret_cast<int32_t*>(smem_raw + L.per);
   int32_t* s_noff = reinterpret_cast<int32_t*>(smem_raw + L.noff);
@@ -105,7 +110,9 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
   for (int i = tid; i < S * N; i += blockDim.x) {
     const DevScen32& s3 = scen32[i / N];
     const int f = i % N;
-    s_lv[i] = make_float4(s3.a_u[f], s3.inv_h[f], __int_as_float(s3.surf_off[f]), s3.x0[f]);
+    const float inv_gxm1 = 1.0f / (float)(tr.gx - 1);
+    s_lv[i] = make_float4(s3.a_u[f] * inv_gxm1, s3.inv_h[f] * inv_gxm1,
+                          __int_as_float((int)((uint32_t)s3.surf_off[f] - 0x4B000000u)), s3.x0[f]);
   }
   float Lf[N * (N + 1) / 2], mu[N], sig[N];
   const int ss = lane_ok ? s : 0;
@@ -157,7 +164,7 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
         const int nd = n0 + j;
         const uint64_t g0 = tile0 + (uint64_t)c * GEN_CH;
         if (g0 >= npaths) continue;  // these paths are never read
-        float* zo = Z + (size_t)(j * N + f) * GEN_CH * nch + c;
+        float* zo = Z + (size_t)(j * N + f) * (Pb + 4) + c;
         if (tr.vr == RG_VR_SOBOL) {
           const uint32_t* row = tb.sobol + 32 * (size_t)__ldg(tb.nf_row + nd * N + f);
           uint64_t n = path0 + g0 + 1;
@@ -200,7 +207,7 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
           const int e0 = s_noff[tt], e1 = s_noff[tt + 1];
           for (int nd = e0; nd < e1; ++nd) {
             const int j = nd - n0;
-            const float z = Z[((size_t)(j * N + f) * GEN_CH + pq) * nch + pc];
+            const float z = Z[(size_t)(j * N + f) * (Pb + 4) + pq * nch + pc];
             const float cf = s_ncf[j];
             const float w = nd == 0 ? z * cf : fmaf(z, cf, 0.5f * (wc + stack[(lsp - 1) * PbN + c]));
             stack[lsp * PbN + c] = w;
@@ -235,20 +242,21 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
           for (int f = 0; f < N; ++f) {
             float sg;
             if (LV) {
-              // sigma at the step's time row, linear in log-spot: u on the grid, floor(u) by a
-              // round-down add of 2^23 (exact for 0 <= u < 2^23), one (value, slope) gather
+              // sigma at the step's time row, linear in log-spot.  u01 = the grid position scaled
+              // to [0, 1], clamped by the FMA's saturation (NaN -> 0); 2^23 + floor(u01·(gx-1))
+              // by one round-down FMA, whose bit pattern minus 0x4B000000 is the grid index —
+              // that bias is folded into the row offset c4.z; then one (value, slope) gather
               const float4 c4 = lvc[f];
-              float u = fmaf(x[f], c4.y, c4.x);
-              u = fminf(fmaxf(u, 0.0f), gxm1);
-              const float fl = __fadd_rd(u, 8388608.0f);
-              const int jj = __float_as_int(fl) - 0x4B000000;
-              const float w = u - (fl - 8388608.0f);
-              const float2 r = __ldg(tb.lv_rows + (__float_as_int(c4.z) + tg + jj));
+              const float u01 = __saturatef(fmaf(x[f], c4.y, c4.x));
+              const float fl = __fmaf_rd(u01, gxm1, 8388608.0f);
+              const float w = fmaf(u01, gxm1, 8388608.0f - fl);
+              const uint32_t idx = (uint32_t)__float_as_int(c4.z) + (uint32_t)tg + (uint32_t)__float_as_int(fl);
+              const float2 r = __ldg(tb.lv_rows + idx);
               sg = fmaf(w, r.y, r.x);
             } else {
               sg = sig[f];
             }
-            x[f] += fmaf(sg, y[f], fmaf(nhdt * sg, sg, mu[f]));
+            x[f] = fmaf(sg, fmaf(nhdt, sg, y[f]), x[f]) + mu[f];
             wmin = fminf(wmin, x[f]);
           }
           worst = wmin;
@@ -293,43 +301,48 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
       __syncthreads();
     }
     // ---- path close (note.rs:221-258) and the per-tile reduction
-    double out[RG_ACC];
+    float out[RG_ACC];
 #pragma unroll
-    for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0;
+    for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0f;
     if (ok) {
       const bool ko = ko_step >= 0;
-      const double df_mat = __ldg(tb.df_mat + ss);
-      const double funding = ko ? __ldg(tb.df + (size_t)ss * T + ko_step) : df_mat;
+      const float df_mat = (float)__ldg(tb.df_mat + ss);
+      const float funding = ko ? (float)__ldg(tb.df + (size_t)ss * T + ko_step) : df_mat;
       const bool hit_ki = worst <= ln_ki;
       const bool put_ok = hit_ki && !ko;
-      const double wf = exp((double)worst);
-      const double put = put_ok ? fmax(tr.strike - wf, 0.0) * df_mat : 0.0;
-      const double cn = (double)cpv + (double)mpv;
-      const double pv = funding + cn - put;
-      out[ACC_PV] = pv - 1.0;
-      out[ACC_PV2] = (pv - 1.0) * (pv - 1.0);
+      const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * df_mat : 0.0f;
+      const float cn = cpv + mpv;
+      const float pv1 = (funding - 1.0f) + cn - put;
+      out[ACC_PV] = pv1;
+      out[ACC_PV2] = pv1 * pv1;
       if (ko) {
-        out[ACC_KOF] = funding - 1.0;
-        out[ACC_KOF2] = (funding - 1.0) * (funding - 1.0);
-        out[ACC_NKO] = 1.0;
+        out[ACC_KOF] = funding - 1.0f;
+        out[ACC_KOF2] = (funding - 1.0f) * (funding - 1.0f);
+        out[ACC_NKO] = 1.0f;
       }
       if (hit_ki) {
         out[ACC_KIPUT] = put;
         out[ACC_KIPUT2] = put * put;
-        out[ACC_NKI] = 1.0;
+        out[ACC_NKI] = 1.0f;
       }
       if (received) {
         out[ACC_CPN] = cn;
         out[ACC_CPN2] = cn * cn;
-        out[ACC_NCPN] = 1.0;
+        out[ACC_NCPN] = 1.0f;
       }
       out[ACC_PUT] = put;
       out[ACC_FUND] = funding;
-      out[ACC_CQ] = cn * 10.0 - (double)mpv * 10.0;
-      out[ACC_MQ] = (double)mpv * 10.0;
-      out[ACC_NPUT] = put_ok ? 1.0 : 0.0;
+      out[ACC_CQ] = cpv * 10.0f;
+      out[ACC_MQ] = mpv * 10.0f;
+      out[ACC_NPUT] = put_ok ? 1.0f : 0.0f;
       if (s == 0 && ko_steps) ko_steps[gi] = ko_step;
       if (REC && s == 0 && records) {
+        const double df_mat = __ldg(tb.df_mat + ss);
+        const double funding = ko ? __ldg(tb.df + (size_t)ss * T + ko_step) : df_mat;
+        const double wf = exp((double)worst);
+        const double put = put_ok ? fmax(tr.strike - wf, 0.0) * df_mat : 0.0;
+        const double cn = (double)cpv + (double)mpv;
+        const double pv = funding + cn - put;
         rg_path_record r;
         r.path_id = path0 + gi;
         r.rng_seed = tr.seed;
@@ -356,7 +369,7 @@ __global__ void __launch_bounds__(512, 2) phoenix32_kernel(
       for (int k = 0; k < RG_ACC; ++k) out[k] += __shfl_xor_sync(0xffffffffu, out[k], off);
     if ((lane % g) == 0)
 #pragma unroll
-      for (int k = 0; k < RG_ACC; ++k) red[(size_t)(tid / g) * RG_ACC + k] = out[k];
+      for (int k = 0; k < RG_ACC; ++k) red[(size_t)(tid / g) * RG_ACC + k] = (double)out[k];
     __syncthreads();
     const int groups_per_scen = Pb / g;
     for (int jx = tid; jx < S * RG_ACC; jx += blockDim.x) {
@@ -393,10 +406,10 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   int sb = 1;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
-  sh.threads = sb >= 8 ? 512 : 256;
+  sh.threads = sb >= 8 ? 1024 : 256;
   sh.Pb = sh.threads / sb;
   const int N = P.n, PbN = sh.Pb * N;
-  int tt = (12288 / PbN - P.stack_max) / 2;
+  int tt = (32768 / PbN - P.stack_max) / 2;
   tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
   sh.TT = tt;
   sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
