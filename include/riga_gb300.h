@@ -324,6 +324,53 @@ int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
 int32_t rg_run_paths(rg_engine* engine, const rg_price_request* request, uint64_t first_path,
                      uint64_t count, rg_path_record* out);
 
+/* ------------------------------------------------------------------ books --------------------- */
+/* A book: many Phoenix trades on one asset universe, priced under one common CRN scenario set.
+ * This entry point has no single counterpart in the reference, which prices one trade per
+ * request (price_put_leg, crates/riga-engine/src/lib.rs:183) and each risk scenario by a full
+ * re-simulation (crates/riga-risk/src/lib.rs:573-626).
+ *
+ * Semantics — one universe path set on a common grid of `universe_steps` steps of
+ * dt = universe_maturity_years / universe_steps: path i draws the universe's normals at QMC
+ * point first_path + i + 1, dimension U·step + u for universe asset u (the reference's
+ * N·step + f numbering with N = U), correlates them with the Cholesky factor of the universe
+ * correlation and bridges every asset over the whole grid (note.rs:83-106 with N = U and
+ * T = universe_steps).  A trade on universe assets a_0..a_{n-1} with `steps` = T_j <=
+ * universe_steps runs the reference's step and Phoenix scan (note.rs:129-259) on the first T_j
+ * steps of those assets' increments with the universe dt.  So a book holding one trade on every
+ * universe asset in order, with T_j = universe_steps, prices exactly that trade's
+ * price_put_leg; a shorter trade reads a truncation of the same Brownian paths. */
+#define RG_BOOK_MAX_UNIVERSE 32
+
+typedef struct rg_book_trade {
+  rg_phoenix_trade terms;     /* maturity_years must be steps × the universe dt (1e-12 relative) */
+  const int32_t* underlyings; /* [terms.n_assets] distinct universe indices */
+} rg_book_trade;
+
+typedef struct rg_book_request {
+  rg_market_snapshot universe; /* base market, n_assets = U <= RG_BOOK_MAX_UNIVERSE, U×U correlation */
+  int64_t universe_steps;
+  double universe_maturity_years;
+  int32_t n_trades;
+  const rg_book_trade* trades; /* [n_trades] */
+  rg_simulation_config config; /* Sobol or Halton; trace_level must be RG_TRACE_OFF */
+} rg_book_request;
+
+/* Prices every trade of the book under every scenario: out[j * S + s] is trade j under
+ * scenarios[s], S = n_scenarios (scenarios NULL and n_scenarios 0: the base market alone, S = 1).
+ * A scenario is a market of the universe (n_assets = U) that keeps the base correlation — its
+ * `correlation` is NULL or equal to the base — so every scenario reads the same paths; spots,
+ * vols, dividend yields and the rate may differ. */
+int32_t rg_price_book(rg_engine* engine, const rg_book_request* request,
+                      const rg_market_snapshot* scenarios, int32_t n_scenarios,
+                      rg_price_result* out);
+
+/* Per-path records of book paths [first_path, first_path + count) for every (trade, scenario):
+ * out[(p * n_trades + j) * S + s] (explain.rs:90-316 applied to each trade of the book). */
+int32_t rg_book_run_paths(rg_engine* engine, const rg_book_request* request,
+                          const rg_market_snapshot* scenarios, int32_t n_scenarios,
+                          uint64_t first_path, uint64_t count, rg_path_record* out);
+
 /* ------------------------------------------------------------------ host tables --------------- */
 /* The Sobol direction table v[dim][32] the engine uses for `dim` dimensions: dimension 0 is van
  * der Corput, dimension d >= 1 the Joe–Kuo recurrence with unit initial values on the d-th

@@ -163,6 +163,41 @@ def price_scenarios(request, scenarios, threads: int = 0):
     return out
 
 
+def price_book(book, scenarios=None, threads: int = 0):
+    """A book (``riga_gb300.types.BookRequest``) under a common scenario set: ``out[j * S + s]``."""
+    from riga_gb300.types import markets_to_abi
+
+    a = book.to_abi()
+    keep = []
+    arr, n = markets_to_abi(scenarios, keep.append)
+    S = max(1, n)
+    out = (abi.PriceResult * (len(book.trades) * S))()
+    th = threads if threads > 0 else (os.cpu_count() or 1)
+    L = lib()
+    L.or_price_book.restype = C.c_int32
+    L.or_price_book.argtypes = [C.POINTER(abi.BookRequest), C.POINTER(abi.Market), C.c_int32, C.c_int32,
+                                C.POINTER(abi.PriceResult)]
+    _check(L.or_price_book(a.ptr, arr, n, th, out))
+    return list(out)
+
+
+def book_run_paths(book, scenarios, first: int, count: int):
+    """Per-path records ``out[(p * n_trades + j) * S + s]`` of book paths [first, first + count)."""
+    from riga_gb300.types import markets_to_abi
+
+    a = book.to_abi()
+    keep = []
+    arr, n = markets_to_abi(scenarios, keep.append)
+    S = max(1, n)
+    out = (abi.PathRecord * (count * len(book.trades) * S))()
+    L = lib()
+    L.or_book_run_paths.restype = C.c_int32
+    L.or_book_run_paths.argtypes = [C.POINTER(abi.BookRequest), C.POINTER(abi.Market), C.c_int32, C.c_uint64,
+                                    C.c_uint64, C.POINTER(abi.PathRecord)]
+    _check(L.or_book_run_paths(a.ptr, arr, n, first, count, out))
+    return list(out)
+
+
 def price_risk_batch(request, cfg: abi.CentralDifferenceConfig, threads: int = 0):
     a = request.to_abi()
     out = abi.BatchRiskReport()

@@ -790,7 +790,8 @@ typedef struct model {
   int n;
   int64_t steps, periods, call_start;
   double dt, rate, maturity;
-  double spots[NMAX], init[NMAX], vols[NMAX], q[NMAX], L[NMAX * NMAX];
+  double spots[NMAX], init[NMAX], vols[NMAX], q[NMAX];
+  double L[RG_BOOK_MAX_UNIVERSE * RG_BOOK_MAX_UNIVERSE]; /* n × n, row-major */
   double call_barrier, coupon_barrier, coupon_rate, strike, ki;
   int fixed_first, memory, trace;
   int has_lv;
@@ -812,6 +813,39 @@ static void model_free(model* m) {
   free(m->hal_perm);
   free(m->hal_bases);
   memset(m, 0, sizeof *m);
+}
+
+/* QMC tables of a model with `need` = N·T normals per path (Ladder set-up, note.rs:58-63,
+ * qmc.rs:93-117, 247-262). */
+static void qmc_init(model* m, const rg_simulation_config* c, int64_t need) {
+  m->vr = c->variance_reduction;
+  m->seed = c->seed;
+  m->first_path = c->first_path;
+  m->scrambler = c->scrambler;
+  if (m->vr == RG_VR_SOBOL) {
+    int64_t d = (int64_t)c->qmc_dimension;
+    if (c->dim_mode == RG_DIM_FULL) {
+      if (d < need) d = need;
+    } else {
+      if (d < 1) d = 1;
+      if (d > QMC_MAX_DIM) d = QMC_MAX_DIM;
+    }
+    m->sob_dim = d;
+    m->sob_v = (uint32_t*)malloc(sizeof(uint32_t) * 32 * (size_t)d);
+    or_sobol_table(d, m->sob_v);
+  } else if (m->vr == RG_VR_HALTON) {
+    int64_t d = (int64_t)c->qmc_dimension;
+    if (d < 1) d = 1;
+    if (d > QMC_MAX_DIM) d = QMC_MAX_DIM;
+    m->hal_dim = (int32_t)d;
+    m->hal_bases = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)d);
+    or_first_primes((int32_t)d, m->hal_bases);
+    m->hal_perm = (uint32_t**)calloc((size_t)d, sizeof(uint32_t*));
+    for (int i = 0; i < d; ++i) {
+      m->hal_perm[i] = (uint32_t*)malloc(sizeof(uint32_t) * m->hal_bases[i]);
+      or_halton_permutation(m->hal_bases[i], m->seed, m->hal_perm[i]);
+    }
+  }
 }
 
 /* price_full_phoenix set-up, note.rs:38-63 and build_local_vol, lib.rs:326-343.
@@ -862,35 +896,7 @@ static int32_t model_init(model* m, const rg_price_request* r, const rg_market_s
   }
   st = or_cholesky(mk->correlation, n, m->L);
   if (st) { model_free(m); return st; }
-  m->vr = r->config.variance_reduction;
-  m->seed = r->config.seed;
-  m->first_path = r->config.first_path;
-  m->scrambler = r->config.scrambler;
-  if (m->vr == RG_VR_SOBOL) {
-    int64_t d = (int64_t)r->config.qmc_dimension;
-    if (r->config.dim_mode == RG_DIM_FULL) {
-      int64_t need = (int64_t)n * m->steps;
-      if (d < need) d = need;
-    } else {
-      if (d < 1) d = 1;
-      if (d > QMC_MAX_DIM) d = QMC_MAX_DIM;
-    }
-    m->sob_dim = d;
-    m->sob_v = (uint32_t*)malloc(sizeof(uint32_t) * 32 * (size_t)d);
-    or_sobol_table(d, m->sob_v);
-  } else if (m->vr == RG_VR_HALTON) {
-    int64_t d = (int64_t)r->config.qmc_dimension;
-    if (d < 1) d = 1;
-    if (d > QMC_MAX_DIM) d = QMC_MAX_DIM;
-    m->hal_dim = (int32_t)d;
-    m->hal_bases = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)d);
-    or_first_primes((int32_t)d, m->hal_bases);
-    m->hal_perm = (uint32_t**)calloc((size_t)d, sizeof(uint32_t*));
-    for (int i = 0; i < d; ++i) {
-      m->hal_perm[i] = (uint32_t*)malloc(sizeof(uint32_t) * m->hal_bases[i]);
-      or_halton_permutation(m->hal_bases[i], m->seed, m->hal_perm[i]);
-    }
-  }
+  qmc_init(m, &r->config, (int64_t)n * m->steps);
   return RG_OK;
 }
 
@@ -937,12 +943,12 @@ static void chol_apply(const double* L, int n, const double* z, double* y) {
   }
 }
 
-/* One path of note.rs:81-259 (QMC lanes). */
-static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chacha8* mc, path_out* o) {
+/* Normals → correlation → bridge of one path (note.rs:83-127): ws->incr[f][step] = ΔW/√dt. */
+static void path_increments(const model* m, uint64_t path_id, workspace* ws, chacha8* mc) {
   const int n = m->n;
   const int64_t T = m->steps;
   const double dt = m->dt;
-  double z[NMAX], y[NMAX];
+  double z[RG_BOOK_MAX_UNIVERSE], y[RG_BOOK_MAX_UNIVERSE];
   if (m->vr == RG_VR_NONE) {
     /* pseudo-random lane: n draws per step then L·z, note.rs:123-127 */
     for (int64_t s = 0; s < T; ++s) {
@@ -963,6 +969,14 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
       for (int64_t s = 0; s < T; ++s) ws->incr[(size_t)f * T + s] *= inv_sqrt_dt;
     }
   }
+}
+
+/* The Euler step and the Phoenix scan of one path (note.rs:129-259) over increment rows
+ * incr[f][0..steps-1]; `stride` is the distance between consecutive steps of one row. */
+static void scan_path(const model* m, const double* const* incr, path_out* o) {
+  const int n = m->n;
+  const int64_t T = m->steps;
+  const double dt = m->dt;
   double spots[NMAX];
   for (int f = 0; f < n; ++f) spots[f] = m->spots[f];
   int ko = 0, received = 0;
@@ -977,7 +991,7 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
     for (int f = 0; f < n; ++f) {
       double vol = m->has_lv ? or_lv_sigma(&m->lv[f], (double)step * dt, spots[f]) : m->vols[f];
       double drift = (m->rate - m->q[f] - 0.5 * vol * vol) * dt;
-      spots[f] *= OEXP(drift + vol * sqrt(dt) * ws->incr[(size_t)f * T + step]);
+      spots[f] *= OEXP(drift + vol * sqrt(dt) * incr[f][step]);
     }
     double worst = spots[0] / m->init[0];
     for (int f = 1; f < n; ++f) worst = fmin(worst, spots[f] / m->init[f]);
@@ -1048,6 +1062,14 @@ static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chach
   o->hit_ki = hit_ki;
   o->put_eligible = put_eligible;
   o->received = received;
+}
+
+/* One path of note.rs:81-259. */
+static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chacha8* mc, path_out* o) {
+  path_increments(m, path_id, ws, mc);
+  const double* rows[NMAX];
+  for (int f = 0; f < m->n; ++f) rows[f] = ws->incr + (size_t)f * (size_t)m->steps;
+  scan_path(m, rows, o);
 }
 
 /* ---------------------------------------------------------------- aggregation --------------- */
@@ -1464,5 +1486,260 @@ int32_t or_price_risk_batch(const rg_price_request* r, const rg_central_differen
   out->correlation_bump = c->correlation_absolute_bump;
   out->pv_mc_error = res[0].mc_error;
   free(res);
+  return RG_OK;
+}
+
+/* ============================================================ books ========================== */
+/* One universe path set priced for many trades under a common scenario set: the reference's
+ * path generation (note.rs:83-106) run once per path for all U universe assets on the universe
+ * grid, then, for every (trade, scenario), the reference's step and Phoenix scan
+ * (note.rs:129-259) over the first T_j steps of the trade's assets. */
+
+#define BOOK_CHUNK_PATHS 256
+
+typedef struct book_ctx {
+  const rg_book_request* r;
+  int32_t n_scen; /* S >= 1 */
+  const rg_market_snapshot* scen; /* [S] */
+  model uni;      /* universe generation model: n = U, steps = universe_steps */
+  model* tm;      /* [n_trades * S] scan models */
+} book_ctx;
+
+static int32_t book_validate(const rg_book_request* r, const rg_market_snapshot* sc, int32_t n_scen) {
+  const rg_market_snapshot* u = &r->universe;
+  int U = u->n_assets;
+  if (!u->as_of || u->as_of[0] == 0) return fail(RG_ERR_MISSING_AS_OF, "as_of is required");
+  if (U < 1 || U > RG_BOOK_MAX_UNIVERSE || !u->spots || !u->vols || !u->dividend_yields || !u->correlation)
+    return fail(RG_ERR_INVALID_MARKET_SHAPE, "the universe needs 1..%d assets with aligned arrays", RG_BOOK_MAX_UNIVERSE);
+  if (r->config.paths == 0 || r->config.path_block_size == 0)
+    return fail(RG_ERR_INVALID_PATHS, "paths and path_block_size must be positive");
+  if (r->universe_steps <= 0 || !isfinite(r->universe_maturity_years) || r->universe_maturity_years <= 0.0)
+    return fail(RG_ERR_INVALID_SCHEDULE, "universe steps and maturity must be positive and finite");
+  if (r->n_trades < 1 || !r->trades) return fail(RG_ERR_INVALID_ARGUMENT, "a book needs at least one trade");
+  if (r->config.variance_reduction != RG_VR_SOBOL && r->config.variance_reduction != RG_VR_HALTON)
+    return fail(RG_ERR_UNSUPPORTED, "books run the Sobol or Halton lane");
+  if (r->config.trace_level != RG_TRACE_OFF)
+    return fail(RG_ERR_INVALID_ARGUMENT, "books record no trace events (trace_level must be off)");
+  if (n_scen < 0 || (n_scen > 0 && !sc)) return fail(RG_ERR_INVALID_ARGUMENT, "bad scenario list");
+  for (int s = 0; s < n_scen; ++s) {
+    if (sc[s].n_assets != U || !sc[s].spots || !sc[s].vols || !sc[s].dividend_yields)
+      return fail(RG_ERR_INVALID_MARKET_SHAPE, "scenario %d is not a market of the universe", s);
+    if (sc[s].correlation && memcmp(sc[s].correlation, u->correlation, sizeof(double) * (size_t)U * (size_t)U) != 0)
+      return fail(RG_ERR_INVALID_ARGUMENT, "scenario %d changes the correlation; book scenarios share the base paths", s);
+  }
+  const double dt = r->universe_maturity_years / (double)r->universe_steps;
+  double sub_spots[NMAX], sub_vols[NMAX], sub_q[NMAX], sub_rho[NMAX * NMAX];
+  for (int j = 0; j < r->n_trades; ++j) {
+    const rg_book_trade* bt = &r->trades[j];
+    const rg_phoenix_trade* t = &bt->terms;
+    int n = t->n_assets;
+    if (n < 1 || n > NMAX || !bt->underlyings)
+      return fail(RG_ERR_INVALID_MARKET_SHAPE, "trade %d needs 1..%d underlyings", j, NMAX);
+    for (int f = 0; f < n; ++f) {
+      int a = bt->underlyings[f];
+      if (a < 0 || a >= U) return fail(RG_ERR_INVALID_MARKET_SHAPE, "trade %d underlying %d is outside the universe", j, a);
+      for (int g = 0; g < f; ++g)
+        if (bt->underlyings[g] == a) return fail(RG_ERR_INVALID_MARKET_SHAPE, "trade %d repeats underlying %d", j, a);
+    }
+    if (t->steps < 1 || t->steps > r->universe_steps)
+      return fail(RG_ERR_INVALID_SCHEDULE, "trade %d steps must be in 1..universe_steps", j);
+    if (!(fabs(t->maturity_years - (double)t->steps * dt) <= 1e-12 * t->maturity_years))
+      return fail(RG_ERR_INVALID_SCHEDULE, "trade %d maturity must be steps x the universe dt", j);
+    /* the reference's own request checks on the trade and its slice of the base market */
+    for (int f = 0; f < n; ++f) {
+      int a = bt->underlyings[f];
+      sub_spots[f] = u->spots[a];
+      sub_vols[f] = u->vols[a];
+      sub_q[f] = u->dividend_yields[a];
+      for (int g = 0; g < n; ++g) sub_rho[f * n + g] = u->correlation[a * U + bt->underlyings[g]];
+    }
+    rg_price_request q;
+    memset(&q, 0, sizeof q);
+    q.trade = *t;
+    q.market = *u;
+    q.market.n_assets = n;
+    q.market.spots = sub_spots;
+    q.market.vols = sub_vols;
+    q.market.dividend_yields = sub_q;
+    q.market.correlation = sub_rho;
+    q.config = r->config;
+    q.as_of = u->as_of;
+    int32_t st = or_validate(&q);
+    if (st) return st;
+  }
+  return RG_OK;
+}
+
+/* The scan model of trade `t` on underlyings `idx` under universe market `mk`. */
+static void book_trade_model(model* m, const rg_phoenix_trade* t, const int32_t* idx,
+                             const rg_market_snapshot* mk, double dt) {
+  memset(m, 0, sizeof *m);
+  m->n = t->n_assets;
+  m->steps = t->steps;
+  m->periods = t->has_coupon_periods ? t->coupon_periods : 9;
+  if (m->periods < 1) m->periods = 1;
+  m->call_start = t->has_call_start_step ? t->call_start_step : 0;
+  m->dt = dt;
+  m->rate = mk->risk_free_rate;
+  m->maturity = t->maturity_years;
+  for (int f = 0; f < m->n; ++f) {
+    m->spots[f] = mk->spots[idx[f]];
+    m->init[f] = t->initial_spots[f];
+    m->vols[f] = mk->vols[idx[f]];
+    m->q[f] = mk->dividend_yields[idx[f]];
+  }
+  m->call_barrier = t->has_knock_out_barrier ? t->knock_out_barrier : INFINITY;
+  m->coupon_barrier = t->has_coupon_barrier ? t->coupon_barrier : INFINITY;
+  m->coupon_rate = t->has_coupon_rate ? t->coupon_rate : 0.0;
+  m->strike = t->strike;
+  m->ki = t->knock_in_barrier;
+  m->fixed_first = t->fixed_first_coupon != 0;
+  m->memory = t->memory_coupon != 0;
+}
+
+static int32_t book_init(book_ctx* b, const rg_book_request* r, const rg_market_snapshot* sc, int32_t n_scen) {
+  memset(b, 0, sizeof *b);
+  int32_t st = book_validate(r, sc, n_scen);
+  if (st) return st;
+  b->r = r;
+  b->n_scen = n_scen > 0 ? n_scen : 1;
+  b->scen = n_scen > 0 ? sc : &r->universe;
+  model* u = &b->uni;
+  u->n = r->universe.n_assets;
+  u->steps = r->universe_steps;
+  u->dt = r->universe_maturity_years / (double)r->universe_steps;
+  st = or_cholesky(r->universe.correlation, u->n, u->L);
+  if (st) return st;
+  qmc_init(u, &r->config, (int64_t)u->n * u->steps);
+  b->tm = (model*)malloc(sizeof(model) * (size_t)r->n_trades * (size_t)b->n_scen);
+  for (int j = 0; j < r->n_trades; ++j)
+    for (int s = 0; s < b->n_scen; ++s)
+      book_trade_model(&b->tm[(size_t)j * b->n_scen + s], &r->trades[j].terms, r->trades[j].underlyings,
+                       &b->scen[s], u->dt);
+  return RG_OK;
+}
+
+static void book_free(book_ctx* b) {
+  model_free(&b->uni);
+  free(b->tm);
+  b->tm = NULL;
+}
+
+/* All (trade, scenario) outcomes of one path: o[j * S + s]. */
+static void book_path(const book_ctx* b, uint64_t p, workspace* ws, path_out* o) {
+  path_increments(&b->uni, p, ws, NULL);
+  const rg_book_request* r = b->r;
+  const int64_t TU = b->uni.steps;
+  for (int j = 0; j < r->n_trades; ++j) {
+    const double* rows[NMAX];
+    for (int f = 0; f < r->trades[j].terms.n_assets; ++f)
+      rows[f] = ws->incr + (size_t)r->trades[j].underlyings[f] * (size_t)TU;
+    for (int s = 0; s < b->n_scen; ++s)
+      scan_path(&b->tm[(size_t)j * b->n_scen + s], rows, &o[(size_t)j * b->n_scen + s]);
+  }
+}
+
+typedef struct book_job {
+  const book_ctx* b;
+  uint64_t paths, n_chunks, next;
+  size_t pairs;
+  accum* chunks; /* [n_chunks][pairs] */
+  pthread_mutex_t lock;
+} book_job;
+
+static void* book_worker(void* arg) {
+  book_job* j = (book_job*)arg;
+  const book_ctx* b = j->b;
+  workspace ws;
+  ws_alloc(&ws, b->uni.n, b->uni.steps);
+  path_out* o = (path_out*)malloc(sizeof(path_out) * j->pairs);
+  for (;;) {
+    pthread_mutex_lock(&j->lock);
+    uint64_t c = j->next++;
+    pthread_mutex_unlock(&j->lock);
+    if (c >= j->n_chunks) break;
+    accum* a = j->chunks + c * j->pairs;
+    memset(a, 0, sizeof(accum) * j->pairs);
+    uint64_t lo = c * BOOK_CHUNK_PATHS, hi = lo + BOOK_CHUNK_PATHS < j->paths ? lo + BOOK_CHUNK_PATHS : j->paths;
+    for (uint64_t p = lo; p < hi; ++p) {
+      book_path(b, p, &ws, o);
+      for (size_t k = 0; k < j->pairs; ++k) accum_path(&a[k], &b->tm[k], p, &o[k]);
+    }
+  }
+  free(o);
+  ws_free(&ws);
+  return NULL;
+}
+
+int32_t or_price_book(const rg_book_request* r, const rg_market_snapshot* sc, int32_t n_scen,
+                      int32_t threads, rg_price_result* out) {
+  book_ctx b;
+  int32_t st = book_init(&b, r, sc, n_scen);
+  if (st) return st;
+  book_job j;
+  j.b = &b;
+  j.paths = r->config.paths;
+  j.pairs = (size_t)r->n_trades * (size_t)b.n_scen;
+  j.n_chunks = (j.paths + BOOK_CHUNK_PATHS - 1) / BOOK_CHUNK_PATHS;
+  j.chunks = (accum*)calloc((size_t)j.n_chunks * j.pairs, sizeof(accum));
+  j.next = 0;
+  pthread_mutex_init(&j.lock, NULL);
+  int nt = threads > 0 ? threads : 1;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+  for (int i = 0; i < nt; ++i) pthread_create(&th[i], NULL, book_worker, &j);
+  for (int i = 0; i < nt; ++i) pthread_join(th[i], NULL);
+  for (size_t k = 0; k < j.pairs; ++k) {
+    accum total;
+    memset(&total, 0, sizeof total);
+    for (uint64_t c = 0; c < j.n_chunks; ++c) accum_merge(&total, &j.chunks[c * j.pairs + k]);
+    finish_result(&total, r->config.paths, r->config.seed, &out[k]);
+  }
+  pthread_mutex_destroy(&j.lock);
+  free(th);
+  free(j.chunks);
+  book_free(&b);
+  return RG_OK;
+}
+
+int32_t or_book_run_paths(const rg_book_request* r, const rg_market_snapshot* sc, int32_t n_scen,
+                          uint64_t first, uint64_t count, rg_path_record* out) {
+  book_ctx b;
+  int32_t st = book_init(&b, r, sc, n_scen);
+  if (st) return st;
+  if (first + count > r->config.paths) {
+    book_free(&b);
+    return fail(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count %llu",
+                (unsigned long long)r->config.paths);
+  }
+  size_t pairs = (size_t)r->n_trades * (size_t)b.n_scen;
+  workspace ws;
+  ws_alloc(&ws, b.uni.n, b.uni.steps);
+  path_out* o = (path_out*)malloc(sizeof(path_out) * pairs);
+  for (uint64_t i = 0; i < count; ++i) {
+    uint64_t p = first + i;
+    book_path(&b, p, &ws, o);
+    for (size_t k = 0; k < pairs; ++k) {
+      rg_path_record* rec = &out[i * pairs + k];
+      memset(rec, 0, sizeof *rec);
+      rec->path_id = b.uni.first_path + p;
+      rec->rng_seed = r->config.seed;
+      rec->sobol_index = b.uni.first_path + p + 1;
+      rec->worst_final = o[k].worst_final;
+      rec->knocked_out = o[k].ko;
+      rec->ko_step = o[k].ko_step;
+      rec->ko_time = o[k].ko ? o[k].redemption_time : NAN;
+      rec->ki_hit = o[k].hit_ki;
+      rec->qualified_steps = o[k].qualified;
+      rec->paid_periods = o[k].paid;
+      rec->put_payoff = o[k].put;
+      rec->coupon_pv = o[k].coupon_pv;
+      rec->memory_coupon_pv = o[k].memory_pv;
+      rec->funding = o[k].funding;
+      rec->pv = o[k].pv;
+    }
+  }
+  free(o);
+  ws_free(&ws);
+  book_free(&b);
   return RG_OK;
 }

@@ -78,6 +78,11 @@ int32_t or_run_paths(const rg_price_request* req, uint64_t first, uint64_t count
 /* Scenario batch: each scenario re-priced with the request's seed (CRN). */
 int32_t or_price_scenarios(const rg_price_request* req, const rg_scenario* sc, int32_t n,
                            int32_t threads, rg_price_result* out);
+/* --- books: one universe path set, many trades, a common scenario set (threads >= 1) --- */
+int32_t or_price_book(const rg_book_request* req, const rg_market_snapshot* sc, int32_t n_scen,
+                      int32_t threads, rg_price_result* out /* [n_trades * S] */);
+int32_t or_book_run_paths(const rg_book_request* req, const rg_market_snapshot* sc, int32_t n_scen,
+                          uint64_t first, uint64_t count, rg_path_record* out);
 /* riga-risk price_risk_batch (+ price_central_greeks). */
 int32_t or_price_risk_batch(const rg_price_request* req, const rg_central_difference_config* cfg,
                             int32_t threads, rg_batch_risk_report* out);

@@ -150,20 +150,6 @@ static void launch_lv(const LvArgs& A, cudaStream_t st) {
 // ==================================================================== C ABI ===================
 using namespace rg;
 
-int32_t rg_guard_device();  // capi.cu: ensures a usable device (gpu_unavailable otherwise)
-
-#define RG_TRY(...)                            \
-  try {                                         \
-    __VA_ARGS__;                                \
-    return RG_OK;                               \
-  } catch (const rg::Error& e) {                \
-    rg::set_last_error(e.message);              \
-    return e.status;                            \
-  } catch (const std::bad_alloc&) {             \
-    rg::set_last_error("host allocation failed"); \
-    return RG_ERR_GPU_ERROR;                    \
-  }
-
 namespace {
 template <class T>
 T* dev_copy(const T* host, size_t count, cudaStream_t st) {

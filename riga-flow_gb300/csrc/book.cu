@@ -1,0 +1,416 @@
+// book.cu — host side of book pricing: validation, tables, the chunked two-stream pipeline and
+// the C entry points rg_price_book / rg_book_run_paths.
+//
+// Pipeline of one book call (engine stream S0, generation stream S1):
+//   validate (each trade with the reference's request checks on its slice of the universe) →
+//   host tables (QMC, bridge schedule over the universe grid, per-trade constants, per-scenario
+//   discount factors) → one packed H2D copy → universe Cholesky (FP64, device) →
+//   for each chunk of paths: generation of the chunk's universe increments on S1 into one of two
+//   buffers, then the scan of every (trade, scenario) on S0; chunk k+1 generates while chunk k is
+//   scanned → fixed-order reduce over path blocks → one D2H copy → PriceResults.
+// FP64 parity mode runs the same pipeline with the FP64 kernels and no overlap.
+#include <algorithm>
+#include <cmath>
+
+#include "rg_internal.h"
+
+namespace rg {
+
+namespace {
+
+enum BookSlot { BK_TABLES = 0, BK_INCR0, BK_INCR1, BK_PARTIAL, BK_SUMS, BK_RECORDS, BK_SCRATCH, BK_NSLOTS };
+static_assert(BK_NSLOTS <= 8, "engine book buffers");
+
+// Byte budget of one increments buffer (two are in flight).
+constexpr size_t kIncrBudget = size_t(6) << 30;
+
+struct BookPlan {
+  int U = 0, S = 0, n_trades = 0;
+  int64_t TU = 0;
+  double dt = 0;
+  DevTrade gen{};
+  Prepared br;  // bridge schedule of the universe grid (node_* and stack_max only)
+  std::vector<int32_t> nf_row;
+  std::vector<uint32_t> nf_shift;
+  std::vector<BookTradeDev> trades;
+  std::vector<BookScenDev> scen;
+  std::vector<BookPair32> pair32;
+  std::vector<double> df, dfm;
+  std::vector<int32_t> order;
+};
+
+void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen) {
+  if (!r) raise(RG_ERR_INVALID_ARGUMENT, "request is null");
+  const rg_market_snapshot& u = r->universe;
+  const int U = u.n_assets;
+  if (!u.as_of || !u.as_of[0]) raise(RG_ERR_MISSING_AS_OF, "as_of is required");
+  if (U < 1 || U > RG_BOOK_MAX_UNIVERSE || !u.spots || !u.vols || !u.dividend_yields || !u.correlation)
+    raise(RG_ERR_INVALID_MARKET_SHAPE, "the universe needs 1..32 assets with aligned arrays");
+  const rg_simulation_config& c = r->config;
+  if (c.paths == 0 || c.path_block_size == 0) raise(RG_ERR_INVALID_PATHS, "paths and path_block_size must be positive");
+  if (r->universe_steps <= 0 || !std::isfinite(r->universe_maturity_years) || r->universe_maturity_years <= 0.0)
+    raise(RG_ERR_INVALID_SCHEDULE, "universe steps and maturity must be positive and finite");
+  if (r->universe_steps > (int64_t(1) << 22)) raise(RG_ERR_INVALID_SCHEDULE, "at most 2^22 steps are supported");
+  if (r->n_trades < 1 || !r->trades) raise(RG_ERR_INVALID_ARGUMENT, "a book needs at least one trade");
+  if (c.variance_reduction != RG_VR_SOBOL && c.variance_reduction != RG_VR_HALTON)
+    raise(RG_ERR_UNSUPPORTED, "books run the Sobol or Halton lane");
+  if (c.trace_level != RG_TRACE_OFF)
+    raise(RG_ERR_INVALID_ARGUMENT, "books record no trace events (trace_level must be off)");
+  if (n_scen < 0 || (n_scen > 0 && !sc)) raise(RG_ERR_INVALID_ARGUMENT, "bad scenario list");
+  for (int s = 0; s < n_scen; ++s) {
+    if (sc[s].n_assets != U || !sc[s].spots || !sc[s].vols || !sc[s].dividend_yields)
+      raise(RG_ERR_INVALID_MARKET_SHAPE, "scenario " + std::to_string(s) + " is not a market of the universe");
+    if (sc[s].correlation &&
+        memcmp(sc[s].correlation, u.correlation, sizeof(double) * (size_t)U * (size_t)U) != 0)
+      raise(RG_ERR_INVALID_ARGUMENT,
+            "scenario " + std::to_string(s) + " changes the correlation; book scenarios share the base paths");
+  }
+  const double dt = r->universe_maturity_years / (double)r->universe_steps;
+  double sub_spots[RG_NMAX], sub_vols[RG_NMAX], sub_q[RG_NMAX], sub_rho[RG_NMAX * RG_NMAX];
+  for (int j = 0; j < r->n_trades; ++j) {
+    const rg_book_trade& bt = r->trades[j];
+    const rg_phoenix_trade& t = bt.terms;
+    const int n = t.n_assets;
+    const std::string tag = "trade " + std::to_string(j);
+    if (n < 1 || n > RG_NMAX || !bt.underlyings)
+      raise(RG_ERR_INVALID_MARKET_SHAPE, tag + " needs 1..5 underlyings");
+    for (int f = 0; f < n; ++f) {
+      const int a = bt.underlyings[f];
+      if (a < 0 || a >= U) raise(RG_ERR_INVALID_MARKET_SHAPE, tag + " has an underlying outside the universe");
+      for (int g = 0; g < f; ++g)
+        if (bt.underlyings[g] == a) raise(RG_ERR_INVALID_MARKET_SHAPE, tag + " repeats an underlying");
+    }
+    if (t.steps < 1 || t.steps > r->universe_steps)
+      raise(RG_ERR_INVALID_SCHEDULE, tag + " steps must be in 1..universe_steps");
+    if (!(std::fabs(t.maturity_years - (double)t.steps * dt) <= 1e-12 * t.maturity_years))
+      raise(RG_ERR_INVALID_SCHEDULE, tag + " maturity must be steps x the universe dt");
+    // the reference's request checks on the trade and its slice of the base market
+    for (int f = 0; f < n; ++f) {
+      const int a = bt.underlyings[f];
+      sub_spots[f] = u.spots[a];
+      sub_vols[f] = u.vols[a];
+      sub_q[f] = u.dividend_yields[a];
+      for (int g = 0; g < n; ++g) sub_rho[f * n + g] = u.correlation[a * U + bt.underlyings[g]];
+    }
+    rg_price_request q;
+    memset(&q, 0, sizeof q);
+    q.trade = t;
+    q.market = u;
+    q.market.n_assets = n;
+    q.market.spots = sub_spots;
+    q.market.vols = sub_vols;
+    q.market.dividend_yields = sub_q;
+    q.market.correlation = sub_rho;
+    q.config = c;
+    q.as_of = u.as_of;
+    validate_request(&q);
+  }
+  // the universe correlation itself (CorrelationMatrix::validate, correlation.rs:74-93)
+  for (int i = 0; i < U; ++i)
+    for (int k = 0; k < U; ++k) {
+      const double v = u.correlation[i * U + k];
+      if (!std::isfinite(v) || (i == k ? std::fabs(v - 1.0) > 1e-12
+                                       : (std::fabs(v) > 1.0 || std::fabs(v - u.correlation[k * U + i]) > 1e-12)))
+        raise(RG_ERR_INVALID_MARKET, "universe correlation must be symmetric with unit diagonal and entries in [-1,1]");
+    }
+  for (int a = 0; a < U; ++a)
+    if (!(u.spots[a] > 0.0) || !(u.vols[a] >= 0.0) || !std::isfinite(u.vols[a]) || !std::isfinite(u.dividend_yields[a]))
+      raise(RG_ERR_INVALID_MARKET, "universe spots must be positive and vols non-negative");
+  for (int s = 0; s < n_scen; ++s) {
+    if (!std::isfinite(sc[s].risk_free_rate)) raise(RG_ERR_INVALID_MARKET, "scenario rate must be finite");
+    for (int a = 0; a < U; ++a)
+      if (!(sc[s].spots[a] > 0.0) || !std::isfinite(sc[s].spots[a]) || !(sc[s].vols[a] >= 0.0) ||
+          !std::isfinite(sc[s].vols[a]) || !std::isfinite(sc[s].dividend_yields[a]))
+        raise(RG_ERR_INVALID_MARKET, "scenario spots must be positive and finite, vols non-negative");
+  }
+}
+
+void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B) {
+  const rg_market_snapshot& u = r->universe;
+  const rg_simulation_config& c = r->config;
+  B.U = u.n_assets;
+  B.TU = r->universe_steps;
+  B.dt = r->universe_maturity_years / (double)r->universe_steps;
+  B.n_trades = r->n_trades;
+  if (n_scen == 0) {
+    sc = &u;
+    n_scen = 1;
+  }
+  B.S = n_scen;
+  DevTrade& g = B.gen;
+  g.n = B.U;
+  g.vr = c.variance_reduction;
+  g.scrambler = c.scrambler;
+  g.steps = B.TU;
+  g.seed = c.seed;
+  g.dt = B.dt;
+  g.sqrt_dt = std::sqrt(B.dt);
+  g.inv_sqrt_dt = 1.0 / std::sqrt(B.dt);
+  g.x_lo = probit_threshold_lo();
+  g.x_hi = probit_threshold_hi();
+  const int64_t need = (int64_t)B.U * B.TU;
+  if (g.vr == RG_VR_SOBOL) {
+    int64_t d = (int64_t)c.qmc_dimension;
+    g.sob_dim = c.dim_mode == RG_DIM_FULL ? std::max<int64_t>(d, need) : std::min<int64_t>(std::max<int64_t>(d, 1), 512);
+  } else {
+    g.hal_dim = (int32_t)std::min<int64_t>(std::max<int64_t>((int64_t)c.qmc_dimension, 1), 512);
+  }
+  bridge_schedule_into(B.TU, B.dt, B.br);
+  B.trades.resize(B.n_trades);
+  for (int j = 0; j < B.n_trades; ++j) {
+    const rg_phoenix_trade& t = r->trades[j].terms;
+    BookTradeDev& d = B.trades[j];
+    memset(&d, 0, sizeof d);
+    d.n = t.n_assets;
+    d.T = (int32_t)t.steps;
+    int64_t per = t.has_coupon_periods ? t.coupon_periods : 9;  // note.rs:43
+    d.periods = (int32_t)std::max<int64_t>(std::min<int64_t>(per, INT32_MAX), 1);
+    const int64_t cs = t.has_call_start_step ? t.call_start_step : 0;
+    d.call_start = (int32_t)std::max<int64_t>(std::min<int64_t>(cs, INT32_MAX), INT32_MIN);
+    for (int f = 0; f < d.n; ++f) {
+      d.idx[f] = r->trades[j].underlyings[f];
+      d.init[f] = t.initial_spots[f];
+    }
+    d.fixed_first = t.fixed_first_coupon ? 1 : 0;
+    d.memory = t.memory_coupon ? 1 : 0;
+    d.maturity = t.maturity_years;
+    d.call_barrier = t.has_knock_out_barrier ? t.knock_out_barrier : INFINITY;
+    d.coupon_barrier = t.has_coupon_barrier ? t.coupon_barrier : INFINITY;
+    d.coupon_rate = t.has_coupon_rate ? t.coupon_rate : 0.0;
+    d.strike = t.strike;
+    d.ki = t.knock_in_barrier;
+    d.ln_ko = (float)std::log(d.call_barrier);
+    d.ln_cb = (float)std::log(d.coupon_barrier);
+    d.ln_ki = (float)std::log(d.ki);
+    d.coupon_f = (float)d.coupon_rate;
+  }
+  B.scen.resize(B.S);
+  B.df.resize((size_t)B.S * B.TU);
+  for (int s = 0; s < B.S; ++s) {
+    BookScenDev& d = B.scen[s];
+    memset(&d, 0, sizeof d);
+    d.rate = sc[s].risk_free_rate;
+    for (int a = 0; a < B.U; ++a) {
+      d.spots[a] = sc[s].spots[a];
+      d.vols[a] = sc[s].vols[a];
+      d.q[a] = sc[s].dividend_yields[a];
+    }
+    // exp(-r (t+1) dt) on the universe grid (note.rs:189, 210)
+    for (int64_t t = 0; t < B.TU; ++t) B.df[(size_t)s * B.TU + t] = rg_exp64(-d.rate * ((double)(t + 1) * B.dt));
+  }
+  B.dfm.resize((size_t)B.n_trades * B.S);
+  B.pair32.resize((size_t)B.n_trades * B.S);
+  for (int j = 0; j < B.n_trades; ++j)
+    for (int s = 0; s < B.S; ++s) {
+      const BookTradeDev& t = B.trades[j];
+      const BookScenDev& m = B.scen[s];
+      B.dfm[(size_t)j * B.S + s] = rg_exp64(-m.rate * t.maturity);  // note.rs:221, 238
+      BookPair32& p = B.pair32[(size_t)j * B.S + s];
+      memset(&p, 0, sizeof p);
+      for (int f = 0; f < t.n; ++f) {
+        const int a = t.idx[f];
+        const double v = m.vols[a];
+        p.x0[f] = (float)std::log(m.spots[a] / t.init[f]);
+        p.drift[f] = (float)((m.rate - m.q[a] - 0.5 * v * v) * B.dt);
+        p.sig[f] = (float)v;
+      }
+    }
+  // work order: longest trades first
+  B.order.resize(B.n_trades);
+  for (int j = 0; j < B.n_trades; ++j) B.order[j] = j;
+  std::stable_sort(B.order.begin(), B.order.end(),
+                   [&](int a, int b) { return B.trades[a].T * 8 + B.trades[a].n > B.trades[b].T * 8 + B.trades[b].n; });
+}
+
+struct BookStaged {
+  DevTables tb{};
+  BookDev bk{};
+  double* L = nullptr;
+  float* L32 = nullptr;
+};
+
+void* book_buf(rg_engine* E, int slot, size_t bytes) {
+  E->book_bufs[slot].ensure(bytes);
+  return E->book_bufs[slot].ptr;
+}
+
+BookStaged stage_book(rg_engine* E, const rg_book_request* r, BookPlan& B) {
+  Pack pk;
+  const int U = B.U;
+  size_t o_sobol = 0, o_hb = 0, o_ho = 0, o_hp = 0;
+  std::vector<uint32_t> hb, ho, hp;
+  if (B.gen.vr == RG_VR_SOBOL) {
+    o_sobol = pk.add(sobol_table(B.gen.sob_dim));
+  } else {
+    halton_tables(B.gen.hal_dim, B.gen.seed, hb, ho, hp);
+    o_hb = pk.add(hb);
+    o_ho = pk.add(ho);
+    o_hp = pk.add(hp);
+  }
+  const size_t o_noff = pk.add(B.br.node_off), o_nk = pk.add(B.br.node_k), o_nc = pk.add(B.br.node_c),
+               o_ncf = pk.add(B.br.node_cf);
+  const size_t o_tr = pk.add(B.trades), o_sc = pk.add(B.scen), o_p32 = pk.add(B.pair32), o_df = pk.add(B.df),
+               o_dfm = pk.add(B.dfm), o_ord = pk.add(B.order);
+  const size_t o_corr = pk.add(r->universe.correlation, (size_t)U * U);
+  const size_t o_L = pk.reserve(sizeof(double) * U * U), o_L32 = pk.reserve(sizeof(float) * U * U);
+  const size_t o_work = pk.reserve(sizeof(double) * 2 * U * U);
+  uint8_t* dev = static_cast<uint8_t*>(book_buf(E, BK_TABLES, pk.host.size()));
+  cuda_check(cudaMemcpyAsync(dev, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, E->stream), "book H2D");
+  BookStaged st;
+  DevTables& tb = st.tb;
+  tb.sobol = B.gen.vr == RG_VR_SOBOL ? reinterpret_cast<const uint32_t*>(dev + o_sobol) : nullptr;
+  tb.hal_base = B.gen.vr == RG_VR_HALTON ? reinterpret_cast<const uint32_t*>(dev + o_hb) : nullptr;
+  tb.hal_off = B.gen.vr == RG_VR_HALTON ? reinterpret_cast<const uint32_t*>(dev + o_ho) : nullptr;
+  tb.hal_perm = B.gen.vr == RG_VR_HALTON ? reinterpret_cast<const uint32_t*>(dev + o_hp) : nullptr;
+  tb.node_off = reinterpret_cast<const int32_t*>(dev + o_noff);
+  tb.node_k = reinterpret_cast<const int32_t*>(dev + o_nk);
+  tb.node_c = reinterpret_cast<const double*>(dev + o_nc);
+  tb.node_cf = reinterpret_cast<const float*>(dev + o_ncf);
+  BookDev& bk = st.bk;
+  bk.U = U;
+  bk.S = B.S;
+  bk.n_trades = B.n_trades;
+  bk.TU = B.TU;
+  bk.trades = reinterpret_cast<const BookTradeDev*>(dev + o_tr);
+  bk.scen = reinterpret_cast<const BookScenDev*>(dev + o_sc);
+  bk.pair32 = reinterpret_cast<const BookPair32*>(dev + o_p32);
+  bk.df = reinterpret_cast<const double*>(dev + o_df);
+  bk.dfm = reinterpret_cast<const double*>(dev + o_dfm);
+  bk.order = reinterpret_cast<const int32_t*>(dev + o_ord);
+  st.L = reinterpret_cast<double*>(dev + o_L);
+  st.L32 = reinterpret_cast<float*>(dev + o_L32);
+  bk.L = st.L;
+  bk.L32 = st.L32;
+  launch_cholesky_big(reinterpret_cast<const double*>(dev + o_corr), U, st.L,
+                      reinterpret_cast<double*>(dev + o_work), E->stream);
+  launch_book_l32(st.L, U, st.L32, E->stream);
+  return st;
+}
+
+// Paths per generation chunk: a multiple of `unit` whose increments fit the budget.
+uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t unit) {
+  const uint64_t per_path = (uint64_t)U * (uint64_t)TU * elem;
+  uint64_t cap = kIncrBudget / per_path;
+  cap = cap / unit * unit;
+  if (cap < unit) cap = unit;
+  return paths < cap ? paths : cap;
+}
+
+// Prices (records == nullptr) or replays [first, first + count) of the book.
+void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* sc, int n_scen,
+              rg_price_result* out, uint64_t first, uint64_t count, rg_path_record* records) {
+  validate_book(r, sc, n_scen);
+  BookPlan B;
+  plan_book(r, sc, n_scen, B);
+  const int pairs = B.n_trades * B.S;
+  const bool fp32 = r->config.precision == RG_PRECISION_FP32 && !records;
+  BookStaged st = stage_book(E, r, B);
+  const uint64_t path_base = r->config.first_path + first;
+  const uint64_t P = records ? count : r->config.paths;
+  cudaStream_t s0 = E->stream, s1 = E->gen_stream;
+  if (fp32) {
+    const Book32Shape sh = book32_shape(B.S, device_sm_count());
+    const uint64_t PC = chunk_paths(P, B.U, B.TU, sizeof(float), (uint64_t)sh.blk_paths);
+    const uint64_t n_chunks = (P + PC - 1) / PC;
+    const uint64_t blocks_per_chunk = (PC + sh.blk_paths - 1) / sh.blk_paths;
+    const uint64_t total_blocks = (P + sh.blk_paths - 1) / sh.blk_paths;
+    const size_t incr_bytes = sizeof(float) * (size_t)B.U * (size_t)B.TU * (size_t)PC;
+    float* incr[2] = {static_cast<float*>(book_buf(E, BK_INCR0, incr_bytes)),
+                      static_cast<float*>(book_buf(E, BK_INCR1, n_chunks > 1 ? incr_bytes : 256))};
+    double* partial = static_cast<double*>(book_buf(E, BK_PARTIAL, sizeof(double) * total_blocks * pairs * RG_ACC));
+    int32_t* scratch = static_cast<int32_t*>(book_buf(E, BK_SCRATCH, 256));
+    int* status = scratch + 1;
+    cuda_check(cudaMemsetAsync(scratch, 0, 256, s0), "book status reset");
+    // the generation stream waits for the tables and the Cholesky factor
+    cuda_check(cudaEventRecord(E->book_ev[0], s0), "event");
+    cuda_check(cudaStreamWaitEvent(s1, E->book_ev[0], 0), "stream wait");
+    for (uint64_t c = 0; c < n_chunks; ++c) {
+      const uint64_t p0 = c * PC, np = std::min<uint64_t>(PC, P - p0);
+      float* buf = incr[c & 1];
+      if (c >= 2) {
+        // buffer reuse: the scan of chunk c-2 must be done with it
+        cuda_check(cudaStreamWaitEvent(s1, E->book_ev[2 + (c & 1)], 0), "stream wait");
+      }
+      launch_book_gen32(B.gen, st.tb, st.L32, B.U, path_base + p0, np, buf, s1);
+      cuda_check(cudaEventRecord(E->book_ev[1], s1), "event");
+      cuda_check(cudaStreamWaitEvent(s0, E->book_ev[1], 0), "stream wait");
+      launch_book_trade32(st.bk, sh, buf, np, c * blocks_per_chunk, partial, scratch, status, s0);
+      cuda_check(cudaEventRecord(E->book_ev[2 + (c & 1)], s0), "event");
+    }
+    double* dsums = static_cast<double*>(book_buf(E, BK_SUMS, sizeof(double) * pairs * RG_ACC));
+    launch_book_reduce_strided(partial, (int64_t)total_blocks, (int64_t)pairs * RG_ACC, RG_ACC, pairs, dsums, s0);
+    std::vector<double> hs((size_t)pairs * RG_ACC);
+    int hstat = 0;
+    cuda_check(cudaMemcpyAsync(hs.data(), dsums, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, s0), "D2H");
+    cuda_check(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, s0), "D2H");
+    cuda_check(cudaStreamSynchronize(s0), "book pricing");
+    if (hstat) raise(RG_ERR_GPU_ERROR, "book_trade32_kernel reported a bad work item");
+    for (size_t k = 0; k < hs.size(); ++k)
+      if (!std::isfinite(hs[k])) raise(RG_ERR_GPU_ERROR, "book: non-finite path sums");
+    for (int p = 0; p < pairs; ++p) finish(hs.data() + (size_t)p * RG_ACC, P, r->config.seed, &out[p]);
+    return;
+  }
+  // FP64 parity: generation then scan per chunk on the engine stream
+  const uint64_t PC = chunk_paths(P, B.U, B.TU, sizeof(double), 128);
+  const uint64_t n_chunks = (P + PC - 1) / PC;
+  const int blocks_per_chunk = (int)((PC + 127) / 128);
+  const uint64_t total_blocks = n_chunks * (uint64_t)blocks_per_chunk;
+  double* incr = static_cast<double*>(book_buf(E, BK_INCR0, sizeof(double) * (size_t)B.U * (size_t)B.TU * (size_t)PC));
+  double* partial = static_cast<double*>(book_buf(E, BK_PARTIAL, sizeof(double) * total_blocks * pairs * RG_ACC));
+  rg_path_record* drec = records ? static_cast<rg_path_record*>(book_buf(E, BK_RECORDS, sizeof(rg_path_record) * (size_t)PC * pairs)) : nullptr;
+  std::vector<double> hs((size_t)pairs * RG_ACC, 0.0);
+  for (uint64_t c = 0; c < n_chunks; ++c) {
+    const uint64_t p0 = c * PC, np = std::min<uint64_t>(PC, P - p0);
+    launch_book_gen64(B.gen, st.tb, st.L, B.U, path_base + p0, np, incr, s0);
+    const int blocks = (int)((np + 127) / 128);
+    launch_book_trade64(B.gen, st.bk, incr, path_base + p0, np, partial, blocks, drec, s0);
+    if (records) {
+      cuda_check(cudaMemcpyAsync(records + (size_t)p0 * pairs, drec, sizeof(rg_path_record) * (size_t)np * pairs,
+                                 cudaMemcpyDeviceToHost, s0), "D2H records");
+      cuda_check(cudaStreamSynchronize(s0), "book replay");
+      continue;
+    }
+    // sum this chunk's blocks into the running FP64 totals, pair by pair, in block order
+    double* dsums = static_cast<double*>(book_buf(E, BK_SUMS, sizeof(double) * pairs * RG_ACC));
+    launch_book_reduce_strided(partial, blocks, RG_ACC, (int64_t)blocks * RG_ACC, pairs, dsums, s0);
+    std::vector<double> part((size_t)pairs * RG_ACC);
+    cuda_check(cudaMemcpyAsync(part.data(), dsums, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s0), "D2H");
+    cuda_check(cudaStreamSynchronize(s0), "book pricing");
+    for (size_t k = 0; k < part.size(); ++k) hs[k] += part[k];
+  }
+  if (records) return;
+  for (int p = 0; p < pairs; ++p) finish(hs.data() + (size_t)p * RG_ACC, P, r->config.seed, &out[p]);
+}
+
+}  // namespace
+
+}  // namespace rg
+
+using namespace rg;
+
+extern "C" int32_t rg_price_book(rg_engine* e, const rg_book_request* request, const rg_market_snapshot* scenarios,
+                                 int32_t n_scenarios, rg_price_result* out) {
+  RG_TRY({
+    if (!e || !request || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    int32_t g = rg_guard_device();
+    if (g) return g;
+    std::lock_guard<std::mutex> lock(e->mu);
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    run_book(e, request, scenarios, n_scenarios, out, 0, 0, nullptr);
+  })
+}
+
+extern "C" int32_t rg_book_run_paths(rg_engine* e, const rg_book_request* request, const rg_market_snapshot* scenarios,
+                                     int32_t n_scenarios, uint64_t first_path, uint64_t count, rg_path_record* out) {
+  RG_TRY({
+    if (!e || !request || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    int32_t g = rg_guard_device();
+    if (g) return g;
+    if (count == 0) raise(RG_ERR_INVALID_ARGUMENT, "count must be positive");
+    if (first_path > request->config.paths || count > request->config.paths - first_path)
+      raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
+    std::lock_guard<std::mutex> lock(e->mu);
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    run_book(e, request, scenarios, n_scenarios, nullptr, first_path, count, out);
+  })
+}

@@ -106,17 +106,6 @@ int32_t rg_guard_device() {
   return d.status;
 }
 
-#define RG_TRY(...)                              \
-  try {                                           \
-    __VA_ARGS__;                                  \
-    return RG_OK;                                 \
-  } catch (const rg::Error& e) {                  \
-    rg::set_last_error(e.message);                \
-    return e.status;                              \
-  } catch (const std::bad_alloc&) {               \
-    rg::set_last_error("host allocation failed"); \
-    return RG_ERR_GPU_ERROR;                      \
-  }
 
 static const char* const kCodes[] = {
     "ok", "missing_as_of", "as_of_mismatch", "invalid_paths", "invalid_schedule",
@@ -166,16 +155,6 @@ extern "C" int32_t rg_arch(char* buf, size_t len) {
 }
 
 // ------------------------------------------------------------------ engine --------------------
-struct rg_engine {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::mutex mu;
-  DevBuf bufs[WS_NSLOTS];
-  HostBuf host_sums;
-  std::vector<uint8_t> host_pack;
-  cudaEvent_t ev[6] = {};
-  rg_timing timing{};
-};
 
 extern "C" int32_t rg_engine_create(int32_t device, rg_engine** out) {
   RG_TRY({
@@ -189,7 +168,10 @@ extern "C" int32_t rg_engine_create(int32_t device, rg_engine** out) {
     std::unique_ptr<rg_engine> e(new rg_engine());
     e->device = device;
     cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&e->gen_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     for (cudaEvent_t& ev : e->ev) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
+    for (cudaEvent_t& ev : e->book_ev)
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
     *out = e.release();
   })
 }
@@ -200,7 +182,13 @@ extern "C" void rg_engine_destroy(rg_engine* e) {
     cudaStreamSynchronize(e->stream);
     cudaStreamDestroy(e->stream);
   }
+  if (e->gen_stream) {
+    cudaStreamSynchronize(e->gen_stream);
+    cudaStreamDestroy(e->gen_stream);
+  }
   for (cudaEvent_t ev : e->ev)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : e->book_ev)
     if (ev) cudaEventDestroy(ev);
   delete e;
 }
@@ -345,7 +333,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
 }
 
 // PriceResult from the FP64 sums (note.rs:262-372); counts are exact in FP64.
-static void finish(const double* a, uint64_t paths, uint64_t seed, rg_price_result* out) {
+void finish(const double* a, uint64_t paths, uint64_t seed, rg_price_result* out) {
   memset(out, 0, sizeof *out);
   const double P = (double)paths;
   auto var = [](double s1, double s2, double n) {

@@ -267,7 +267,7 @@ void bridge_schedule_into(int64_t T, double dt, Prepared& P) {
   P.node_cf.assign(P.node_c.begin(), P.node_c.end());
 }
 
-static uint32_t probit_threshold_lo() {
+uint32_t probit_threshold_lo() {
   // smallest x with (x + 0.5) / 2^32 >= 0.02425 (the central branch of qmc.rs:81)
   const double plow = 0.02425;
   uint64_t x = (uint64_t)std::floor(plow * 4294967296.0);
@@ -276,7 +276,7 @@ static uint32_t probit_threshold_lo() {
   return (uint32_t)x;
 }
 
-static uint32_t probit_threshold_hi() {
+uint32_t probit_threshold_hi() {
   // largest x with (x + 0.5) / 2^32 <= 1 - 0.02425
   const double phigh = 1.0 - 0.02425;
   uint64_t x = (uint64_t)std::floor(phigh * 4294967296.0);

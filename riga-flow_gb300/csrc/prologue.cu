@@ -6,7 +6,7 @@
 //   the (v, dv) FP32 pairs the production kernel interpolates.
 // * cholesky_kernel: one thread per scenario.  Jacobi minimum eigenvalue, diagonal-loading PSD
 //   clamp and Cholesky–Banachiewicz (crates/riga-market/src/correlation.rs:95-168), in place on
-//   the scenario's correlation block.
+//   the scenario's correlation block; cholesky_big_kernel: the same for a book's universe.
 // Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's; exp and log are
 // the deterministic rg_exp64/rg_log64, so the grid is bit-identical to a host calibration.
 #include "rg_internal.h"
@@ -180,11 +180,11 @@ void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ correlation ---------------
-__device__ static double min_eigenvalue(const double* c, int n) {
-  double a[RG_NMAX * RG_NMAX];
-  for (int i = 0; i < n * n; ++i) a[i] = c[i];
+// Smallest eigenvalue by cyclic Jacobi (correlation.rs:217-260); `a` holds the n×n matrix and is
+// overwritten.
+__device__ static double min_eigenvalue_inplace(double* a, int n) {
   if (n == 1) return a[0];
-  for (int it = 0; it < 100; ++it) {  // cyclic Jacobi, correlation.rs:217-260
+  for (int it = 0; it < 100; ++it) {
     int p = 0, q = 0;
     double mx = 0.0;
     for (int i = 0; i < n; ++i)
@@ -213,21 +213,18 @@ __device__ static double min_eigenvalue(const double* c, int n) {
   return m;
 }
 
-__global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_scen) return;
-  DevScenario& sc = scen[i];
-  double src[RG_NMAX * RG_NMAX], l[RG_NMAX * RG_NMAX];
-  for (int k = 0; k < n * n; ++k) src[k] = sc.L[k];
-  // use the matrix as is when min eig >= 1e-10, else PSD-clamp with floor 1e-8
-  // (is_positive_semidefinite(-1e-10) and psd_clamp(1e-8), correlation.rs:103-136, 144-148)
-  double mn = min_eigenvalue(src, n);
+// L·Lᵀ = C: the matrix as is when its min eigenvalue is >= 1e-10, else PSD-clamped with floor
+// 1e-8 (is_positive_semidefinite(-1e-10) and psd_clamp(1e-8), correlation.rs:103-136, 144-148),
+// then Cholesky–Banachiewicz (:150-168).  `src` (n×n) is modified, `eig` is n×n scratch.
+__device__ static void factor_correlation(double* src, int n, double* l, double* eig) {
+  for (int k = 0; k < n * n; ++k) eig[k] = src[k];
+  double mn = min_eigenvalue_inplace(eig, n);
   if (!(mn >= 1.0e-10)) {
-    double shift = 1.0e-8 - mn, inv[RG_NMAX];
+    double shift = 1.0e-8 - mn;
     for (int k = 0; k < n; ++k) src[k * n + k] += shift;
-    for (int k = 0; k < n; ++k) inv[k] = 1.0 / sqrt(src[k * n + k]);
+    for (int k = 0; k < n; ++k) eig[k] = 1.0 / sqrt(src[k * n + k]);
     for (int a = 0; a < n; ++a)
-      for (int b = 0; b < n; ++b) src[a * n + b] *= inv[a] * inv[b];
+      for (int b = 0; b < n; ++b) src[a * n + b] *= eig[a] * eig[b];
   }
   for (int k = 0; k < n * n; ++k) l[k] = 0.0;
   for (int a = 0; a < n; ++a)
@@ -241,8 +238,33 @@ __global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int 
         l[a * n + b] = pivot > 0.0 ? sum / pivot : 0.0;
       }
     }
+}
+
+// One thread per scenario, in place on the scenario's correlation block.
+__global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_scen) return;
+  DevScenario& sc = scen[i];
+  double src[RG_NMAX * RG_NMAX], l[RG_NMAX * RG_NMAX], eig[RG_NMAX * RG_NMAX];
+  for (int k = 0; k < n * n; ++k) src[k] = sc.L[k];
+  factor_correlation(src, n, l, eig);
   for (int k = 0; k < n * n; ++k) sc.L[k] = l[k];
   sc.status = 0;
+}
+
+// One thread for a universe correlation (n <= RG_BOOK_MAX_UNIVERSE); scratch in `work`.
+__global__ void cholesky_big_kernel(const double* __restrict__ c, int n, double* __restrict__ l,
+                                    double* __restrict__ work) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double* src = work;
+  double* eig = work + n * n;
+  for (int k = 0; k < n * n; ++k) src[k] = c[k];
+  factor_correlation(src, n, l, eig);
+}
+
+void launch_cholesky_big(const double* c, int n, double* l, double* work, cudaStream_t s) {
+  cholesky_big_kernel<<<1, 32, 0, s>>>(c, n, l, work);
+  cuda_check(cudaGetLastError(), "cholesky_big_kernel launch");
 }
 
 void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s) {

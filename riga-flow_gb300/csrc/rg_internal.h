@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -21,6 +22,8 @@ struct Error {
 };
 
 [[noreturn]] void raise(int32_t status, const std::string& message);
+// PriceResult from the FP64 path sums of one scenario (note.rs:262-372).
+void finish(const double* sums, uint64_t paths, uint64_t seed, rg_price_result* out);
 void set_last_error(const std::string& message);
 void cuda_check(cudaError_t e, const char* what);
 
@@ -182,4 +185,101 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
                       const Fp32Shape& shape, const LaunchOut& out, cudaStream_t s);
 void launch_reduce(const double* partial, int grid, int n_scen, double* out, cudaStream_t s);
 
+// The 32-bit Sobol integers at which the inverse normal switches between its central and tail
+// branches (computed in FP64 so the FP32 kernels branch exactly as the reference does).
+uint32_t probit_threshold_lo();
+uint32_t probit_threshold_hi();
+// Cholesky factor (with the reference's PSD clamp) of one n×n correlation, n <= RG_BOOK_MAX_UNIVERSE,
+// by one device thread; `work` holds 2·n·n doubles.
+void launch_cholesky_big(const double* c, int n, double* l, double* work, cudaStream_t s);
+
+// ------------------------------------------------------------------ books ---------------------
+// One book trade's constants on the device.
+struct BookTradeDev {
+  int32_t n, T, periods, call_start;
+  int32_t idx[RG_NMAX];   // universe asset of each underlying
+  int32_t fixed_first, memory;
+  double init[RG_NMAX];
+  double maturity, call_barrier, coupon_barrier, coupon_rate, strike, ki;
+  float ln_ko, ln_cb, ln_ki, coupon_f;
+};
+// One scenario of a book: a market of the universe.
+struct BookScenDev {
+  double rate;
+  double spots[RG_BOOK_MAX_UNIVERSE], vols[RG_BOOK_MAX_UNIVERSE], q[RG_BOOK_MAX_UNIVERSE];
+};
+// FP32 constants of one (trade, scenario) pair: ln(S/S0), the log drift per step and the vol.
+struct BookPair32 {
+  float x0[RG_NMAX], drift[RG_NMAX], sig[RG_NMAX];
+};
+// Device pointers of a staged book.
+struct BookDev {
+  int32_t U, S, n_trades;
+  int64_t TU;
+  const BookTradeDev* trades;  // [n_trades]
+  const BookScenDev* scen;     // [S]
+  const BookPair32* pair32;    // [n_trades][S]
+  const double* df;            // [S][TU]  exp(-r_s (t+1) dt)
+  const double* dfm;           // [n_trades][S] exp(-r_s maturity_j)
+  const double* L;             // [U][U] universe Cholesky factor (FP64)
+  const float* L32;            // [U][U] the same in FP32
+  const int32_t* order;        // [n_trades] trade order of the work items (longest first)
+};
+// Universe increments of paths [path0, path0 + npaths): incr[t][u][p], FP64 ΔW/√dt (parity) or
+// FP32 ΔW (production); one thread per (path, universe asset).
+void launch_book_gen64(const DevTrade& gen, const DevTables& tb, const double* L, int U,
+                       uint64_t path0, uint64_t npaths, double* incr, cudaStream_t s);
+void launch_book_gen32(const DevTrade& gen, const DevTables& tb, const float* L32, int U,
+                       uint64_t path0, uint64_t npaths, float* incr, cudaStream_t s);
+// FP64 scan of every (trade, scenario) on the chunk's increments: one thread per (pair, path);
+// partial[pair][block][RG_ACC] over `blocks` blocks of 128 paths; records[p][pair] when given.
+// partial[pair][block][RG_ACC] with `blocks` blocks of 128 paths per pair.
+void launch_book_trade64(const DevTrade& gen, const BookDev& bk, const double* incr, uint64_t path0,
+                         uint64_t npaths, double* partial, int blocks, rg_path_record* records,
+                         cudaStream_t s);
+// FP32 persistent scan: work items (path block, trade) with block-major order; every item's
+// FP64 sums land in partial[(block0 + b) * n_trades + j][S][RG_ACC].
+struct Book32Shape {
+  int threads, Sb, Pb, grid, blk_paths;
+};
+Book32Shape book32_shape(int S, int sm_count);
+void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const float* incr, uint64_t npaths,
+                         uint64_t block0, double* partial, int32_t* counter, int* status,
+                         cudaStream_t s);
+// The FP32 copy of the universe Cholesky factor.
+void launch_book_l32(const double* L, int U, float* L32, cudaStream_t s);
+// Fixed-order sums over path blocks: out[pair][k] = Σ_b partial[b·stride_b + pair·stride_pair + k].
+void launch_book_reduce_strided(const double* partial, int64_t blocks, int64_t stride_b, int64_t stride_pair,
+                                int pairs, double* out, cudaStream_t s);
+
 }  // namespace rg
+
+// Body of every C entry point: rg::Error and allocation failures become status codes.
+#define RG_TRY(...)                              \
+  try {                                           \
+    __VA_ARGS__;                                  \
+    return RG_OK;                                 \
+  } catch (const rg::Error& e) {                  \
+    rg::set_last_error(e.message);                \
+    return e.status;                              \
+  } catch (const std::bad_alloc&) {               \
+    rg::set_last_error("host allocation failed"); \
+    return RG_ERR_GPU_ERROR;                      \
+  }
+
+int32_t rg_guard_device();
+
+// The engine behind the opaque C handle.
+struct rg_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t gen_stream = nullptr;  // book path generation, overlapped with the scan
+  std::mutex mu;
+  rg::DevBuf bufs[rg::WS_NSLOTS];
+  rg::DevBuf book_bufs[8];
+  rg::HostBuf host_sums;
+  std::vector<uint8_t> host_pack;
+  cudaEvent_t ev[6] = {};
+  cudaEvent_t book_ev[4] = {};
+  rg_timing timing{};
+};

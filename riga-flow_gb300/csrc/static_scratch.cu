@@ -24,8 +24,6 @@
 
 static __device__ __align__(256) unsigned char g_static_scratch[RG_STATIC_SCRATCH_BYTES];
 
-int32_t rg_guard_device();
-
 namespace {
 
 std::mutex g_static_mu;

@@ -267,6 +267,16 @@ class PathRecord(C.Structure):
     ]
 
 
+class BookTrade(C.Structure):
+    _fields_ = [("terms", Trade), ("underlyings", C.POINTER(C.c_int32))]
+
+
+class BookRequest(C.Structure):
+    _fields_ = [("universe", Market), ("universe_steps", C.c_int64),
+                ("universe_maturity_years", C.c_double), ("n_trades", C.c_int32),
+                ("trades", C.POINTER(BookTrade)), ("config", SimConfig)]
+
+
 class RigaError(Exception):
     """Mirror of ``RigaError { code, message }`` (crates/riga-core/src/lib.rs:5-19)."""
 
@@ -298,6 +308,10 @@ SIGNATURES = {
     "rg_run_paths": (_i32, [_vp, C.POINTER(PriceRequest), _u64, _u64, C.POINTER(PathRecord)]),
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
+    "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
+                             C.POINTER(PriceResult)]),
+    "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,
+                                 C.POINTER(PathRecord)]),
     "rg_sobol_directions": (_i32, [_i64, C.POINTER(C.c_uint32)]),
     "rg_bridge_schedule": (_i32, [_i64, C.c_double, C.POINTER(_i32), C.POINTER(_i32),
                                   C.POINTER(C.c_double), C.POINTER(_i32)]),

@@ -5,6 +5,8 @@
 * ``price_risk_batch`` — ``riga_risk::price_risk_batch`` (crates/riga-risk/src/lib.rs:573-626)
 * ``run_paths`` / ``reconstruct_path`` / ``query_worst_percentile`` —
   crates/riga-engine/src/explain.rs:90-372
+* ``price_book_raw`` / ``book_run_paths_raw`` — many trades on one universe under one common CRN
+  scenario set (``rg_price_book``; the reference prices one trade per request)
 """
 from __future__ import annotations
 
@@ -15,7 +17,8 @@ from typing import Optional
 
 from . import abi
 from .abi import RigaError, check, load_library
-from .types import PriceRequest, market_to_abi, record_to_dict, result_to_json
+from .types import (BookRequest, PriceRequest, market_to_abi, markets_to_abi, record_to_dict,
+                    result_to_json)
 
 
 class Engine:
@@ -47,6 +50,28 @@ class Engine:
 
     def price_put_leg(self, request: PriceRequest) -> dict:
         return result_to_json(self.price_raw(request), request)
+
+    # -------------------------------------------------------------- books -----------------
+    def price_book_raw(self, book: BookRequest, scenarios=None) -> list:
+        """Results of every (trade, scenario), trade-major: ``out[j * S + s]``.  ``scenarios`` is
+        a list of universe ``MarketSnapshot``s (None: the base market alone)."""
+        a = book.to_abi()
+        keep = []
+        arr, n = markets_to_abi(scenarios, keep.append)
+        S = max(1, n)
+        out = (abi.PriceResult * (len(book.trades) * S))()
+        check(self.lib, self.lib.rg_price_book(self.handle, a.ptr, arr, n, out))
+        return list(out)
+
+    def book_run_paths_raw(self, book: BookRequest, scenarios, first: int, count: int) -> list:
+        """Per-path records ``out[(p * n_trades + j) * S + s]`` of paths [first, first + count)."""
+        a = book.to_abi()
+        keep = []
+        arr, n = markets_to_abi(scenarios, keep.append)
+        S = max(1, n)
+        out = (abi.PathRecord * (count * len(book.trades) * S))()
+        check(self.lib, self.lib.rg_book_run_paths(self.handle, a.ptr, arr, n, first, count, out))
+        return list(out)
 
     def price_scenarios_raw(self, request: PriceRequest, scenarios) -> list:
         """``scenarios``: list of (MarketSnapshot, implied-vol shift list or None)."""

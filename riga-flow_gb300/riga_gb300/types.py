@@ -233,34 +233,10 @@ class AbiRequest:
             self._keep.append(x)
             return x
 
-        tr = abi.Trade()
-        tr.trade_id = keep(t.trade_id.encode())
-        tr.n_assets = len(t.initial_spots)
-        tr.initial_spots = C.cast(keep(_darr(t.initial_spots)), C.POINTER(C.c_double))
-        tr.maturity_years = t.maturity_years
-        tr.steps = t.steps
-        tr.strike = t.strike
-        tr.knock_in_barrier = t.knock_in_barrier
-        for name in ("knock_out_barrier", "coupon_barrier", "coupon_rate"):
-            v = getattr(t, name)
-            setattr(tr, "has_" + name, 0 if v is None else 1)
-            setattr(tr, name, 0.0 if v is None else float(v))
-        tr.memory_coupon = int(bool(t.memory_coupon))
-        tr.has_coupon_periods = 0 if t.coupon_periods is None else 1
-        tr.coupon_periods = 0 if t.coupon_periods is None else int(t.coupon_periods)
-        tr.fixed_first_coupon = int(bool(t.fixed_first_coupon))
-        tr.has_call_start_step = 0 if t.call_start_step is None else 1
-        tr.call_start_step = 0 if t.call_start_step is None else int(t.call_start_step)
+        tr = trade_to_abi(t, keep)
 
         self.market = market_to_abi(m, keep)
-        cfg = abi.SimConfig()
-        cfg.paths, cfg.path_block_size, cfg.seed = c.paths, c.path_block_size, c.seed
-        cfg.trace_level = TRACE_LEVELS.index(c.trace_level)
-        cfg.variance_reduction = c.variance_reduction.code
-        cfg.qmc_dimension = c.variance_reduction.dimension
-        cfg.scrambler, cfg.precision, cfg.dim_mode, cfg.lv_grid_x = (
-            o.scrambler, o.precision, o.dim_mode, o.lv_grid_x)
-        cfg.first_path = o.first_path
+        cfg = config_to_abi(c, o)
 
         r = abi.PriceRequest()
         r.trade = tr
@@ -284,6 +260,113 @@ class AbiRequest:
             r.local_vol = None
         self.req = r
         self.ptr = C.pointer(r)
+
+
+def trade_to_abi(t: PhoenixTrade, keep) -> abi.Trade:
+    tr = abi.Trade()
+    tr.trade_id = keep(t.trade_id.encode())
+    tr.n_assets = len(t.initial_spots)
+    tr.initial_spots = C.cast(keep(_darr(t.initial_spots)), C.POINTER(C.c_double))
+    tr.maturity_years = t.maturity_years
+    tr.steps = t.steps
+    tr.strike = t.strike
+    tr.knock_in_barrier = t.knock_in_barrier
+    for name in ("knock_out_barrier", "coupon_barrier", "coupon_rate"):
+        v = getattr(t, name)
+        setattr(tr, "has_" + name, 0 if v is None else 1)
+        setattr(tr, name, 0.0 if v is None else float(v))
+    tr.memory_coupon = int(bool(t.memory_coupon))
+    tr.has_coupon_periods = 0 if t.coupon_periods is None else 1
+    tr.coupon_periods = 0 if t.coupon_periods is None else int(t.coupon_periods)
+    tr.fixed_first_coupon = int(bool(t.fixed_first_coupon))
+    tr.has_call_start_step = 0 if t.call_start_step is None else 1
+    tr.call_start_step = 0 if t.call_start_step is None else int(t.call_start_step)
+    return tr
+
+
+def config_to_abi(c: SimulationConfig, o: EngineOptions) -> abi.SimConfig:
+    cfg = abi.SimConfig()
+    cfg.paths, cfg.path_block_size, cfg.seed = c.paths, c.path_block_size, c.seed
+    cfg.trace_level = TRACE_LEVELS.index(c.trace_level)
+    cfg.variance_reduction = c.variance_reduction.code
+    cfg.qmc_dimension = c.variance_reduction.dimension
+    cfg.scrambler, cfg.precision, cfg.dim_mode, cfg.lv_grid_x = (
+        o.scrambler, o.precision, o.dim_mode, o.lv_grid_x)
+    cfg.first_path = o.first_path
+    return cfg
+
+
+# ---------------------------------------------------------------------- books ----------------
+@dataclass
+class BookTrade:
+    """One trade of a book: Phoenix terms on `underlyings` (indices into the book's universe)."""
+
+    terms: PhoenixTrade
+    underlyings: list
+
+
+@dataclass
+class BookRequest:
+    """Many trades on one asset universe over one common grid (``rg_book_request``)."""
+
+    universe: MarketSnapshot
+    universe_steps: int
+    universe_maturity_years: float
+    trades: list  # list[BookTrade]
+    config: SimulationConfig
+    options: EngineOptions = field(default_factory=EngineOptions)
+
+    @property
+    def dt(self) -> float:
+        return self.universe_maturity_years / self.universe_steps
+
+    def to_abi(self) -> "AbiBookRequest":
+        return AbiBookRequest(self)
+
+
+class AbiBookRequest:
+    """Owns the ctypes buffers behind one ``rg_book_request``."""
+
+    def __init__(self, book: BookRequest):
+        self._keep = []
+
+        def keep(x):
+            self._keep.append(x)
+            return x
+
+        arr = (abi.BookTrade * len(book.trades))()
+        for i, bt in enumerate(book.trades):
+            arr[i].terms = trade_to_abi(bt.terms, keep)
+            idx = (C.c_int32 * max(1, len(bt.underlyings)))(*[int(a) for a in bt.underlyings])
+            arr[i].underlyings = C.cast(keep(idx), C.POINTER(C.c_int32))
+        keep(arr)
+        r = abi.BookRequest()
+        r.universe = market_to_abi(book.universe, keep)
+        r.universe_steps = int(book.universe_steps)
+        r.universe_maturity_years = float(book.universe_maturity_years)
+        r.n_trades = len(book.trades)
+        r.trades = C.cast(arr, C.POINTER(abi.BookTrade))
+        cfg = config_to_abi(book.config, book.options)
+        r.config = cfg
+        self.req = r
+        self.ptr = C.pointer(r)
+
+
+def markets_to_abi(markets, keep):
+    """A C array of ``rg_market_snapshot`` (or (None, 0) for an empty list); `keep` is called with
+    every ctypes buffer the array points into, so the caller can hold them alive."""
+    if not markets:
+        return None, 0
+
+    def hold(x):
+        keep(x)
+        return x
+
+    arr = (abi.Market * len(markets))()
+    for i, m in enumerate(markets):
+        arr[i] = market_to_abi(m, hold)
+    hold(arr)
+    return arr, len(markets)
 
 
 def market_to_abi(m: MarketSnapshot, keep) -> abi.Market:

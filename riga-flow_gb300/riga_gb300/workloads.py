@@ -139,3 +139,105 @@ def crn15_scenarios(req: PriceRequest):
         m.vols = [v - (0.01 if i == f else 0.0) for i, v in enumerate(m.vols)]
         out.append((f"vol[{f}]-", m, [-0.01 if i == f else 0.0 for i in range(n)]))
     return out
+
+
+# ---------------------------------------------------------------------- books ----------------
+# The book configuration: a 20-asset universe with a 4-factor correlation C = B·Bᵀ + diag(1 -
+# Σ_k B_ik²), loadings B_ik ∈ U[0.2, 0.7] with every row rescaled so that Σ_k B_ik² <= 0.95 (an
+# unscaled row could exceed 1, which is not a correlation), vols U[0.15, 0.45], spots 100,
+# r = 0.03, q = 0.01, on a 5-year grid of 1260 daily steps.  Trades draw 1..5 distinct
+# underlyings, a maturity of 1..5 years (252 steps a year, truncating the universe grid), a
+# daily KO barrier U[0.95, 1.10] from step 63, a coupon barrier U[0.60, 0.80], an EKI barrier
+# U[0.50, 0.70], and a quarterly coupon U[1%, 3%] with memory; put strike 100%.
+
+BOOK_STEPS_PER_YEAR = 252
+
+
+def book_universe(n_assets: int = 20, n_factors: int = 4, seed: int = 1, as_of: str = "2026-01-02") -> MarketSnapshot:
+    rng = SplitMix64(seed)
+    B = [[rng.uniform(0.2, 0.7) for _ in range(n_factors)] for _ in range(n_assets)]
+    for row in B:
+        ss = sum(b * b for b in row)
+        if ss > 0.95:
+            scale = math.sqrt(0.95 / ss)
+            for k in range(n_factors):
+                row[k] *= scale
+    corr = [[1.0 if i == j else sum(B[i][k] * B[j][k] for k in range(n_factors))
+             for j in range(n_assets)] for i in range(n_assets)]
+    vols = [rng.uniform(0.15, 0.45) for _ in range(n_assets)]
+    return MarketSnapshot(as_of, [100.0] * n_assets, vols, 0.03, [0.01] * n_assets, corr)
+
+
+def book_trades(n_trades: int, universe_assets: int, seed: int = 2, max_years: int = 5,
+                steps_per_year: int = BOOK_STEPS_PER_YEAR):
+    from .types import BookTrade
+
+    rng = SplitMix64(seed)
+    dt = 1.0 / steps_per_year
+    out = []
+    for j in range(n_trades):
+        n = 1 + rng.next_u64() % 5
+        n = min(n, universe_assets)
+        pool = list(range(universe_assets))
+        under = []
+        for _ in range(n):
+            under.append(pool.pop(rng.next_u64() % len(pool)))
+        years = 1 + rng.next_u64() % max_years
+        steps = years * steps_per_year
+        terms = PhoenixTrade(
+            trade_id=f"book-{j}", initial_spots=[100.0] * n, maturity_years=steps * dt, steps=steps,
+            strike=1.00, knock_in_barrier=rng.uniform(0.50, 0.70),
+            knock_out_barrier=rng.uniform(0.95, 1.10), coupon_barrier=rng.uniform(0.60, 0.80),
+            coupon_rate=rng.uniform(0.01, 0.03), memory_coupon=True, coupon_periods=4 * years,
+            fixed_first_coupon=False, call_start_step=63)
+        out.append(BookTrade(terms, under))
+    return out
+
+
+def book(paths: int = 1 << 18, n_trades: int = 4096, fp32: bool = True, n_assets: int = 20,
+         max_years: int = 5, steps_per_year: int = BOOK_STEPS_PER_YEAR, seed: int = 1):
+    """The book configuration (defaults: 4,096 trades, 2^18 Sobol paths, digital shift, seed 1)."""
+    from .types import BookRequest
+
+    universe = book_universe(n_assets, seed=seed)
+    steps = max_years * steps_per_year
+    config = SimulationConfig(paths, paths, 1, "off", VarianceReduction("sobol", n_assets * steps))
+    options = production_options() if fp32 else EngineOptions(
+        scrambler=abi.SCRAMBLE_DIGITAL_SHIFT, dim_mode=abi.DIM_FULL)
+    return BookRequest(universe, steps, steps / steps_per_year,
+                       book_trades(n_trades, n_assets, seed + 1, max_years, steps_per_year), config, options)
+
+
+def book_scenarios(universe: MarketSnapshot, groups: int = 4):
+    """The book's common CRN set: the base and 15 bumps — every spot ±1%, every vol ±1 point, the
+    rate ±1bp, spot +1% and -1% on each of `groups` contiguous asset groups, and every spot +1%
+    together with every vol +1 point."""
+    def bump(spot=None, vol=0.0, rate=0.0, members=None):
+        m = copy.deepcopy(universe)
+        idx = range(len(m.spots)) if members is None else members
+        for a in idx:
+            if spot is not None:
+                m.spots[a] *= spot
+            m.vols[a] += vol
+        m.risk_free_rate += rate
+        return m
+
+    n = len(universe.spots)
+    size = (n + groups - 1) // groups
+    grp = [list(range(g * size, min(n, (g + 1) * size))) for g in range(groups)]
+    out = [("base", copy.deepcopy(universe)), ("spot_up", bump(1.01)), ("spot_down", bump(0.99)),
+           ("vol_up", bump(vol=0.01)), ("vol_down", bump(vol=-0.01)), ("rate_up", bump(rate=1e-4)),
+           ("rate_down", bump(rate=-1e-4))]
+    out += [(f"group{g}_spot_up", bump(1.01, members=grp[g])) for g in range(groups)]
+    out += [(f"group{g}_spot_down", bump(0.99, members=grp[g])) for g in range(groups)]
+    out.append(("spot_up_vol_up", bump(1.01, vol=0.01)))
+    return out
+
+
+def small_book(paths: int = 512, n_assets: int = 6, n_trades: int = 8, steps_per_year: int = 12,
+               max_years: int = 3, fp32: bool = False, seed: int = 5):
+    """A book small enough for the oracle: the book configuration's shapes at toy sizes."""
+    b = book(paths, n_trades, fp32, n_assets, max_years, steps_per_year, seed)
+    for bt in b.trades:
+        bt.terms.call_start_step = min(bt.terms.call_start_step, bt.terms.steps // 4)
+    return b

@@ -1,0 +1,123 @@
+"""GPU tests of book pricing (rg_price_book / rg_book_run_paths) through the C ABI.
+
+Bars, each written in its assertion:
+* FP64 parity mode against the oracle on the same scrambled points: per (path, trade, scenario)
+  record the KO step, the qualifying-coupon count and the paid periods exactly, payoffs within
+  1e-12 relative; aggregated results within 1e-12 relative (the oracle runs the portable exp/log
+  the parity kernels use).
+* A one-trade book on every universe asset over the whole grid is bit-identical to that trade
+  priced alone by rg_price_put_leg (FP64).
+* FP32 production mode: every (trade, scenario) price within min(0.1 × MC standard error, 1bp of
+  notional) of the FP64 book on the same points.
+* Continuous batching precondition: a trade's FP32 result is bit-identical alone and in the mix.
+"""
+from __future__ import annotations
+
+import copy
+
+import pytest
+
+import oracle as O
+from riga_gb300 import abi, workloads
+from riga_gb300.build import build_library
+from riga_gb300.engine import Engine
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    build_library()
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(autouse=True)
+def portable_oracle():
+    O.set_portable_math(True)
+    yield
+    O.set_portable_math(False)
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def test_fp64_book_records_match_the_oracle(engine):
+    b = workloads.small_book(paths=256, n_trades=6)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:3]
+    got = engine.book_run_paths_raw(b, sc, 0, 64)
+    want = O.book_run_paths(b, sc, 0, 64)
+    assert len(got) == len(want) == 64 * 6 * 3
+    for g, w in zip(got, want):
+        assert (g.path_id, g.knocked_out, g.ko_step, g.ki_hit, g.qualified_steps, g.paid_periods) == \
+            (w.path_id, w.knocked_out, w.ko_step, w.ki_hit, w.qualified_steps, w.paid_periods)
+        for f in ("pv", "put_payoff", "coupon_pv", "memory_coupon_pv", "funding", "worst_final"):
+            assert _rel(getattr(g, f), getattr(w, f)) <= 1e-12, f
+
+
+def test_fp64_book_prices_match_the_oracle(engine):
+    b = workloads.small_book(paths=1024, n_trades=5)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:4]
+    got = engine.price_book_raw(b, sc)
+    want = O.price_book(b, sc, threads=8)
+    for g, w in zip(got, want):
+        assert (g.ko_count, g.ki_count, g.put_eligible_count, g.coupon_path_count) == \
+            (w.ko_count, w.ki_count, w.put_eligible_count, w.coupon_path_count)
+        assert _rel(g.pv, w.pv) <= 1e-12
+        assert _rel(g.mc_error, w.mc_error) <= 1e-9
+
+
+def test_one_trade_book_is_bit_identical_to_price_put_leg(engine):
+    req = workloads.plain3(paths=2048, steps=126)
+    n = len(req.market.spots)
+    from riga_gb300.types import BookRequest, BookTrade
+    b = BookRequest(copy.deepcopy(req.market), req.trade.steps, req.trade.maturity_years,
+                    [BookTrade(copy.deepcopy(req.trade), list(range(n)))], copy.deepcopy(req.config),
+                    copy.deepcopy(req.options))
+    booked = engine.book_run_paths_raw(b, None, 0, 512)
+    single = engine.run_paths_raw(req, 0, 512)
+    for g, w in zip(booked, single):
+        assert (g.ko_step, g.qualified_steps, g.paid_periods, g.pv, g.worst_final) == \
+            (w.ko_step, w.qualified_steps, w.paid_periods, w.pv, w.worst_final)
+
+
+def test_fp32_book_within_a_tenth_of_the_standard_error(engine):
+    b64 = workloads.small_book(paths=1 << 14, n_trades=8, steps_per_year=52, max_years=2)
+    b32 = copy.deepcopy(b64)
+    b32.options = workloads.production_options()
+    sc = [m for _, m in workloads.book_scenarios(b64.universe)]
+    r64 = engine.price_book_raw(b64, sc)
+    r32 = engine.price_book_raw(b32, sc)
+    for a, w in zip(r32, r64):
+        bound = min(0.1 * w.mc_error, 1e-4)  # min(0.1 SE, 1bp of notional)
+        assert abs(a.pv - w.pv) <= bound
+
+
+def test_fp32_trade_is_bit_identical_alone_and_in_the_mix(engine):
+    b = workloads.small_book(paths=1 << 13, n_trades=7, steps_per_year=52, max_years=2, fp32=True)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:5]
+    mixed = engine.price_book_raw(b, sc)
+    for j in (0, 4, 6):
+        alone = copy.deepcopy(b)
+        alone.trades = [b.trades[j]]
+        res = engine.price_book_raw(alone, sc)
+        for s in range(len(sc)):
+            assert bytes(res[s]) == bytes(mixed[j * len(sc) + s])
+
+
+def test_fp32_book_is_deterministic_across_calls(engine):
+    b = workloads.small_book(paths=1 << 12, n_trades=5, steps_per_year=52, fp32=True)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:3]
+    a = engine.price_book_raw(b, sc)
+    c = engine.price_book_raw(b, sc)
+    assert [bytes(x) for x in a] == [bytes(x) for x in c]
+
+
+def test_book_errors_keep_the_reference_codes(engine):
+    b = workloads.small_book(paths=64, n_trades=2)
+    b.trades[1].underlyings[0] = 77
+    with pytest.raises(abi.RigaError) as e:
+        engine.price_book_raw(b)
+    assert e.value.code == "invalid_market_shape"
