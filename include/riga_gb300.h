@@ -371,6 +371,72 @@ int32_t rg_book_run_paths(rg_engine* engine, const rg_book_request* request,
                           const rg_market_snapshot* scenarios, int32_t n_scenarios,
                           uint64_t first_path, uint64_t count, rg_path_record* out);
 
+/* ------------------------------------------------------------------ serving ------------------- */
+/* A continuous-batching request server on one GPU (the engine side of the reference's MCP task
+ * loop, crates/riga-mcp/src/main.rs:1000-1042, with its tasks/get, tasks/result and tasks/cancel
+ * semantics).  It owns `slots` engines, each with its own CUDA stream and workspace.  Submitted
+ * requests are deep-copied and queued in arrival order; a request is admitted as soon as a slot is
+ * free and its device-memory estimate fits in the budget beside the slots' current holdings (idle
+ * slots release their buffers when that makes room), so requests that arrive while others run are
+ * admitted as slots and memory free up and run concurrently with them on the device.  A request's
+ * results do not depend on what runs beside it.  Requests whose estimate exceeds the whole budget
+ * are rejected at submission (RG_ERR_INVALID_ARGUMENT). */
+typedef struct rg_server rg_server;
+
+typedef struct rg_server_config {
+  int32_t device;
+  int32_t slots;                 /* concurrent requests (engines); 0 = 4 */
+  uint64_t device_memory_budget; /* bytes for the slots' workspaces; 0 = 80% of free memory */
+} rg_server_config;
+
+enum { RG_JOB_QUEUED = 0, RG_JOB_RUNNING = 1, RG_JOB_DONE = 2, RG_JOB_FAILED = 3, RG_JOB_CANCELLED = 4 };
+enum { RG_JOB_PRICE = 0, RG_JOB_RISK = 1, RG_JOB_BOOK = 2 };
+
+typedef struct rg_job_info {
+  int32_t state;          /* RG_JOB_* */
+  int32_t status;         /* RG_OK or the failure's status code once FAILED */
+  int32_t kind;           /* RG_JOB_PRICE / RISK / BOOK */
+  int32_t slot;           /* slot that ran it, -1 before admission */
+  uint64_t n_results;     /* rg_price_result entries the request produces */
+  uint64_t device_bytes;  /* admission estimate */
+  double submit_s, start_s, end_s; /* seconds since the server started (0 until reached) */
+} rg_job_info;
+
+typedef struct rg_server_stats {
+  uint64_t submitted, completed, failed, cancelled, queued, running;
+  uint64_t device_bytes_held, device_memory_budget;
+  double p50_ms, p99_ms, max_ms; /* submit-to-completion latency of completed requests */
+  double busy_s;                 /* wall time with at least one request running */
+} rg_server_stats;
+
+int32_t rg_server_create(const rg_server_config* config, rg_server** out);
+/* Waits for running requests, cancels queued ones and frees the engines. */
+void rg_server_destroy(rg_server* server);
+/* A price request, optionally over a CRN scenario batch (n_scenarios 0 = the request's market). */
+int32_t rg_server_submit_price(rg_server* server, const rg_price_request* request,
+                               const rg_scenario* scenarios, int32_t n_scenarios, uint64_t* ticket);
+/* riga_risk::price_risk_batch (crates/riga-risk/src/lib.rs:573-626). */
+int32_t rg_server_submit_risk(rg_server* server, const rg_price_request* request,
+                              const rg_central_difference_config* config, uint64_t* ticket);
+/* A book under a common scenario set (rg_price_book). */
+int32_t rg_server_submit_book(rg_server* server, const rg_book_request* request,
+                              const rg_market_snapshot* scenarios, int32_t n_scenarios, uint64_t* ticket);
+/* Current state without blocking. */
+int32_t rg_server_poll(rg_server* server, uint64_t ticket, rg_job_info* info);
+/* Blocks until the request is DONE, FAILED or CANCELLED, or `timeout_ms` passes (negative = no
+ * limit; RG_ERR_TIMEOUT when it passes first).  Returns RG_OK with the final state in *info; a
+ * FAILED request's status and message are also the calling thread's rg_last_error. */
+int32_t rg_server_wait(rg_server* server, uint64_t ticket, int64_t timeout_ms, rg_job_info* info);
+/* Copies a DONE price or book request's results (n_results entries) into out[capacity]. */
+int32_t rg_server_results(rg_server* server, uint64_t ticket, rg_price_result* out, uint64_t capacity);
+/* Copies a DONE risk request's report. */
+int32_t rg_server_risk_report(rg_server* server, uint64_t ticket, rg_batch_risk_report* out);
+/* A queued request is dropped; a running one finishes on the device and is reported CANCELLED. */
+int32_t rg_server_cancel(rg_server* server, uint64_t ticket);
+/* Forgets a finished request and its results. */
+int32_t rg_server_release(rg_server* server, uint64_t ticket);
+int32_t rg_server_get_stats(rg_server* server, rg_server_stats* out);
+
 /* ------------------------------------------------------------------ host tables --------------- */
 /* The Sobol direction table v[dim][32] the engine uses for `dim` dimensions: dimension 0 is van
  * der Corput, dimension d >= 1 the Joe–Kuo recurrence with unit initial values on the d-th

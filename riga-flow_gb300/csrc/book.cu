@@ -296,6 +296,29 @@ uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t un
   return paths < cap ? paths : cap;
 }
 
+}  // namespace
+
+size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
+  const size_t S = n_scen > 0 ? (size_t)n_scen : 1;
+  const size_t U = (size_t)(r->universe.n_assets > 0 ? r->universe.n_assets : 1);
+  const size_t TU = (size_t)(r->universe_steps > 0 ? r->universe_steps : 1);
+  const size_t pairs = (size_t)(r->n_trades > 0 ? r->n_trades : 1) * S;
+  const uint64_t P = r->config.paths;
+  const bool fp32 = r->config.precision == RG_PRECISION_FP32;
+  const size_t elem = fp32 ? sizeof(float) : sizeof(double);
+  const uint64_t unit = fp32 ? (uint64_t)book32_shape((int)std::min<size_t>(S, 32), device_sm_count()).blk_paths : 128;
+  const uint64_t PC = chunk_paths(P, (int)U, (int64_t)TU, elem, unit);
+  const uint64_t chunks = (P + PC - 1) / PC;
+  size_t b = (size_t)PC * U * TU * elem * (fp32 && chunks > 1 ? 2 : 1);
+  const uint64_t blocks = fp32 ? (P + unit - 1) / unit : ((PC + 127) / 128) * chunks;
+  b += (size_t)blocks * pairs * RG_ACC * 8 + pairs * RG_ACC * 8;
+  size_t sob_rows = r->config.dim_mode == RG_DIM_FULL ? U * TU : 512;
+  b += sob_rows * 128 + TU * 32 + S * TU * 8 + pairs * 96 + (size_t)r->n_trades * 256 + (size_t(64) << 10);
+  return b + b / 8 + (size_t(1) << 20);
+}
+
+namespace {
+
 // Prices (records == nullptr) or replays [first, first + count) of the book.
 void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* sc, int n_scen,
               rg_price_result* out, uint64_t first, uint64_t count, rg_path_record* records) {

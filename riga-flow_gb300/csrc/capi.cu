@@ -6,6 +6,7 @@
 //   (Dupire calibration per distinct surface, Cholesky per scenario) → fused path kernel
 //   (FP64 parity or FP32 CRN) → fixed-order reduction → one D2H copy of the FP64 sums →
 //   PriceResult assembly on the host (note.rs:262-372).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -515,6 +516,46 @@ struct EngineWorkspace : Workspace {
     return E->host_sums.ptr;
   }
 };
+
+size_t estimate_price_bytes(const rg_price_request* r, int n_scen) {
+  const size_t S = n_scen > 0 ? (size_t)n_scen : 1;
+  const size_t n = (size_t)(r->market.n_assets > 0 ? r->market.n_assets : 1);
+  const size_t T = (size_t)(r->trade.steps > 0 ? r->trade.steps : 1);
+  const bool fp32 = r->config.precision == RG_PRECISION_FP32;
+  size_t sob_rows = r->config.dim_mode == RG_DIM_FULL ? n * T : 512;
+  size_t b = sob_rows * 128 + n * T * 64 + S * T * 8 + S * 1024 + (size_t(64) << 10);  // tables
+  if (r->n_local_vol) {
+    const size_t gx = (size_t)(r->config.lv_grid_x > 0 ? r->config.lv_grid_x : 96);
+    size_t nt = 1, nk = 1;
+    for (int f = 0; f < r->n_local_vol; ++f) {
+      nt = std::max(nt, (size_t)r->local_vol[f].n_maturities);
+      nk = std::max(nk, (size_t)r->local_vol[f].n_strikes);
+    }
+    const size_t surf = S * n;
+    b += surf * ((2 * nt * gx + gx) * 8 + (4 * nt * gx + gx + 6 * nt * nk) * 8);  // calibration
+    if (fp32) b += surf * T * gx * 8;                                            // step rows
+  }
+  const size_t grid = fp32 ? (size_t)device_info().sm_count * 2 : 152 * 16;
+  b += grid * std::min<size_t>(S, 32) * RG_ACC * 8 + S * RG_ACC * 8;  // partial and reduced sums
+  if (r->config.trace_level != RG_TRACE_OFF) b += (size_t)r->config.paths * 4;
+  return b + b / 4 + (size_t(1) << 20);
+}
+
+size_t engine_device_bytes(rg_engine* E) {
+  size_t b = 0;
+  for (const DevBuf& d : E->bufs) b += d.bytes;
+  for (const DevBuf& d : E->book_bufs) b += d.bytes;
+  return b;
+}
+
+void engine_trim(rg_engine* E) {
+  std::lock_guard<std::mutex> lock(E->mu);
+  cuda_check(cudaSetDevice(E->device), "cudaSetDevice");
+  cuda_check(cudaStreamSynchronize(E->stream), "trim");
+  cuda_check(cudaStreamSynchronize(E->gen_stream), "trim");
+  for (DevBuf& d : E->bufs) d.release();
+  for (DevBuf& d : E->book_bufs) d.release();
+}
 
 static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* sc, int n_scen,
                   rg_price_result* out) {

@@ -269,6 +269,16 @@ void launch_book_reduce_strided(const double* partial, int64_t blocks, int64_t s
 
 int32_t rg_guard_device();
 
+struct rg_engine;
+namespace rg {
+// Device bytes an engine's workspace holds, and releasing them (the engine must be idle).
+size_t engine_device_bytes(rg_engine* E);
+void engine_trim(rg_engine* E);
+// Device bytes one call will hold at its peak (workspace buffers; upper estimates).
+size_t estimate_price_bytes(const rg_price_request* r, int n_scen);
+size_t estimate_book_bytes(const rg_book_request* r, int n_scen);
+}  // namespace rg
+
 // The engine behind the opaque C handle.
 struct rg_engine {
   int device = 0;

@@ -277,6 +277,28 @@ class BookRequest(C.Structure):
                 ("trades", C.POINTER(BookTrade)), ("config", SimConfig)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("device_memory_budget", C.c_uint64)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("kind", C.c_int32), ("slot", C.c_int32),
+                ("n_results", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("queued", C.c_uint64), ("running", C.c_uint64),
+                ("device_bytes_held", C.c_uint64), ("device_memory_budget", C.c_uint64),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("busy_s", C.c_double)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
+JOB_PRICE, JOB_RISK, JOB_BOOK = range(3)
+
+
 class RigaError(Exception):
     """Mirror of ``RigaError { code, message }`` (crates/riga-core/src/lib.rs:5-19)."""
 
@@ -312,6 +334,21 @@ SIGNATURES = {
                              C.POINTER(PriceResult)]),
     "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,
                                  C.POINTER(PathRecord)]),
+    "rg_server_create": (_i32, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "rg_server_destroy": (None, [_vp]),
+    "rg_server_submit_price": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32,
+                                      C.POINTER(_u64)]),
+    "rg_server_submit_risk": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(CentralDifferenceConfig),
+                                     C.POINTER(_u64)]),
+    "rg_server_submit_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
+                                     C.POINTER(_u64)]),
+    "rg_server_poll": (_i32, [_vp, _u64, C.POINTER(JobInfo)]),
+    "rg_server_wait": (_i32, [_vp, _u64, _i64, C.POINTER(JobInfo)]),
+    "rg_server_results": (_i32, [_vp, _u64, C.POINTER(PriceResult), _u64]),
+    "rg_server_risk_report": (_i32, [_vp, _u64, C.POINTER(BatchRiskReport)]),
+    "rg_server_cancel": (_i32, [_vp, _u64]),
+    "rg_server_release": (_i32, [_vp, _u64]),
+    "rg_server_get_stats": (_i32, [_vp, C.POINTER(ServerStats)]),
     "rg_sobol_directions": (_i32, [_i64, C.POINTER(C.c_uint32)]),
     "rg_bridge_schedule": (_i32, [_i64, C.c_double, C.POINTER(_i32), C.POINTER(_i32),
                                   C.POINTER(C.c_double), C.POINTER(_i32)]),

@@ -1,0 +1,176 @@
+"""GPU tests of the continuous-batching server (rg_server_*) and the MCP-shaped loop over it.
+
+* Every request's result is bit-identical in the mix and alone: a mix of price, CRN-batch, risk
+  and book requests submitted from several threads at once, against the same requests priced one
+  at a time through a plain engine.
+* Work overlaps: with several slots, requests that were queued together run at the same time.
+* Admission by device memory: with a budget that holds one request at a time, requests never
+  overlap and all complete; a request larger than the whole budget is rejected at submission.
+* Tasks: a queued request can be cancelled, a wait can time out, and stats report p50/p99.
+"""
+from __future__ import annotations
+
+import copy
+import threading
+
+import pytest
+
+from riga_gb300 import abi, workloads
+from riga_gb300.abi import RigaError
+from riga_gb300.build import build_library
+from riga_gb300.engine import Engine
+from riga_gb300.serve import McpLoop, Server, default_risk_config
+from riga_gb300.types import result_to_json
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    build_library()
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+def _mix():
+    """(kind, request, scenarios) of a varied request mix."""
+    mix = []
+    mix.append(("price", workloads.plain3(paths=1 << 12, steps=126), None))
+    p32 = workloads.plain3(paths=1 << 14, steps=252, fp32=True)
+    mix.append(("price", p32, [(m, s) for _, m, s in workloads.crn15_scenarios(p32)][:8]))
+    lv = workloads.lv3(paths=1 << 13, steps=126)
+    mix.append(("price", lv, [(m, s) for _, m, s in workloads.crn15_scenarios(lv)]))
+    mix.append(("risk", workloads.plain3(paths=1 << 11, steps=63), None))
+    b = workloads.small_book(paths=1 << 12, n_trades=6, steps_per_year=52, fp32=True)
+    mix.append(("book", b, [m for _, m in workloads.book_scenarios(b.universe)]))
+    b64 = workloads.small_book(paths=512, n_trades=3)
+    mix.append(("book", b64, [m for _, m in workloads.book_scenarios(b64.universe)][:2]))
+    return mix
+
+
+def _alone(engine, kind, req, sc):
+    if kind == "price":
+        return [engine.price_raw(req)] if sc is None else engine.price_scenarios_raw(req, sc)
+    if kind == "risk":
+        return engine.price_risk_batch_raw(req, default_risk_config())
+    return engine.price_book_raw(req, sc)
+
+
+def _submit(server, kind, req, sc):
+    if kind == "price":
+        return server.submit_price(req, sc)
+    if kind == "risk":
+        return server.submit_risk(req)
+    return server.submit_book(req, sc)
+
+
+def _collect(server, kind, t):
+    return server.risk_report(t) if kind == "risk" else server.results(t)
+
+
+def test_results_are_identical_alone_and_in_the_mix(engine):
+    mix = _mix() * 2
+    alone = [_alone(engine, k, r, s) for k, r, s in mix]
+    with Server(slots=4) as srv:
+        tickets = [None] * len(mix)
+
+        def submit(i):
+            tickets[i] = _submit(srv, *mix[i])
+
+        threads = [threading.Thread(target=submit, args=(i,)) for i in range(len(mix))]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        got = [_collect(srv, mix[i][0], tickets[i]) for i in range(len(mix))]
+        st = srv.stats()
+    assert st.completed == len(mix) and st.failed == 0
+    assert st.p50_ms > 0 and st.p99_ms >= st.p50_ms
+    for (kind, _, _), a, g in zip(mix, alone, got):
+        if kind == "risk":
+            assert bytes(a) == bytes(g)
+        else:
+            assert [bytes(x) for x in a] == [bytes(x) for x in g]
+
+
+def test_queued_requests_overlap_on_the_device():
+    reqs = [workloads.lv3(paths=1 << 17, steps=252) for _ in range(4)]
+    for r in reqs:
+        r.options = workloads.production_options()
+    with Server(slots=4) as srv:
+        ts = [srv.submit_price(r, [(m, s) for _, m, s in workloads.crn15_scenarios(r)]) for r in reqs]
+        infos = [srv.wait(t) for t in ts]
+    spans = sorted((i.start_s, i.end_s) for i in infos)
+    assert any(spans[k + 1][0] < spans[k][1] for k in range(len(spans) - 1))
+    assert len({i.slot for i in infos}) > 1
+
+
+def test_memory_budget_admits_one_request_at_a_time():
+    books = [workloads.small_book(paths=1 << 13, n_trades=4, steps_per_year=52, fp32=True, seed=s) for s in range(4)]
+    with Server(slots=4, memory_budget=1 << 62) as probe:
+        t = probe.submit_book(books[0])
+        est = probe.wait(t).device_bytes
+    with Server(slots=4, memory_budget=int(est * 1.5)) as srv:
+        ts = [srv.submit_book(b) for b in books]
+        infos = [srv.wait(t) for t in ts]
+        results = [srv.results(t) for t in ts]
+    spans = sorted((i.start_s, i.end_s) for i in infos)
+    assert all(spans[k + 1][0] >= spans[k][1] for k in range(len(spans) - 1))
+    assert all(len(r) == 4 for r in results)
+
+
+def test_a_request_larger_than_the_budget_is_rejected():
+    with Server(slots=2, memory_budget=1 << 20) as srv:
+        with pytest.raises(RigaError) as e:
+            srv.submit_book(workloads.small_book(paths=1 << 14, n_trades=4, steps_per_year=52, fp32=True))
+        assert e.value.code == "invalid_argument"
+
+
+def test_cancel_a_queued_request_and_wait_timeouts():
+    big = workloads.lv3(paths=1 << 17, steps=756)
+    big.options = workloads.production_options()
+    sc = [(m, s) for _, m, s in workloads.crn15_scenarios(big)]
+    with Server(slots=1) as srv:
+        a = srv.submit_price(big, sc)
+        b = srv.submit_price(big, sc)
+        srv.cancel(b)
+        assert srv.poll(b).state == abi.JOB_CANCELLED
+        with pytest.raises(RigaError) as e:
+            srv.wait(a, timeout_ms=0)
+        assert e.value.code == "device_timeout"
+        assert srv.wait(a).state == abi.JOB_DONE
+        with pytest.raises(RigaError) as e:
+            srv.results(b)
+        assert e.value.code == "cancelled"
+        st = srv.stats()
+        assert st.completed == 1 and st.cancelled == 1
+
+
+def test_failed_request_reports_the_reference_code():
+    with Server(slots=2) as srv:
+        b = workloads.small_book(paths=64, n_trades=2)
+        b.trades[1].underlyings[0] = 40
+        t = srv.submit_book(b)
+        with pytest.raises(RigaError) as e:
+            srv.wait(t)
+        assert e.value.code == "invalid_market_shape"
+        assert srv.stats().failed == 1
+
+
+def test_mcp_loop_over_the_gpu_server(engine):
+    """The reference's request JSON alone prices with the reference's arithmetic (Owen scrambling,
+    FP64, 512-dimension wrap); the engine knobs ride in "options"."""
+    from riga_gb300.types import EngineOptions, PriceRequest
+    req = workloads.plain3(paths=1 << 12, steps=126)
+    plain = PriceRequest.from_json(req.to_json())
+    with Server(slots=2) as srv:
+        loop = McpLoop(srv)
+        out = loop.handle({"jsonrpc": "2.0", "id": 1, "method": "tools/call",
+                           "params": {"name": "price_trade", "arguments": {"request": req.to_json()}}})
+        knobs = {"scrambler": req.options.scrambler, "precision": req.options.precision,
+                 "dim_mode": req.options.dim_mode}
+        out2 = loop.handle({"jsonrpc": "2.0", "id": 2, "method": "tools/call",
+                            "params": {"name": "price_trade", "arguments": {"request": req.to_json(), "options": knobs}}})
+    assert out["result"]["structuredContent"] == result_to_json(engine.price_raw(plain), plain)
+    assert out2["result"]["structuredContent"] == result_to_json(engine.price_raw(req), req)
