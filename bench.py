@@ -21,6 +21,7 @@ from __future__ import annotations
 import argparse
 import copy
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -167,6 +168,105 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- book (cfg 2) --
+def book_measure(eng, n_trades: int, paths: int):
+    """The book configuration in one call: `n_trades` trades of the 20-asset universe at `paths`
+    Sobol paths under the book's 16 common scenarios, FP32, host inputs (rg_price_book)."""
+    import torch
+    from riga_gb300 import workloads
+
+    b = workloads.book(paths=paths, n_trades=n_trades, fp32=True)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)]
+    warm = copy.deepcopy(b)
+    warm.config.paths = 1 << 12
+    eng.price_book_raw(warm, sc)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.price_book_raw(b, sc)
+    wall = time.perf_counter() - t0
+    units = float(sum(t.terms.steps for t in b.trades)) * paths * len(sc)
+    # accuracy: FP32 against the FP64 book on the same points, first 16 trades at 2^14 paths
+    sub32 = workloads.book(paths=1 << 14, n_trades=16, fp32=True)
+    sub64 = workloads.book(paths=1 << 14, n_trades=16, fp32=False)
+    r32 = eng.price_book_raw(sub32, sc)
+    r64 = eng.price_book_raw(sub64, sc)
+    errs = [abs(a.pv - w.pv) for a, w in zip(r32, r64)]
+    within = all(abs(a.pv - w.pv) <= min(0.1 * w.mc_error, 1e-4) for a, w in zip(r32, r64))
+    return {"workload": f"book: {n_trades} Phoenix trades (1-5 underlyings, 1-5y) on a 20-asset 4-factor "
+                        f"universe, one universe path set on 1260 daily steps, {paths} Sobol paths, "
+                        f"{len(sc)} common CRN scenarios, one rg_price_book call with host inputs",
+            "trades": n_trades, "paths": paths, "scenarios": len(sc), "wall_s": wall,
+            "path_steps_per_s": units / wall, "trades_bumps_per_s": n_trades * len(sc) / wall,
+            "accuracy": {"max_abs_err_vs_fp64": max(errs), "within_min_0.1se_1bp": within,
+                         "sample": "first 16 trades, 2^14 paths, 16 scenarios"}}
+
+
+def fp64_plain_rate(eng):
+    """The plain FP64 GPU path: the FP64 parity kernel pricing one trade per call (3-asset
+    flat-vol Phoenix, 2^16 paths, 756 steps), path-steps/s through rg_price_put_leg."""
+    from riga_gb300 import workloads
+
+    req = workloads.plain3(paths=1 << 16, steps=756)
+    eng.price_raw(req)
+    t0 = time.perf_counter()
+    eng.price_raw(req)
+    wall = time.perf_counter() - t0
+    return float(1 << 16) * 756 / wall
+
+
+# ----------------------------------------------------------------------------- serving (cfg 3) -
+def serving_measure(duration_s: float = 5.0, rate_per_s: float = 200.0, seed: int = 7):
+    """Seeded Poisson arrivals into the continuous-batching server (4 slots): 90% single trades
+    (3-asset local vol, 2^14 paths, 756 steps, FP32) with 0, 7 or 15 CRN bumps, 10% books of
+    16-64 trades of the book universe at 2^14 paths under 8 common scenarios.  Latency is submit
+    to completion; throughput counts every finished request's path-steps."""
+    from riga_gb300 import workloads
+    from riga_gb300.serve import Server
+
+    rng = workloads.SplitMix64(seed)
+    single = workloads.lv3(paths=1 << 14, steps=756, fp32=True)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(single)]
+    bk = workloads.book(paths=1 << 14, n_trades=64, fp32=True)
+    bsc = [m for _, m in workloads.book_scenarios(bk.universe)][:8]
+    plan, t = [], 0.0
+    while True:
+        t += -math.log(1.0 - rng.uniform(0.0, 1.0)) / rate_per_s
+        if t >= duration_s:
+            break
+        if rng.uniform(0.0, 1.0) < 0.9:
+            k = (0, 7, 15)[rng.next_u64() % 3]
+            plan.append((t, "price", k))
+        else:
+            plan.append((t, "book", 16 + rng.next_u64() % 49))
+    units = 0.0
+    with Server(slots=4) as srv:
+        srv.wait(srv.submit_price(single, scen[:1]))  # warm the slots' engines
+        t0 = time.perf_counter()
+        tickets = []
+        for at, kind, k in plan:
+            delay = at - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            if kind == "price":
+                tickets.append(srv.submit_price(single, scen[: k + 1] if k else None))
+                units += float(1 << 14) * 756 * (k + 1)
+            else:
+                b = copy.deepcopy(bk)
+                b.trades = bk.trades[:k]
+                tickets.append(srv.submit_book(b, bsc))
+                units += float(sum(tr.terms.steps for tr in b.trades)) * (1 << 14) * len(bsc)
+        for tk in tickets:
+            srv.wait(tk)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    return {"workload": f"Poisson arrivals at {rate_per_s:g}/s for {duration_s:g} s (seed {seed}): 90% single "
+                        f"3-asset local-vol trades at 2^14 paths with 0/7/15 bumps, 10% 16-64-trade books at "
+                        f"2^14 paths x 8 scenarios; 4 slots",
+            "requests": len(plan), "completed": st.completed, "failed": st.failed,
+            "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "max_ms": st.max_ms, "wall_s": wall,
+            "path_steps_per_s": units / wall, "busy_s": st.busy_s}
+
+
 # ----------------------------------------------------------------------------- GPU arm --------
 def run_gpu(args):
     import torch
@@ -277,6 +377,16 @@ def run_gpu(args):
     }
     if merged_pv is not None:
         line["merged_base_pv"] = merged_pv
+    if world == 1 and not args.no_book:
+        book = book_measure(eng, args.book_trades, args.book_paths)
+        plain = fp64_plain_rate(eng)
+        book["fp64_plain_path_steps_per_s"] = plain
+        book["fp64_plain_workload"] = ("FP64 parity kernel, one trade per call: 3-asset flat-vol Phoenix, "
+                                       "2^16 paths x 756 steps, rg_price_put_leg")
+        book["throughput_vs_fp64_plain"] = book["path_steps_per_s"] / plain
+        line["book"] = book
+    if world == 1 and not args.no_serving:
+        line["serving"] = serving_measure()
     if world == 1 and not args.no_cpu_baseline:
         rate, cores, paths, dt = cpu_rate(P, T, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -295,6 +405,10 @@ def main():
     ap.add_argument("--timesteps", type=int, default=756)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-book", action="store_true", help="skip the book (cfg 2) measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving (cfg 3) measurement")
+    ap.add_argument("--book-trades", type=int, default=4096)
+    ap.add_argument("--book-paths", type=int, default=1 << 18)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

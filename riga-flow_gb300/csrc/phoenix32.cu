@@ -413,12 +413,29 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
   sh.TT = tt;
   sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
-  for (int rec = 0; rec < 2; ++rec) {
-    const void* kr = select_kernel(P.n, P.trade.has_lv != 0, rec != 0);
-    cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem),
-               "phoenix32 smem attribute");
-    cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
-               "phoenix32 carveout");
+  // Function attributes are process-wide: raise every instantiation's dynamic shared-memory limit
+  // to the device maximum once, so engines pricing concurrently never lower it under each other.
+  {
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (!done[dev]) {
+      int optin = 0;
+      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem opt-in");
+      for (int n = 1; n <= RG_NMAX; ++n)
+        for (int lv = 0; lv < 2; ++lv)
+          for (int rec = 0; rec < 2; ++rec) {
+            const void* kr = select_kernel(n, lv != 0, rec != 0);
+            cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
+                       "phoenix32 smem attribute");
+            cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                       "phoenix32 carveout");
+          }
+      done[dev] = 1;
+    }
   }
   const void* k = select_kernel(P.n, P.trade.has_lv != 0, false);
   int per_sm = 0;

@@ -174,3 +174,18 @@ def test_mcp_loop_over_the_gpu_server(engine):
                             "params": {"name": "price_trade", "arguments": {"request": req.to_json(), "options": knobs}}})
     assert out["result"]["structuredContent"] == result_to_json(engine.price_raw(plain), plain)
     assert out2["result"]["structuredContent"] == result_to_json(engine.price_raw(req), req)
+
+
+def test_concurrent_requests_of_different_launch_shapes(engine):
+    """FP32 requests with 1..16 scenarios (shared-memory footprints from ~60 to ~160 KB) priced
+    concurrently on four slots all succeed and equal the same requests priced alone: a kernel's
+    launch attributes are process-wide, so no request may narrow them for another."""
+    base = workloads.lv3(paths=1 << 14, steps=252)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(base)]
+    reqs = [(base, scen[:k]) for k in (1, 2, 3, 5, 8, 11, 16)] * 3
+    alone = [engine.price_scenarios_raw(r, sc) for r, sc in reqs]
+    with Server(slots=4) as srv:
+        ts = [srv.submit_price(r, sc) for r, sc in reqs]
+        got = [srv.results(t) for t in ts]
+    for a, g in zip(alone, got):
+        assert [bytes(x) for x in a] == [bytes(x) for x in g]
