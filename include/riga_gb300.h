@@ -452,6 +452,30 @@ int32_t rg_sobol_directions(int64_t dim, uint32_t* out /* [dim * 32] */);
 int32_t rg_bridge_schedule(int64_t steps, double dt, int32_t* node_off, int32_t* node_k,
                            double* node_c, int32_t* stack_depth);
 
+/* ------------------------------------------------------------------ pseudo-random lane ------- */
+/* The reference's MC lane draws ChaCha8Rng::seed_from_u64(seed) -> rand_distr::StandardNormal
+ * (rand_chacha 0.9.0, rand_distr 0.5.1; note.rs:58,123-127): one sequential stream in which path p,
+ * step s, factor f is draw (p·T + s)·n + f.  The engine generates that stream on the device (a
+ * parallel parse of the ziggurat's variable consumption), so VarianceReduction::None prices on the
+ * GPU through rg_price_put_leg / rg_price_scenarios / rg_price_risk_batch / rg_run_paths (always
+ * with the FP64 kernel) and the PathCube functions below exist.  Not available through
+ * rg_price_put_leg_static (RG_ERR_UNSUPPORTED). */
+
+/* Draws [first, first + count) of the stream for `seed` (count <= 2^31). */
+int32_t rg_chacha8_normals(uint64_t seed, uint64_t first, uint64_t count, double* out);
+
+/* pathcube::generate_correlated_block, crates/riga-engine/src/pathcube.rs:37-66: out[path][time]
+ * [factor] = (f32)(L·z) with z the stream's draws in (path, time, factor) order and `chol` the
+ * factors × factors Cholesky factor (row-major, lower triangle read). */
+int32_t rg_generate_correlated_block(uint64_t seed, int64_t paths, int64_t times, int32_t factors,
+                                     const double* chol, float* out);
+
+/* pathcube::gbm_evolve, crates/riga-engine/src/pathcube.rs:146-187: out[path][time][factor] =
+ * (f32)exp(ln s0 + Σ_{i<=time} ((rate - q - vol²/2)·dt + vol·√dt·block[path][i][factor])). */
+int32_t rg_gbm_evolve(const double* s0, const double* vols, double rate, const double* dividend_yields,
+                      int32_t factors, double dt, const float* block, int64_t paths, int64_t times,
+                      float* out);
+
 /* ------------------------------------------------------------------ gpu backend drop-in ------- */
 /* gpu::worst_of, crates/riga-engine/src/gpu.rs:171-205 / :515-517 (out = min(a, b)). */
 int32_t rg_worst_of(const float* a, const float* b, float* out, int64_t n);

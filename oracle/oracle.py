@@ -163,6 +163,41 @@ def price_scenarios(request, scenarios, threads: int = 0):
     return out
 
 
+def chacha8_normals(seed: int, count: int):
+    buf = (C.c_double * max(1, count))()
+    L = lib()
+    L.or_chacha8_normals.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]
+    L.or_chacha8_normals(seed, count, buf)
+    return buf
+
+
+def generate_correlated_block(seed: int, paths: int, times: int, chol):
+    """pathcube::generate_correlated_block restated; `chol` is a factors x factors list of rows."""
+    n = len(chol)
+    Lm = (C.c_double * (n * n))(*[v for r in chol for v in r])
+    out = (C.c_float * max(1, paths * times * n))()
+    L = lib()
+    L.or_generate_correlated_block.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int32,
+                                               C.POINTER(C.c_double), C.POINTER(C.c_float)]
+    L.or_generate_correlated_block(seed, paths, times, n, Lm, out)
+    return out
+
+
+def gbm_evolve(s0, vols, rate, q, dt, block, paths, times):
+    """pathcube::gbm_evolve restated; `block` is a flat f32 sequence [path][time][factor]."""
+    n = len(s0)
+    arr = lambda v: (C.c_double * n)(*v)
+    blk = (C.c_float * len(block))(*block) if not isinstance(block, C.Array) else block
+    out = (C.c_float * max(1, paths * times * n))()
+    L = lib()
+    L.or_gbm_evolve.restype = C.c_int32
+    L.or_gbm_evolve.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double),
+                                C.c_int32, C.c_double, C.POINTER(C.c_float), C.c_int64, C.c_int64,
+                                C.POINTER(C.c_float)]
+    _check(L.or_gbm_evolve(arr(s0), arr(vols), rate, arr(q), n, dt, blk, paths, times, out))
+    return out
+
+
 def price_book(book, scenarios=None, threads: int = 0):
     """A book (``riga_gb300.types.BookRequest``) under a common scenario set: ``out[j * S + s]``."""
     from riga_gb300.types import markets_to_abi

@@ -1743,3 +1743,39 @@ int32_t or_book_run_paths(const rg_book_request* r, const rg_market_snapshot* sc
   book_free(&b);
   return RG_OK;
 }
+
+/* ============================================================ PathCube ======================= */
+/* generate_correlated_block, crates/riga-engine/src/pathcube.rs:37-66: per (path, time) draw
+ * `factors` normals of the one ChaCha8 stream, y = L·z, store (f32)y. */
+void or_generate_correlated_block(uint64_t seed, int64_t paths, int64_t times, int32_t factors,
+                                  const double* chol, float* out) {
+  pthread_once(&zig_once, zig_init);
+  chacha8 g;
+  chacha8_seed_u64(&g, seed);
+  double z[RG_BOOK_MAX_UNIVERSE], y[RG_BOOK_MAX_UNIVERSE];
+  for (int64_t p = 0; p < paths; ++p)
+    for (int64_t t = 0; t < times; ++t) {
+      for (int f = 0; f < factors; ++f) z[f] = zig_normal(&g);
+      chol_apply(chol, factors, z, y);
+      for (int f = 0; f < factors; ++f) out[(p * times + t) * factors + f] = (float)y[f];
+    }
+}
+
+/* gbm_evolve, crates/riga-engine/src/pathcube.rs:146-187 (FP64 log-space, f32 output). */
+int32_t or_gbm_evolve(const double* s0, const double* vols, double rate, const double* q, int32_t factors,
+                      double dt, const float* block, int64_t paths, int64_t times, float* out) {
+  if (factors < 1) return fail(RG_ERR_SHAPE_MISMATCH, "s0, vols and dividend_yields must have equal length");
+  double sqrt_dt = sqrt(dt);
+  for (int64_t p = 0; p < paths; ++p)
+    for (int f = 0; f < factors; ++f) {
+      double log_s = log(s0[f]);
+      double drift = (rate - q[f] - 0.5 * vols[f] * vols[f]) * dt;
+      double diffusion = vols[f] * sqrt_dt;
+      for (int64_t i = 0; i < times; ++i) {
+        int64_t at = (p * times + i) * factors + f;
+        log_s += drift + diffusion * (double)block[at];
+        out[at] = (float)exp(log_s);
+      }
+    }
+  return RG_OK;
+}

@@ -78,6 +78,12 @@ int32_t or_run_paths(const rg_price_request* req, uint64_t first, uint64_t count
 /* Scenario batch: each scenario re-priced with the request's seed (CRN). */
 int32_t or_price_scenarios(const rg_price_request* req, const rg_scenario* sc, int32_t n,
                            int32_t threads, rg_price_result* out);
+/* --- pathcube.rs: the correlated ChaCha8 Brownian block and gbm_evolve --- */
+void or_generate_correlated_block(uint64_t seed, int64_t paths, int64_t times, int32_t factors,
+                                  const double* chol, float* out);
+int32_t or_gbm_evolve(const double* s0, const double* vols, double rate, const double* q, int32_t factors,
+                      double dt, const float* block, int64_t paths, int64_t times, float* out);
+
 /* --- books: one universe path set, many trades, a common scenario set (threads >= 1) --- */
 int32_t or_price_book(const rg_book_request* req, const rg_market_snapshot* sc, int32_t n_scen,
                       int32_t threads, rg_price_result* out /* [n_trades * S] */);

@@ -409,18 +409,26 @@ static void collect_trace(Workspace& W, const int32_t* dev_ko, uint64_t paths, u
   }
 }
 
-static void check_lane(const rg_price_request* req) {
-  if (req->config.variance_reduction == RG_VR_NONE)
-    raise(RG_ERR_UNSUPPORTED,
-          "the pseudo-random (ChaCha8) lane is one sequential stream over all paths and has no "
-          "device implementation; use variance_reduction sobol or halton");
+// The pseudo-random lane (VarianceReduction::None, note.rs:58,123-127): the slice of the ChaCha8
+// normal stream that paths [first, first + count) of the request draw, generated on the device;
+// null for the QMC lanes.  The lane always runs the FP64 kernel.
+static const double* mc_lane_normals(Workspace& W, const rg_price_request* req, uint64_t first, uint64_t count) {
+  if (req->config.variance_reduction != RG_VR_NONE) return nullptr;
+  if (!W.persistent())
+    raise(RG_ERR_UNSUPPORTED, "the pseudo-random lane needs an engine: its normal stream does not fit the static region");
+  const uint64_t per_path = (uint64_t)req->trade.steps * (uint64_t)req->market.n_assets;
+  const uint64_t n = count * per_path;
+  if (n > (uint64_t(1) << 31))
+    raise(RG_ERR_UNSUPPORTED, "the pseudo-random lane holds at most 2^31 normals per call (fewer paths or steps)");
+  double* z = static_cast<double*>(W.device(WS_MCZ, n * sizeof(double)));
+  mc_normals(req->config.seed, (req->config.first_path + first) * per_path, n, z, W);
+  return z;
 }
 
 // Prices `n_scen` scenarios (0 = the request's own market) into out[max(1, n_scen)].
 void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc, int n_scen,
                 rg_price_result* out) {
   validate_request(req);
-  check_lane(req);
   for (int i = 0; i < n_scen; ++i) {
     rg_price_request r2 = *req;
     r2.market = sc[i].market;
@@ -428,7 +436,8 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     validate_request(&r2);
   }
   const int total = n_scen ? n_scen : 1;
-  const bool fp32 = req->config.precision == RG_PRECISION_FP32;
+  const double* mcz = mc_lane_normals(W, req, 0, req->config.paths);
+  const bool fp32 = req->config.precision == RG_PRECISION_FP32 && !mcz;
   const int per_launch = fp32 ? 32 : 1;
   const uint64_t paths = req->config.paths;
   const bool trace = req->config.trace_level != RG_TRACE_OFF;
@@ -440,6 +449,7 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     W.begin_launch();
     Staged S = stage(W, req, P);
     LaunchOut lo{};
+    lo.mcz = mcz;
     int grid;
     Fp32Shape sh{};
     if (fp32) {
@@ -728,7 +738,6 @@ extern "C" int32_t rg_run_paths(rg_engine* e, const rg_price_request* req, uint6
   RG_TRY({
     if (!e || !req || (count && !out)) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
     validate_request(req);
-    check_lane(req);
     if (first > req->config.paths || count > req->config.paths - first)
       raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
     if (count == 0) return RG_OK;
@@ -738,8 +747,10 @@ extern "C" int32_t rg_run_paths(rg_engine* e, const rg_price_request* req, uint6
     prepare(req, nullptr, 0, P);
     EngineWorkspace W(e);
     Staged S = stage(W, req, P);
-    const bool fp32 = req->config.precision == RG_PRECISION_FP32;
+    const double* mcz = mc_lane_normals(W, req, first, count);
+    const bool fp32 = req->config.precision == RG_PRECISION_FP32 && !mcz;
     LaunchOut lo{};
+    lo.mcz = mcz;
     Fp32Shape sh{};
     lo.grid = fp32 ? (sh = phoenix32_shape(P, count, device_info().sm_count)).grid : phoenix64_grid(P, count);
     lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));

@@ -2,7 +2,8 @@
 //
 // One thread prices one path of one scenario in the reference's own operation order
 // (crates/riga-engine/src/note.rs:81-259): QMC normals per step, y = L·z, the depth-first
-// Brownian bridge of each factor, the multiplicative GBM/Dupire step, the Phoenix state machine
+// Brownian bridge of each factor (or, in the pseudo-random lane, the path's slice of the ChaCha8
+// normal stream and y = L·z with no bridge, note.rs:123-127), the multiplicative GBM/Dupire step, the Phoenix state machine
 // and the path close.  The bridge is streamed: an in-order traversal of the bisection tree needs
 // only the current point and a stack of right anchors, so no per-path O(T) buffer exists.  The
 // node schedule (which preorder index and standard deviation each step consumes) is a host table
@@ -38,13 +39,14 @@ __device__ __forceinline__ double lv_sigma64(const double* __restrict__ v, const
   return (1.0 - wt) * v0 + wt * v1;
 }
 
-template <int N, bool LV>
+template <int N, bool LV, bool MC>
 __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables tb,
                                                         const DevScenario* __restrict__ scen,
                                                         uint64_t path0, uint64_t npaths,
                                                         double* __restrict__ partial,
                                                         int32_t* __restrict__ ko_steps,
-                                                        rg_path_record* __restrict__ records) {
+                                                        rg_path_record* __restrict__ records,
+                                                        const double* __restrict__ mcz) {
   __shared__ double red[128][RG_ACC + 1];
   __shared__ double acc_blk[RG_ACC];
   const int tid = threadIdx.x;
@@ -83,37 +85,52 @@ __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables t
       int ko = 0, received = 0, ko_step = -1, qualified = 0, paid = 0;
       double accrual = 0.0, unpaid = 0.0, cpv = 0.0, mpv = 0.0, final_worst = 1.0;
       for (int64_t t = 0; t < T; ++t) {
-        // bridge nodes consumed at this step (note.rs:89-105 and qmc.rs:158-191)
-        const int c0 = __ldg(tb.node_off + t), c1 = __ldg(tb.node_off + t + 1);
-        for (int c = c0; c < c1; ++c) {
-          const int k = __ldg(tb.node_k + c);
-          const double cc = __ldg(tb.node_c + c);
-          double z[N], y[N];
+        double shock[N];
+        if (MC) {
+          // pseudo-random lane (note.rs:123-127): n draws of the sequential stream, then L·z
+          const double* zp = mcz + (i * (uint64_t)T + (uint64_t)t) * N;
+          double z[N];
 #pragma unroll
-          for (int f = 0; f < N; ++f) z[f] = rg_qmc_normal64(tr, tb, path, (uint64_t)k * N + f);
+          for (int f = 0; f < N; ++f) z[f] = zp[f];
 #pragma unroll
-          for (int a = 0; a < N; ++a) {  // Cholesky::apply_into (correlation.rs:196-206)
+          for (int a = 0; a < N; ++a) {
             double s = 0.0;
 #pragma unroll
             for (int b = 0; b <= a; ++b) s += L[a * N + b] * z[b];
-            y[a] = s;
+            shock[a] = s;
           }
-          if (c == 0) {
+        } else {
+          // bridge nodes consumed at this step (note.rs:89-105 and qmc.rs:158-191)
+          const int c0 = __ldg(tb.node_off + t), c1 = __ldg(tb.node_off + t + 1);
+          for (int c = c0; c < c1; ++c) {
+            const int k = __ldg(tb.node_k + c);
+            const double cc = __ldg(tb.node_c + c);
+            double z[N], y[N];
 #pragma unroll
-            for (int f = 0; f < N; ++f) stk[sp][f] = y[f] * cc;
-          } else {
+            for (int f = 0; f < N; ++f) z[f] = rg_qmc_normal64(tr, tb, path, (uint64_t)k * N + f);
 #pragma unroll
-            for (int f = 0; f < N; ++f) stk[sp][f] = 0.5 * (wcur[f] + stk[sp - 1][f]) + y[f] * cc;
+            for (int a = 0; a < N; ++a) {  // Cholesky::apply_into (correlation.rs:196-206)
+              double s = 0.0;
+#pragma unroll
+              for (int b = 0; b <= a; ++b) s += L[a * N + b] * z[b];
+              y[a] = s;
+            }
+            if (c == 0) {
+#pragma unroll
+              for (int f = 0; f < N; ++f) stk[sp][f] = y[f] * cc;
+            } else {
+#pragma unroll
+              for (int f = 0; f < N; ++f) stk[sp][f] = 0.5 * (wcur[f] + stk[sp - 1][f]) + y[f] * cc;
+            }
+            ++sp;
           }
-          ++sp;
-        }
-        --sp;
-        double shock[N];
+          --sp;
 #pragma unroll
-        for (int f = 0; f < N; ++f) {
-          double wn = stk[sp][f];
-          shock[f] = (wn - wcur[f]) * inv_sqrt_dt;
-          wcur[f] = wn;
+          for (int f = 0; f < N; ++f) {
+            double wn = stk[sp][f];
+            shock[f] = (wn - wcur[f]) * inv_sqrt_dt;
+            wcur[f] = wn;
+          }
         }
         // GBM / Dupire step (note.rs:133-142)
         int2 tix[N];
@@ -212,7 +229,7 @@ __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables t
         rg_path_record r;
         r.path_id = path;
         r.rng_seed = tr.seed;
-        r.sobol_index = path + 1;
+        r.sobol_index = MC ? 0 : path + 1;
         r.worst_final = final_worst;
         r.knocked_out = ko;
         r.ko_step = ko_step;
@@ -253,8 +270,12 @@ int phoenix64_grid(const Prepared& P, uint64_t npaths) {
 template <int N, bool LV>
 static void launch_n(const Prepared& P, const DevTables& tb, const DevScenario* scen, uint64_t path0,
                      uint64_t npaths, const LaunchOut& out, cudaStream_t s) {
-  phoenix64_kernel<N, LV><<<out.grid, 128, 0, s>>>(P.trade, tb, scen, path0, npaths, out.partial,
-                                                   out.ko_steps, out.records);
+  if (out.mcz)
+    phoenix64_kernel<N, LV, true><<<out.grid, 128, 0, s>>>(P.trade, tb, scen, path0, npaths, out.partial,
+                                                           out.ko_steps, out.records, out.mcz);
+  else
+    phoenix64_kernel<N, LV, false><<<out.grid, 128, 0, s>>>(P.trade, tb, scen, path0, npaths, out.partial,
+                                                            out.ko_steps, out.records, nullptr);
 }
 
 void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario* scen,

@@ -119,7 +119,11 @@ struct Engine;
 
 // The device and host memory one pricing call draws on: the engine's growable buffers, or a fixed
 // region.  Slots are requested in this order within each fused launch.
-enum WsSlot { WS_ARENA = 0, WS_CALIB, WS_LVROWS, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS, WS_NSLOTS };
+enum WsSlot {
+  WS_ARENA = 0, WS_CALIB, WS_LVROWS, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS,
+  WS_MCZ, WS_MCKEYS, WS_MCAUX,  // the pseudo-random lane's normals, keystream and parse tables
+  WS_NSLOTS
+};
 struct Workspace {
   cudaStream_t stream = nullptr;
   cudaEvent_t* ev = nullptr;    // six events for the timing breakdown, or null
@@ -128,6 +132,8 @@ struct Workspace {
   virtual void begin_launch() {}
   virtual void* device(int slot, size_t bytes) = 0;
   virtual void* host(size_t bytes) = 0;  // landing area of the FP64 sums
+  // whether slots keep their contents across fused launches (false for a bump allocator)
+  virtual bool persistent() const { return true; }
   virtual ~Workspace() = default;
 };
 // validate → host tables → H2D → prologue → fused kernel → reduce → D2H → PriceResults
@@ -172,7 +178,10 @@ struct LaunchOut {
   int32_t* ko_steps;    // [npaths] (scenario 0) or null
   rg_path_record* records;  // [npaths] or null
   int grid;
+  const double* mcz = nullptr;  // pseudo-random lane: normals [npaths][T][n] of the launch's paths
 };
+// StandardNormal draws [first, first + count) of ChaCha8Rng::seed_from_u64(seed) into d_out.
+void mc_normals(uint64_t seed, uint64_t first, uint64_t count, double* d_out, Workspace& W);
 int phoenix64_grid(const Prepared& P, uint64_t npaths);
 void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
                       uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);

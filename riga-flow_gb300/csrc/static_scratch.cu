@@ -35,6 +35,7 @@ struct StaticWorkspace : rg::Workspace {
   size_t cap = 0, off = 0;
   double sums[RG_MAX_SCEN * RG_ACC];
   void begin_launch() override { off = 0; }
+  bool persistent() const override { return false; }
   void* device(int slot, size_t bytes) override {
     (void)slot;
     const size_t o = (off + 255) & ~(size_t)255;

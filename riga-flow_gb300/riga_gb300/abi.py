@@ -349,6 +349,10 @@ SIGNATURES = {
     "rg_server_cancel": (_i32, [_vp, _u64]),
     "rg_server_release": (_i32, [_vp, _u64]),
     "rg_server_get_stats": (_i32, [_vp, C.POINTER(ServerStats)]),
+    "rg_chacha8_normals": (_i32, [_u64, _u64, _u64, C.POINTER(C.c_double)]),
+    "rg_generate_correlated_block": (_i32, [_u64, _i64, _i64, _i32, C.POINTER(C.c_double), _fp]),
+    "rg_gbm_evolve": (_i32, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double),
+                             _i32, C.c_double, _fp, _i64, _i64, _fp]),
     "rg_sobol_directions": (_i32, [_i64, C.POINTER(C.c_uint32)]),
     "rg_bridge_schedule": (_i32, [_i64, C.c_double, C.POINTER(_i32), C.POINTER(_i32),
                                   C.POINTER(C.c_double), C.POINTER(_i32)]),

@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
-NO_FMA = {"phoenix64.cu", "prologue.cu", "book64.cu"}
+NO_FMA = {"phoenix64.cu", "prologue.cu", "book64.cu", "mclane.cu"}
 
 
 def nvcc() -> str:

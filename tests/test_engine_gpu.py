@@ -272,7 +272,6 @@ def test_invalid_requests_keep_the_reference_error_codes(engine, termsheet1):
     assert code(lambda r: setattr(r.config, "paths", 0)) == "invalid_paths"
     assert code(lambda r: setattr(r.trade, "steps", 0)) == "invalid_schedule"
     assert code(lambda r: setattr(r.market, "spots", [1.0])) == "invalid_market_shape"
-    assert code(lambda r: None, kind="none") == "unsupported"
     with pytest.raises(abi.RigaError) as e:
         engine.run_paths_raw(_termsheet(termsheet1, 64), 60, 10)
     assert e.value.code == "path_out_of_range"

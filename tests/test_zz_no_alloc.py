@@ -58,3 +58,14 @@ def test_static_entry_point_rejects_requests_beyond_its_region():
     status = lib.rg_price_put_leg_static(a.ptr, C.byref(out))
     assert abi.STATUS_CODES[status] == "invalid_argument"
     assert "16 MiB" in abi.last_error(lib)
+
+
+def test_static_entry_point_declines_the_pseudo_random_lane(termsheet1):
+    """The ChaCha8 lane's normal stream lives in engine buffers, not in the static region."""
+    build_library()
+    lib = abi.load_library()
+    req = termsheet1.request
+    a = req.to_abi()
+    out = abi.PriceResult()
+    status = lib.rg_price_put_leg_static(a.ptr, C.byref(out))
+    assert lib.rg_status_code(status).decode() == "unsupported"
