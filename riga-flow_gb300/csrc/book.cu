@@ -9,6 +9,8 @@
 //   buffers, then the scan of every (trade, scenario) on S0; chunk k+1 generates while chunk k is
 //   scanned → fixed-order reduce over path blocks → one D2H copy → PriceResults.
 // FP64 parity mode runs the same pipeline with the FP64 kernels and no overlap.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 
@@ -37,6 +39,7 @@ struct BookPlan {
   std::vector<BookPair32> pair32;
   std::vector<double> df, dfm;
   std::vector<int32_t> order;
+  int group_lo[RG_NMAX], group_n[RG_NMAX];
 };
 
 void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen) {
@@ -215,11 +218,18 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
         p.sig[f] = (float)v;
       }
     }
-  // work order: longest trades first
+  // work order: grouped by underlying count (one launch each), longest trades first in a group
   B.order.resize(B.n_trades);
   for (int j = 0; j < B.n_trades; ++j) B.order[j] = j;
-  std::stable_sort(B.order.begin(), B.order.end(),
-                   [&](int a, int b) { return B.trades[a].T * 8 + B.trades[a].n > B.trades[b].T * 8 + B.trades[b].n; });
+  std::stable_sort(B.order.begin(), B.order.end(), [&](int a, int b) {
+    if (B.trades[a].n != B.trades[b].n) return B.trades[a].n < B.trades[b].n;
+    return B.trades[a].T > B.trades[b].T;
+  });
+  for (int n = 0; n < RG_NMAX; ++n) B.group_lo[n] = B.group_n[n] = 0;
+  for (int i = 0; i < B.n_trades; ++i) {
+    const int n = B.trades[B.order[i]].n;
+    if (B.group_n[n - 1]++ == 0) B.group_lo[n - 1] = i;
+  }
 }
 
 struct BookStaged {
@@ -287,6 +297,29 @@ BookStaged stage_book(rg_engine* E, const rg_book_request* r, BookPlan& B) {
   return st;
 }
 
+// The tensor map of one chunk's FP32 increments, viewed as [TU][U][npaths] with rows of `rowlen`
+// floats: boxes of Pb paths × 1 asset × TT steps (zero-filled past npaths and TU).
+CUtensorMap increments_map(const float* incr, uint64_t npaths, uint64_t rowlen, int U, int64_t TU, int Pb, int TT) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cuda_check(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
+               "cuTensorMapEncodeTiled entry point");
+    if (!fn || q != cudaDriverEntryPointSuccess) raise(RG_ERR_GPU_ERROR, "cuTensorMapEncodeTiled unavailable");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  CUtensorMap map;
+  const cuuint64_t dims[3] = {npaths, (cuuint64_t)U, (cuuint64_t)TU};
+  const cuuint64_t strides[2] = {rowlen * 4, (cuuint64_t)U * rowlen * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)Pb, 1, (cuuint32_t)TT};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(incr), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) raise(RG_ERR_GPU_ERROR, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return map;
+}
+
 // Paths per generation chunk: a multiple of `unit` whose increments fit the budget.
 uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t unit) {
   const uint64_t per_path = (uint64_t)U * (uint64_t)TU * elem;
@@ -337,7 +370,8 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
     const uint64_t n_chunks = (P + PC - 1) / PC;
     const uint64_t blocks_per_chunk = (PC + sh.blk_paths - 1) / sh.blk_paths;
     const uint64_t total_blocks = (P + sh.blk_paths - 1) / sh.blk_paths;
-    const size_t incr_bytes = sizeof(float) * (size_t)B.U * (size_t)B.TU * (size_t)PC;
+    const uint64_t rowlen_max = (PC + 63) / 64 * 64;  // rows padded for 16-byte tensor-map strides
+    const size_t incr_bytes = sizeof(float) * (size_t)B.U * (size_t)B.TU * (size_t)rowlen_max;
     float* incr[2] = {static_cast<float*>(book_buf(E, BK_INCR0, incr_bytes)),
                       static_cast<float*>(book_buf(E, BK_INCR1, n_chunks > 1 ? incr_bytes : 256))};
     double* partial = static_cast<double*>(book_buf(E, BK_PARTIAL, sizeof(double) * total_blocks * pairs * RG_ACC));
@@ -354,10 +388,12 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
         // buffer reuse: the scan of chunk c-2 must be done with it
         cuda_check(cudaStreamWaitEvent(s1, E->book_ev[2 + (c & 1)], 0), "stream wait");
       }
-      launch_book_gen32(B.gen, st.tb, st.L32, B.U, path_base + p0, np, buf, s1);
+      const uint64_t rowlen = (np + 63) / 64 * 64;
+      launch_book_gen32(B.gen, st.tb, st.L32, B.U, path_base + p0, np, rowlen, buf, s1);
       cuda_check(cudaEventRecord(E->book_ev[1], s1), "event");
       cuda_check(cudaStreamWaitEvent(s0, E->book_ev[1], 0), "stream wait");
-      launch_book_trade32(st.bk, sh, buf, np, c * blocks_per_chunk, partial, scratch, status, s0);
+      const CUtensorMap tmap = increments_map(buf, np, rowlen, B.U, B.TU, sh.Pb, sh.TT);
+      launch_book_trade32(st.bk, sh, tmap, np, c * blocks_per_chunk, B.group_lo, B.group_n, partial, scratch, status, s0);
       cuda_check(cudaEventRecord(E->book_ev[2 + (c & 1)], s0), "event");
     }
     double* dsums = static_cast<double*>(book_buf(E, BK_SUMS, sizeof(double) * pairs * RG_ACC));
@@ -367,6 +403,7 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
     cuda_check(cudaMemcpyAsync(hs.data(), dsums, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, s0), "D2H");
     cuda_check(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, s0), "D2H");
     cuda_check(cudaStreamSynchronize(s0), "book pricing");
+    if (hstat == KSTAT_TIMEOUT) raise(RG_ERR_TIMEOUT, "book_trade32_kernel: a bounded stage wait ran out");
     if (hstat) raise(RG_ERR_GPU_ERROR, "book_trade32_kernel reported a bad work item");
     for (size_t k = 0; k < hs.size(); ++k)
       if (!std::isfinite(hs[k])) raise(RG_ERR_GPU_ERROR, "book: non-finite path sums");

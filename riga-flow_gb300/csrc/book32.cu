@@ -11,19 +11,23 @@
 // book_trade32_kernel: persistent.  Work items are (path block, trade), taken from an atomic
 // counter in path-block-major order with trades longest first, so the CTAs in flight read the
 // same block of increments (L2-resident) and the tail is short.  A CTA is Sb scenario slots × Pb
-// paths (a warp is 32 paths of one scenario); thread (s, p) steps the trade's assets in log space
-// — x_f += σ_f·ΔW + (r - q_f - σ_f²/2)·dt, reading ΔW of its assets with coalesced loads that
-// the Sb scenario warps share through L1 — and runs the Phoenix state machine of note.rs:
-// 150-218 with the period schedule advanced incrementally.  Per path the payoff values are FP32;
+// paths (a warp is 32 paths of one scenario); the increments each (path tile, time tile) stage
+// needs are staged in shared memory by TMA, double-buffered on mbarriers, and thread (s, p) steps
+// the trade's assets in log space — x_f += σ_f·ΔW + (r - q_f - σ_f²/2)·dt — from shared memory
+// and runs the Phoenix state machine of note.rs:150-218 with the period schedule advanced
+// incrementally.  Per path the payoff values are FP32;
 // a warp's 32 paths are summed by a fixed butterfly and every sum above that is FP64 in a fixed
 // order, so an item's sums do not depend on which CTA ran it.
+#include <algorithm>
+#include <mutex>
+
 #include "rg_internal.h"
 
 namespace rg {
 
 __global__ void __launch_bounds__(1024) book_gen32_kernel(DevTrade gen, DevTables tb,
                                                           const float* __restrict__ L32, int U,
-                                                          uint64_t path0, uint64_t npaths,
+                                                          uint64_t path0, uint64_t npaths, uint64_t rowlen,
                                                           float* __restrict__ incr) {
   __shared__ float zs[2][RG_BOOK_MAX_UNIVERSE][33];
   const int lane = threadIdx.x, u = threadIdx.y;
@@ -53,82 +57,140 @@ __global__ void __launch_bounds__(1024) book_gen32_kernel(DevTrade gen, DevTable
     }
     --sp;
     const float wn = stk[sp];
-    if (ok) incr[((uint64_t)t * U + u) * npaths + p] = wn - wcur;
+    if (ok) incr[((uint64_t)t * U + u) * rowlen + p] = wn - wcur;
     wcur = wn;
   }
 }
 
 void launch_book_gen32(const DevTrade& gen, const DevTables& tb, const float* L32, int U,
-                       uint64_t path0, uint64_t npaths, float* incr, cudaStream_t s) {
+                       uint64_t path0, uint64_t npaths, uint64_t rowlen, float* incr, cudaStream_t s) {
   const unsigned blocks = (unsigned)((npaths + 31) / 32);
-  book_gen32_kernel<<<blocks, dim3(32, U), 0, s>>>(gen, tb, L32, U, path0, npaths, incr);
+  book_gen32_kernel<<<blocks, dim3(32, U), 0, s>>>(gen, tb, L32, U, path0, npaths, rowlen, incr);
   cuda_check(cudaGetLastError(), "book_gen32_kernel launch");
 }
 
-// One (trade, block) item for N underlyings: steps every tile of Pb paths of the block and adds
-// the tiles' FP32 warp sums into `acc` (lane k holds slot k of this warp's FP64 sums).
+// ------------------------------------------------------------------ TMA-staged scan ----------
+// The increments a (trade, path tile) stage needs — for each of the trade's N underlyings, TT
+// steps × Pb paths — are one 3-D tensor-map box each (paths innermost).  One elected thread
+// issues the next stage's boxes into the other shared-memory buffer (cp.async.bulk.tensor,
+// completion counted on that buffer's "full" mbarrier) while every warp consumes the current
+// buffer, and each warp releases a buffer on its "empty" mbarrier when it is done with it.
+// Every wait is bounded: a wait that runs out sets the status word and the kernel returns.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of `bar` with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+  for (uint32_t it = 0; it < (1u << 24); ++it)
+    if (mbar_test(bar, parity)) return true;
+  atomicExch(status, KSTAT_TIMEOUT);
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+struct BookStage {
+  int tile, k;  // path tile within the item, time tile within the trade
+};
+
 template <int N>
-__device__ __forceinline__ void book_scan32(const BookDev& bk, const BookTradeDev& tr, int j, int s,
-                                            bool lane_ok, int pl, int Pb, const float* __restrict__ incr,
-                                            uint64_t npaths, uint64_t p_lo, uint64_t p_hi, double& acc) {
+__device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTradeDev& tr, int j, int s, bool lane_ok,
+                                                int pl, int Pb, int TT, uint64_t p_lo, uint64_t p_hi,
+                                                const CUtensorMap* tmap, float* bufs, uint64_t* full,
+                                                uint64_t* empty, uint32_t& G, int* status, double& acc) {
   const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x;
   const int ss = lane_ok ? s : 0;
   const BookPair32 pc = bk.pair32[(size_t)j * bk.S + ss];
   float drift[N], sig[N];
-  uint32_t off[N];  // asset rows within a step: idx·npaths < 2^32 for every chunk the budget allows
 #pragma unroll
   for (int f = 0; f < N; ++f) {
     drift[f] = pc.drift[f];
     sig[f] = pc.sig[f];
-    off[f] = (uint32_t)tr.idx[f] * (uint32_t)npaths;
   }
-  const uint64_t step_stride = (uint64_t)bk.U * npaths;
   const double* df = bk.df + (size_t)ss * bk.TU;
-  const double dfm_d = bk.dfm[(size_t)j * bk.S + ss];
-  const float dfm = (float)dfm_d;
+  const float dfm = (float)bk.dfm[(size_t)j * bk.S + ss];
   const int T = tr.T, PER = tr.periods;
-  for (uint64_t p0 = p_lo; p0 < p_hi; p0 += Pb) {
-    const uint64_t p = p0 + pl;
-    const bool ok = lane_ok && p < p_hi;
-    const float* base = incr + (ok ? p : p_lo);
-    float x[N];
+  const int ntiles = (int)((p_hi - p_lo + Pb - 1) / Pb);
+  const int ntt = (T + TT - 1) / TT;
+  const int nst = ntiles * ntt;
+  const uint32_t stage_floats = (uint32_t)(5 * TT * Pb);
+  const uint32_t bytes = (uint32_t)(N * TT * Pb * 4);
+  // the producer: stage st of this item into buffer g & 1 (the (g >> 1)-th use of that buffer)
+  auto produce = [&](uint32_t g, int st) -> bool {
+    const uint32_t b = g & 1u, u = g >> 1;
+    if (u >= 1 && !mbar_wait(&empty[b], (u - 1) & 1u, status)) return false;
+    const int tile = st / ntt, k = st % ntt;
+    mbar_expect_tx(&full[b], bytes);
+    float* dst = bufs + b * stage_floats;
 #pragma unroll
-    for (int f = 0; f < N; ++f) x[f] = pc.x0[f];
-    bool alive = true, received = false;
-    int qual = 0, unpaid = 0, ko_step = -1;
-    float cpv = 0.0f, mpv = 0.0f, worst = 0.0f;
-    // period schedule (note.rs:150-218): current period, its last step, its accrual increment
-    // the last step of period 0: the largest s with min(s·PER/T, PER-1) == 0
-    int per = 0;
-    int pend = PER > 1 ? (int)(((int64_t)T + PER - 1) / PER) - 1 : T - 1;
-    auto accr = [&](int q) {
-      const int64_t a = (int64_t)T * (q + 1) / PER, b = (int64_t)T * q / PER;
-      int64_t ps = a > b ? a - b : 0;
-      if (ps < 1) ps = 1;
-      return (float)(tr.coupon_rate / (double)ps);
-    };
-    float inc = accr(0);
-    bool fixed = tr.fixed_first != 0;
-    // ΔW of the next step is loaded one step ahead when registers allow (N <= 3)
-    constexpr bool kAhead = N <= 3;
-    float y[N];
+    for (int f = 0; f < N; ++f)
+      tma_load_3d(dst + f * TT * Pb, tmap, &full[b], (int)(p_lo + (uint64_t)tile * Pb), tr.idx[f], k * TT);
+    return true;
+  };
+  if (tid == 0 && !produce(G, 0)) return false;
+  float x[N];
+  bool alive = true, received = false, ok = false;
+  int qual = 0, unpaid = 0, ko_step = -1, per = 0, pend = 0;
+  float cpv = 0.0f, mpv = 0.0f, worst = 0.0f, inc = 0.0f;
+  bool fixed = false;
+  auto accr = [&](int q) {
+    const int64_t a = (int64_t)T * (q + 1) / PER, b = (int64_t)T * q / PER;
+    int64_t ps = a > b ? a - b : 0;
+    if (ps < 1) ps = 1;
+    return (float)(tr.coupon_rate / (double)ps);
+  };
+  for (int st = 0; st < nst; ++st, ++G) {
+    const int tile = st / ntt, k = st % ntt;
+    if (tid == 0 && st + 1 < nst && !produce(G + 1, st + 1)) return false;
+    if (k == 0) {
+      // a new path tile: fresh path state
+      ok = lane_ok && p_lo + (uint64_t)tile * Pb + pl < p_hi;
 #pragma unroll
-    for (int f = 0; f < N; ++f) y[f] = kAhead ? __ldg(base + off[f]) : 0.0f;
-    for (int t = 0; t < T; ++t) {
-      float yn[N];
-      if (kAhead) {
-        const float* nb = base + (uint64_t)(t + 1 < T ? t + 1 : t) * step_stride;
-#pragma unroll
-        for (int f = 0; f < N; ++f) yn[f] = __ldg(nb + off[f]);
-      } else {
-        const float* cb = base + (uint64_t)t * step_stride;
-#pragma unroll
-        for (int f = 0; f < N; ++f) y[f] = __ldg(cb + off[f]);
-      }
+      for (int f = 0; f < N; ++f) x[f] = pc.x0[f];
+      alive = true;
+      received = false;
+      qual = unpaid = 0;
+      ko_step = -1;
+      cpv = mpv = worst = 0.0f;
+      per = 0;
+      pend = PER > 1 ? (int)(((int64_t)T + PER - 1) / PER) - 1 : T - 1;
+      inc = accr(0);
+      fixed = tr.fixed_first != 0;
+    }
+    const uint32_t b = G & 1u;
+    if (!mbar_wait(&full[b], (G >> 1) & 1u, status)) return false;
+    const float* buf = bufs + b * stage_floats;
+    const int t0 = k * TT, tn = min(TT, T - t0);
+    for (int tt = 0; tt < tn; ++tt) {
+      const int t = t0 + tt;
       float wmin = INFINITY;
 #pragma unroll
       for (int f = 0; f < N; ++f) {
-        x[f] = fmaf(sig[f], y[f], x[f]) + drift[f];
+        x[f] = fmaf(sig[f], buf[(f * TT + tt) * Pb + pl], x[f]) + drift[f];
         wmin = fminf(wmin, x[f]);
       }
       worst = wmin;
@@ -159,7 +221,6 @@ __device__ __forceinline__ void book_scan32(const BookDev& bk, const BookTradeDe
         }
       }
       if (t == pend && t + 1 < T) {
-        // the next step opens period min((t+1)·PER/T, PER-1); find where it ends
         int64_t q = (int64_t)(t + 1) * PER / T;
         if (q > PER - 1) q = PER - 1;
         per = (int)q;
@@ -168,86 +229,102 @@ __device__ __forceinline__ void book_scan32(const BookDev& bk, const BookTradeDe
         fixed = false;
         qual = 0;
       }
-      if (kAhead) {
-#pragma unroll
-        for (int f = 0; f < N; ++f) y[f] = yn[f];
-      }
     }
-    // path close (note.rs:221-258) in FP32; each accumulator slot is formed, summed over the
-    // warp's 32 paths by a fixed butterfly and kept by lane k, one slot at a time
-    const bool ko = ko_step >= 0;
-    const float funding = ok ? (ko ? (float)__ldg(df + ko_step) : dfm) : 0.0f;
-    const bool hit_ki = ok && worst <= tr.ln_ki;
-    const bool put_ok = hit_ki && !ko;
-    const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * dfm : 0.0f;
-    const float cn = cpv + mpv;
-    const float pv1 = ok ? (funding - 1.0f) + cn - put : 0.0f;
-    const bool kof = ok && ko, rec = ok && received;
-    float mine = 0.0f;
+    // this warp is done with the buffer
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+    if (k == ntt - 1) {
+      // path close (note.rs:221-258) in FP32; each slot summed over the warp's 32 paths by a
+      // fixed butterfly and kept by lane k
+      const bool ko = ko_step >= 0;
+      const float funding = ok ? (ko ? (float)__ldg(df + ko_step) : dfm) : 0.0f;
+      const bool hit_ki = ok && worst <= tr.ln_ki;
+      const bool put_ok = hit_ki && !ko;
+      const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * dfm : 0.0f;
+      const float cn = cpv + mpv;
+      const float pv1 = ok ? (funding - 1.0f) + cn - put : 0.0f;
+      const bool kof = ok && ko, rec = ok && received;
+      float mine = 0.0f;
 #pragma unroll
-    for (int k = 0; k < RG_ACC; ++k) {
-      float v;
-      switch (k) {
-        case ACC_PV: v = pv1; break;
-        case ACC_PV2: v = pv1 * pv1; break;
-        case ACC_KOF: v = kof ? funding - 1.0f : 0.0f; break;
-        case ACC_KOF2: v = kof ? (funding - 1.0f) * (funding - 1.0f) : 0.0f; break;
-        case ACC_KIPUT: v = hit_ki ? put : 0.0f; break;
-        case ACC_KIPUT2: v = hit_ki ? put * put : 0.0f; break;
-        case ACC_CPN: v = rec ? cn : 0.0f; break;
-        case ACC_CPN2: v = rec ? cn * cn : 0.0f; break;
-        case ACC_PUT: v = put; break;
-        case ACC_FUND: v = funding; break;
-        case ACC_CQ: v = ok ? cpv * 10.0f : 0.0f; break;
-        case ACC_MQ: v = ok ? mpv * 10.0f : 0.0f; break;
-        case ACC_NKO: v = kof ? 1.0f : 0.0f; break;
-        case ACC_NKI: v = hit_ki ? 1.0f : 0.0f; break;
-        case ACC_NPUT: v = put_ok ? 1.0f : 0.0f; break;
-        default: v = rec ? 1.0f : 0.0f; break;  // ACC_NCPN
+      for (int kk = 0; kk < RG_ACC; ++kk) {
+        float v;
+        switch (kk) {
+          case ACC_PV: v = pv1; break;
+          case ACC_PV2: v = pv1 * pv1; break;
+          case ACC_KOF: v = kof ? funding - 1.0f : 0.0f; break;
+          case ACC_KOF2: v = kof ? (funding - 1.0f) * (funding - 1.0f) : 0.0f; break;
+          case ACC_KIPUT: v = hit_ki ? put : 0.0f; break;
+          case ACC_KIPUT2: v = hit_ki ? put * put : 0.0f; break;
+          case ACC_CPN: v = rec ? cn : 0.0f; break;
+          case ACC_CPN2: v = rec ? cn * cn : 0.0f; break;
+          case ACC_PUT: v = put; break;
+          case ACC_FUND: v = funding; break;
+          case ACC_CQ: v = ok ? cpv * 10.0f : 0.0f; break;
+          case ACC_MQ: v = ok ? mpv * 10.0f : 0.0f; break;
+          case ACC_NKO: v = kof ? 1.0f : 0.0f; break;
+          case ACC_NKI: v = hit_ki ? 1.0f : 0.0f; break;
+          case ACC_NPUT: v = put_ok ? 1.0f : 0.0f; break;
+          default: v = rec ? 1.0f : 0.0f; break;  // ACC_NCPN
+        }
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
+        if (lane == kk) mine = v;
       }
-#pragma unroll
-      for (int w = 16; w > 0; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
-      if (lane == k) mine = v;
+      acc += (double)mine;
     }
-    acc += (double)mine;
   }
+  return true;
 }
 
-__global__ void __launch_bounds__(1024, 1) book_trade32_kernel(BookDev bk, const float* __restrict__ incr,
+// One persistent launch per underlying count N over that group of trades (order[g_lo, g_lo + ng)),
+// so each instantiation gets the registers its N needs.
+template <int N>
+__global__ void __launch_bounds__(1024, 1) book_trade32_kernel(const __grid_constant__ CUtensorMap tmap, BookDev bk,
                                                                uint64_t npaths, uint64_t block0, int blk_paths,
-                                                               int Pb, double* __restrict__ partial,
-                                                               int32_t* __restrict__ counter,
-                                                               int* __restrict__ status) {
+                                                               int Pb, int TT, int g_lo, int ng,
+                                                               double* __restrict__ partial,
+                                                               int32_t* __restrict__ counter, int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ double s_red[32][RG_ACC];
+  float* bufs = reinterpret_cast<float*>(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + (size_t)2 * 5 * TT * Pb * 4);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + 2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
   const int s = tid / Pb, pl = tid % Pb;
   const bool lane_ok = s < bk.S;
   const int warps_per_scen = Pb / 32;
   const int64_t nblk = (int64_t)((npaths + blk_paths - 1) / blk_paths);
-  const int64_t n_items = nblk * bk.n_trades;
+  const int64_t n_items = nblk * ng;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], (uint32_t)nwarps);
+    mbar_init(&empty[1], (uint32_t)nwarps);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t G = 0;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(counter, 1);
     __syncthreads();
     const int64_t item = s_item;
     __syncthreads();
-    if (item >= n_items) break;
-    const int64_t b = item / bk.n_trades;
-    const int j = bk.order[item % bk.n_trades];
+    if (item >= n_items || *(volatile int*)status != 0) break;
+    const int64_t b = item / ng;
+    const int j = bk.order[g_lo + item % ng];
     const BookTradeDev& tr = bk.trades[j];
+    if (tr.n != N) {
+      if (tid == 0) atomicExch(status, KSTAT_BAD_LAUNCH);
+      return;
+    }
     const uint64_t p_lo = (uint64_t)b * blk_paths;
     const uint64_t p_hi = p_lo + blk_paths < npaths ? p_lo + blk_paths : npaths;
     double acc = 0.0;
-    switch (tr.n) {
-      case 1: book_scan32<1>(bk, tr, j, s, lane_ok, pl, Pb, incr, npaths, p_lo, p_hi, acc); break;
-      case 2: book_scan32<2>(bk, tr, j, s, lane_ok, pl, Pb, incr, npaths, p_lo, p_hi, acc); break;
-      case 3: book_scan32<3>(bk, tr, j, s, lane_ok, pl, Pb, incr, npaths, p_lo, p_hi, acc); break;
-      case 4: book_scan32<4>(bk, tr, j, s, lane_ok, pl, Pb, incr, npaths, p_lo, p_hi, acc); break;
-      case 5: book_scan32<5>(bk, tr, j, s, lane_ok, pl, Pb, incr, npaths, p_lo, p_hi, acc); break;
-      default:
-        if (tid == 0) atomicExch(status, KSTAT_BAD_LAUNCH);
-        break;
-    }
+    if (!book_scan32_tma<N>(bk, tr, j, s, lane_ok, pl, Pb, TT, p_lo, p_hi, &tmap, bufs, full, empty, G, status, acc))
+      return;  // a bounded wait ran out (status set): nothing more is issued
     // the scenario's warps in index order
     if (lane < RG_ACC) s_red[warp][lane] = acc;
     __syncthreads();
@@ -268,17 +345,53 @@ Book32Shape book32_shape(int S, int sm_count) {
   sh.Sb = sb;
   sh.threads = sb >= 8 ? 1024 : 256;
   sh.Pb = sh.threads / sb;
+  sh.TT = std::min(32, 4096 / sh.Pb);
   sh.grid = sm_count * (sh.threads == 1024 ? 1 : 4);
   sh.blk_paths = sh.Pb * 32;
+  sh.smem = 2 * 5 * sh.TT * sh.Pb * 4 + 64;
   return sh;
 }
 
-void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const float* incr, uint64_t npaths,
-                         uint64_t block0, double* partial, int32_t* counter, int* status, cudaStream_t s) {
+template <int N>
+static void launch_group(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
+                         uint64_t block0, int g_lo, int ng, double* partial, int32_t* counter, int* status,
+                         cudaStream_t s) {
+  // process-wide attribute, raised once per device to cover every shape's stage buffers
+  {
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (!done[dev]) {
+      cuda_check(cudaFuncSetAttribute(book_trade32_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      176 * 1024),
+                 "book smem attribute");
+      done[dev] = 1;
+    }
+  }
   cuda_check(cudaMemsetAsync(counter, 0, sizeof(int32_t), s), "book counter reset");
-  book_trade32_kernel<<<sh.grid, sh.threads, 0, s>>>(bk, incr, npaths, block0, sh.blk_paths, sh.Pb,
-                                                     partial, counter, status);
+  book_trade32_kernel<N><<<sh.grid, sh.threads, sh.smem, s>>>(tmap, bk, npaths, block0, sh.blk_paths, sh.Pb, sh.TT,
+                                                              g_lo, ng, partial, counter, status);
   cuda_check(cudaGetLastError(), "book_trade32_kernel launch");
+}
+
+void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
+                         uint64_t block0, const int* group_lo, const int* group_n, double* partial,
+                         int32_t* counter, int* status, cudaStream_t s) {
+  if (sh.smem > 176 * 1024) raise(RG_ERR_GPU_ERROR, "book stage buffers exceed the shared-memory limit");
+  for (int n = 1; n <= RG_NMAX; ++n) {
+    const int lo = group_lo[n - 1], ng = group_n[n - 1];
+    if (ng == 0) continue;
+    switch (n) {
+      case 1: launch_group<1>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
+      case 2: launch_group<2>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
+      case 3: launch_group<3>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
+      case 4: launch_group<4>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
+      default: launch_group<5>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
+    }
+  }
 }
 
 __global__ void book_l32_kernel(const double* __restrict__ L, int n, float* __restrict__ L32) {

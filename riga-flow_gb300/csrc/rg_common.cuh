@@ -156,26 +156,26 @@ __device__ __forceinline__ double rg_probit64(double p) {
   }
 }
 
-// The same approximation in FP32, taking the 32-bit scrambled integer x (u = (x + 1/2) / 2^32).
-// The branch is decided on x against integer thresholds computed in FP64 on the host, so every
-// coordinate takes the same branch as the FP64 reference.  Tail probabilities are formed from x
-// or ~x so that no 1 - u cancellation occurs.
-__device__ __forceinline__ float rg_probit32(uint32_t x, uint32_t x_lo, uint32_t x_hi) {
+// Acklam's approximation in FP32 on the 32-bit scrambled integer x (u = (x + 1/2) / 2^32), split
+// into its branches.  Central branch (x_lo <= x <= x_hi): q = u - 1/2 formed exactly from x.
+__device__ __forceinline__ float rg_probit32_central(uint32_t x) {
   const float a0 = -3.969683028665376e1f, a1 = 2.209460984245205e2f, a2 = -2.759285104469687e2f,
               a3 = 1.383577518672690e2f, a4 = -3.066479806614716e1f, a5 = 2.506628277459239e0f;
   const float b0 = -5.447609879822406e1f, b1 = 1.615858368580409e2f, b2 = -1.556989798598866e2f,
               b3 = 6.680131188771972e1f, b4 = -1.328068155288572e1f;
+  float q = fmaf((float)(int32_t)(x ^ 0x80000000u), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+  float r = q * q;
+  float num = fmaf(fmaf(fmaf(fmaf(fmaf(a0, r, a1), r, a2), r, a3), r, a4), r, a5) * q;
+  float den = fmaf(fmaf(fmaf(fmaf(fmaf(b0, r, b1), r, b2), r, b3), r, b4), r, 1.0f);
+  return __fdividef(num, den);
+}
+
+// Tail branches (x < x_lo or x > x_hi): the tail probability from x or ~x, no 1 - u cancellation.
+__device__ __forceinline__ float rg_probit32_tail(uint32_t x, uint32_t x_lo) {
   const float c0 = -7.784894002430293e-3f, c1 = -3.223964580411365e-1f, c2 = -2.400758277161838e0f,
               c3 = -2.549732539343734e0f, c4 = 4.374664141464968e0f, c5 = 2.938163982698783e0f;
   const float d0 = 7.784695709041462e-3f, d1 = 3.224671290700398e-1f, d2 = 2.445134137142996e0f,
               d3 = 3.754408661907416e0f;
-  if (x >= x_lo && x <= x_hi) {
-    float q = fmaf((float)(int32_t)(x ^ 0x80000000u), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-    float r = q * q;
-    float num = fmaf(fmaf(fmaf(fmaf(fmaf(a0, r, a1), r, a2), r, a3), r, a4), r, a5) * q;
-    float den = fmaf(fmaf(fmaf(fmaf(fmaf(b0, r, b1), r, b2), r, b3), r, b4), r, 1.0f);
-    return __fdividef(num, den);
-  }
   const bool lower = x < x_lo;
   const uint32_t t = lower ? x : ~x;
   float p = fmaf((float)t, 2.3283064365386963e-10f, 1.1641532182693481e-10f);
@@ -184,6 +184,13 @@ __device__ __forceinline__ float rg_probit32(uint32_t x, uint32_t x_lo, uint32_t
   float den = fmaf(fmaf(fmaf(fmaf(d0, q, d1), q, d2), q, d3), q, 1.0f);
   float z = __fdividef(num, den);
   return lower ? z : -z;
+}
+
+// The same approximation in FP32, taking the 32-bit scrambled integer x (u = (x + 1/2) / 2^32).
+// The branch is decided on x against integer thresholds computed in FP64 on the host, so every
+// coordinate takes the same branch as the FP64 reference.
+__device__ __forceinline__ float rg_probit32(uint32_t x, uint32_t x_lo, uint32_t x_hi) {
+  return (x >= x_lo && x <= x_hi) ? rg_probit32_central(x) : rg_probit32_tail(x, x_lo);
 }
 
 // ------------------------------------------------------------------ Halton -------------------
@@ -236,4 +243,4 @@ __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTa
 struct DevRecordOut;  // forward
 
 // Status word a kernel raises instead of trapping.
-enum { KSTAT_OK = 0, KSTAT_BAD_LAUNCH = 1 };
+enum { KSTAT_OK = 0, KSTAT_BAD_LAUNCH = 1, KSTAT_TIMEOUT = 2 };

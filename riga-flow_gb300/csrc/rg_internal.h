@@ -2,6 +2,7 @@
 // kernel launchers.  Nothing here crosses the C ABI.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -235,11 +236,11 @@ struct BookDev {
   const int32_t* order;        // [n_trades] trade order of the work items (longest first)
 };
 // Universe increments of paths [path0, path0 + npaths): incr[t][u][p], FP64 ΔW/√dt (parity) or
-// FP32 ΔW (production); one thread per (path, universe asset).
+// FP32 ΔW (production, rows of `rowlen` >= npaths floats so that tensor-map strides are aligned).
 void launch_book_gen64(const DevTrade& gen, const DevTables& tb, const double* L, int U,
                        uint64_t path0, uint64_t npaths, double* incr, cudaStream_t s);
 void launch_book_gen32(const DevTrade& gen, const DevTables& tb, const float* L32, int U,
-                       uint64_t path0, uint64_t npaths, float* incr, cudaStream_t s);
+                       uint64_t path0, uint64_t npaths, uint64_t rowlen, float* incr, cudaStream_t s);
 // FP64 scan of every (trade, scenario) on the chunk's increments: one thread per (pair, path);
 // partial[pair][block][RG_ACC] over `blocks` blocks of 128 paths; records[p][pair] when given.
 // partial[pair][block][RG_ACC] with `blocks` blocks of 128 paths per pair.
@@ -249,12 +250,15 @@ void launch_book_trade64(const DevTrade& gen, const BookDev& bk, const double* i
 // FP32 persistent scan: work items (path block, trade) with block-major order; every item's
 // FP64 sums land in partial[(block0 + b) * n_trades + j][S][RG_ACC].
 struct Book32Shape {
-  int threads, Sb, Pb, grid, blk_paths;
+  int threads, Sb, Pb, TT, grid, blk_paths, smem;
 };
 Book32Shape book32_shape(int S, int sm_count);
-void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const float* incr, uint64_t npaths,
-                         uint64_t block0, double* partial, int32_t* counter, int* status,
-                         cudaStream_t s);
+// `tmap` views the chunk's increments as [TU][U][npaths] floats (boxes of Pb paths × 1 asset × TT
+// steps) for the kernel's TMA stages.
+// One persistent launch per underlying count n with trades order[group_lo[n-1], + group_n[n-1]).
+void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
+                         uint64_t block0, const int* group_lo, const int* group_n, double* partial,
+                         int32_t* counter, int* status, cudaStream_t s);
 // The FP32 copy of the universe Cholesky factor.
 void launch_book_l32(const double* L, int U, float* L32, cudaStream_t s);
 // Fixed-order sums over path blocks: out[pair][k] = Σ_b partial[b·stride_b + pair·stride_pair + k].
