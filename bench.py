@@ -407,9 +407,24 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-book", action="store_true", help="skip the book (cfg 2) measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (cfg 3) measurement")
+    ap.add_argument("--only", choices=["book", "serving"], default=None,
+                    help="run one secondary measurement alone (for profiling) and print its JSON")
     ap.add_argument("--book-trades", type=int, default=4096)
     ap.add_argument("--book-paths", type=int, default=1 << 18)
     args = ap.parse_args()
+    if args.only:
+        import torch
+
+        torch.cuda.set_device(0)
+        from riga_gb300.build import build_library
+        from riga_gb300.engine import Engine
+
+        build_library()
+        if args.only == "book":
+            print(json.dumps(book_measure(Engine(0), args.book_trades, args.book_paths)), flush=True)
+        else:
+            print(json.dumps(serving_measure()), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -371,6 +371,23 @@ int32_t rg_book_run_paths(rg_engine* engine, const rg_book_request* request,
                           const rg_market_snapshot* scenarios, int32_t n_scenarios,
                           uint64_t first_path, uint64_t count, rg_path_record* out);
 
+/* A resident book: trades uploaded once, then priced under many scenario sets.  rg_book_create
+ * uploads the book to the engine's device once — trade tables, QMC tables, bridge schedule, the
+ * universe Cholesky factor and the universe's FP32 increments of every path (they do not depend on
+ * the scenarios; up to 96 GiB).  rg_book_price prices it under a new scenario set: host planning of
+ * the scenario tables, then the replay of a CUDA graph of the device work (scenario upload, scans,
+ * reduction, download) captured on the first call for that scenario count, after an autotuner has
+ * timed the scan's stage depth (time steps per TMA stage) on a prefix of the paths.  Results equal
+ * rg_price_book's for the same book and scenarios bit for bit (the tuned stage depth changes the
+ * schedule, not the arithmetic).  FP32 books only; the engine must outlive the book. */
+typedef struct rg_book rg_book;
+int32_t rg_book_create(rg_engine* engine, const rg_book_request* request, rg_book** out);
+int32_t rg_book_price(rg_book* book, const rg_market_snapshot* scenarios, int32_t n_scenarios,
+                      rg_price_result* out);
+/* The stage depth the autotuner chose for n_scenarios (0 before the first price at that count). */
+int32_t rg_book_tuned_stage(rg_book* book, int32_t n_scenarios, int32_t* steps_per_stage);
+void rg_book_destroy(rg_book* book);
+
 /* ------------------------------------------------------------------ serving ------------------- */
 /* A continuous-batching request server on one GPU (the engine side of the reference's MCP task
  * loop, crates/riga-mcp/src/main.rs:1000-1042, with its tasks/get, tasks/result and tasks/cancel

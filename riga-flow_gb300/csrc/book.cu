@@ -14,33 +14,10 @@
 #include <algorithm>
 #include <cmath>
 
-#include "rg_internal.h"
+#include "rg_book.h"
 
 namespace rg {
-
-namespace {
-
-enum BookSlot { BK_TABLES = 0, BK_INCR0, BK_INCR1, BK_PARTIAL, BK_SUMS, BK_RECORDS, BK_SCRATCH, BK_NSLOTS };
-static_assert(BK_NSLOTS <= 8, "engine book buffers");
-
-// Byte budget of one increments buffer (two are in flight).
-constexpr size_t kIncrBudget = size_t(6) << 30;
-
-struct BookPlan {
-  int U = 0, S = 0, n_trades = 0;
-  int64_t TU = 0;
-  double dt = 0;
-  DevTrade gen{};
-  Prepared br;  // bridge schedule of the universe grid (node_* and stack_max only)
-  std::vector<int32_t> nf_row;
-  std::vector<uint32_t> nf_shift;
-  std::vector<BookTradeDev> trades;
-  std::vector<BookScenDev> scen;
-  std::vector<BookPair32> pair32;
-  std::vector<double> df, dfm;
-  std::vector<int32_t> order;
-  int group_lo[RG_NMAX], group_n[RG_NMAX];
-};
+namespace bk {
 
 void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen) {
   if (!r) raise(RG_ERR_INVALID_ARGUMENT, "request is null");
@@ -59,15 +36,6 @@ void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n
     raise(RG_ERR_UNSUPPORTED, "books run the Sobol or Halton lane");
   if (c.trace_level != RG_TRACE_OFF)
     raise(RG_ERR_INVALID_ARGUMENT, "books record no trace events (trace_level must be off)");
-  if (n_scen < 0 || (n_scen > 0 && !sc)) raise(RG_ERR_INVALID_ARGUMENT, "bad scenario list");
-  for (int s = 0; s < n_scen; ++s) {
-    if (sc[s].n_assets != U || !sc[s].spots || !sc[s].vols || !sc[s].dividend_yields)
-      raise(RG_ERR_INVALID_MARKET_SHAPE, "scenario " + std::to_string(s) + " is not a market of the universe");
-    if (sc[s].correlation &&
-        memcmp(sc[s].correlation, u.correlation, sizeof(double) * (size_t)U * (size_t)U) != 0)
-      raise(RG_ERR_INVALID_ARGUMENT,
-            "scenario " + std::to_string(s) + " changes the correlation; book scenarios share the base paths");
-  }
   const double dt = r->universe_maturity_years / (double)r->universe_steps;
   double sub_spots[RG_NMAX], sub_vols[RG_NMAX], sub_q[RG_NMAX], sub_rho[RG_NMAX * RG_NMAX];
   for (int j = 0; j < r->n_trades; ++j) {
@@ -119,7 +87,19 @@ void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n
   for (int a = 0; a < U; ++a)
     if (!(u.spots[a] > 0.0) || !(u.vols[a] >= 0.0) || !std::isfinite(u.vols[a]) || !std::isfinite(u.dividend_yields[a]))
       raise(RG_ERR_INVALID_MARKET, "universe spots must be positive and vols non-negative");
+  validate_book_scenarios(u, sc, n_scen);
+}
+
+void validate_book_scenarios(const rg_market_snapshot& u, const rg_market_snapshot* sc, int n_scen) {
+  const int U = u.n_assets;
+  if (n_scen < 0 || (n_scen > 0 && !sc)) raise(RG_ERR_INVALID_ARGUMENT, "bad scenario list");
   for (int s = 0; s < n_scen; ++s) {
+    if (sc[s].n_assets != U || !sc[s].spots || !sc[s].vols || !sc[s].dividend_yields)
+      raise(RG_ERR_INVALID_MARKET_SHAPE, "scenario " + std::to_string(s) + " is not a market of the universe");
+    if (sc[s].correlation &&
+        memcmp(sc[s].correlation, u.correlation, sizeof(double) * (size_t)U * (size_t)U) != 0)
+      raise(RG_ERR_INVALID_ARGUMENT,
+            "scenario " + std::to_string(s) + " changes the correlation; book scenarios share the base paths");
     if (!std::isfinite(sc[s].risk_free_rate)) raise(RG_ERR_INVALID_MARKET, "scenario rate must be finite");
     for (int a = 0; a < U; ++a)
       if (!(sc[s].spots[a] > 0.0) || !std::isfinite(sc[s].spots[a]) || !(sc[s].vols[a] >= 0.0) ||
@@ -135,11 +115,6 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
   B.TU = r->universe_steps;
   B.dt = r->universe_maturity_years / (double)r->universe_steps;
   B.n_trades = r->n_trades;
-  if (n_scen == 0) {
-    sc = &u;
-    n_scen = 1;
-  }
-  B.S = n_scen;
   DevTrade& g = B.gen;
   g.n = B.U;
   g.vr = c.variance_reduction;
@@ -187,6 +162,28 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
     d.ln_ki = (float)std::log(d.ki);
     d.coupon_f = (float)d.coupon_rate;
   }
+  // work order: grouped by underlying count (one launch each), longest trades first in a group
+  B.order.resize(B.n_trades);
+  for (int j = 0; j < B.n_trades; ++j) B.order[j] = j;
+  std::stable_sort(B.order.begin(), B.order.end(), [&](int a, int b) {
+    if (B.trades[a].n != B.trades[b].n) return B.trades[a].n < B.trades[b].n;
+    return B.trades[a].T > B.trades[b].T;
+  });
+  for (int n = 0; n < RG_NMAX; ++n) B.group_lo[n] = B.group_n[n] = 0;
+  for (int i = 0; i < B.n_trades; ++i) {
+    const int n = B.trades[B.order[i]].n;
+    if (B.group_n[n - 1]++ == 0) B.group_lo[n - 1] = i;
+  }
+  plan_book_scenarios(r, sc, n_scen, B);
+}
+
+// The scenario-dependent tables: markets, discount factors, per-(trade, scenario) FP32 constants.
+void plan_book_scenarios(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B) {
+  if (n_scen == 0) {
+    sc = &r->universe;
+    n_scen = 1;
+  }
+  B.S = n_scen;
   B.scen.resize(B.S);
   B.df.resize((size_t)B.S * B.TU);
   for (int s = 0; s < B.S; ++s) {
@@ -218,33 +215,14 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
         p.sig[f] = (float)v;
       }
     }
-  // work order: grouped by underlying count (one launch each), longest trades first in a group
-  B.order.resize(B.n_trades);
-  for (int j = 0; j < B.n_trades; ++j) B.order[j] = j;
-  std::stable_sort(B.order.begin(), B.order.end(), [&](int a, int b) {
-    if (B.trades[a].n != B.trades[b].n) return B.trades[a].n < B.trades[b].n;
-    return B.trades[a].T > B.trades[b].T;
-  });
-  for (int n = 0; n < RG_NMAX; ++n) B.group_lo[n] = B.group_n[n] = 0;
-  for (int i = 0; i < B.n_trades; ++i) {
-    const int n = B.trades[B.order[i]].n;
-    if (B.group_n[n - 1]++ == 0) B.group_lo[n - 1] = i;
-  }
 }
-
-struct BookStaged {
-  DevTables tb{};
-  BookDev bk{};
-  double* L = nullptr;
-  float* L32 = nullptr;
-};
 
 void* book_buf(rg_engine* E, int slot, size_t bytes) {
   E->book_bufs[slot].ensure(bytes);
   return E->book_bufs[slot].ptr;
 }
 
-BookStaged stage_book(rg_engine* E, const rg_book_request* r, BookPlan& B) {
+BookStaged stage_book_static(DevBuf& tables, cudaStream_t st, const rg_book_request* r, const BookPlan& B) {
   Pack pk;
   const int U = B.U;
   size_t o_sobol = 0, o_hb = 0, o_ho = 0, o_hp = 0;
@@ -259,15 +237,15 @@ BookStaged stage_book(rg_engine* E, const rg_book_request* r, BookPlan& B) {
   }
   const size_t o_noff = pk.add(B.br.node_off), o_nk = pk.add(B.br.node_k), o_nc = pk.add(B.br.node_c),
                o_ncf = pk.add(B.br.node_cf);
-  const size_t o_tr = pk.add(B.trades), o_sc = pk.add(B.scen), o_p32 = pk.add(B.pair32), o_df = pk.add(B.df),
-               o_dfm = pk.add(B.dfm), o_ord = pk.add(B.order);
+  const size_t o_tr = pk.add(B.trades), o_ord = pk.add(B.order);
   const size_t o_corr = pk.add(r->universe.correlation, (size_t)U * U);
   const size_t o_L = pk.reserve(sizeof(double) * U * U), o_L32 = pk.reserve(sizeof(float) * U * U);
   const size_t o_work = pk.reserve(sizeof(double) * 2 * U * U);
-  uint8_t* dev = static_cast<uint8_t*>(book_buf(E, BK_TABLES, pk.host.size()));
-  cuda_check(cudaMemcpyAsync(dev, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, E->stream), "book H2D");
-  BookStaged st;
-  DevTables& tb = st.tb;
+  tables.ensure(pk.host.size());
+  uint8_t* dev = static_cast<uint8_t*>(tables.ptr);
+  cuda_check(cudaMemcpyAsync(dev, pk.host.data(), pk.host.size(), cudaMemcpyHostToDevice, st), "book H2D");
+  BookStaged out;
+  DevTables& tb = out.tb;
   tb.sobol = B.gen.vr == RG_VR_SOBOL ? reinterpret_cast<const uint32_t*>(dev + o_sobol) : nullptr;
   tb.hal_base = B.gen.vr == RG_VR_HALTON ? reinterpret_cast<const uint32_t*>(dev + o_hb) : nullptr;
   tb.hal_off = B.gen.vr == RG_VR_HALTON ? reinterpret_cast<const uint32_t*>(dev + o_ho) : nullptr;
@@ -276,25 +254,38 @@ BookStaged stage_book(rg_engine* E, const rg_book_request* r, BookPlan& B) {
   tb.node_k = reinterpret_cast<const int32_t*>(dev + o_nk);
   tb.node_c = reinterpret_cast<const double*>(dev + o_nc);
   tb.node_cf = reinterpret_cast<const float*>(dev + o_ncf);
-  BookDev& bk = st.bk;
+  BookDev& bk = out.bk;
   bk.U = U;
   bk.S = B.S;
   bk.n_trades = B.n_trades;
   bk.TU = B.TU;
   bk.trades = reinterpret_cast<const BookTradeDev*>(dev + o_tr);
-  bk.scen = reinterpret_cast<const BookScenDev*>(dev + o_sc);
-  bk.pair32 = reinterpret_cast<const BookPair32*>(dev + o_p32);
-  bk.df = reinterpret_cast<const double*>(dev + o_df);
-  bk.dfm = reinterpret_cast<const double*>(dev + o_dfm);
   bk.order = reinterpret_cast<const int32_t*>(dev + o_ord);
-  st.L = reinterpret_cast<double*>(dev + o_L);
-  st.L32 = reinterpret_cast<float*>(dev + o_L32);
-  bk.L = st.L;
-  bk.L32 = st.L32;
-  launch_cholesky_big(reinterpret_cast<const double*>(dev + o_corr), U, st.L,
-                      reinterpret_cast<double*>(dev + o_work), E->stream);
-  launch_book_l32(st.L, U, st.L32, E->stream);
-  return st;
+  out.L = reinterpret_cast<double*>(dev + o_L);
+  out.L32 = reinterpret_cast<float*>(dev + o_L32);
+  bk.L = out.L;
+  bk.L32 = out.L32;
+  launch_cholesky_big(reinterpret_cast<const double*>(dev + o_corr), U, out.L,
+                      reinterpret_cast<double*>(dev + o_work), st);
+  launch_book_l32(out.L, U, out.L32, st);
+  return out;
+}
+
+ScenarioPack pack_book_scenarios(const BookPlan& B) {
+  ScenarioPack sp;
+  sp.o_scen = sp.pk.add(B.scen);
+  sp.o_p32 = sp.pk.add(B.pair32);
+  sp.o_df = sp.pk.add(B.df);
+  sp.o_dfm = sp.pk.add(B.dfm);
+  return sp;
+}
+
+void point_scenarios(const ScenarioPack& sp, const uint8_t* dev, int S, BookDev& bk) {
+  bk.S = S;
+  bk.scen = reinterpret_cast<const BookScenDev*>(dev + sp.o_scen);
+  bk.pair32 = reinterpret_cast<const BookPair32*>(dev + sp.o_p32);
+  bk.df = reinterpret_cast<const double*>(dev + sp.o_df);
+  bk.dfm = reinterpret_cast<const double*>(dev + sp.o_dfm);
 }
 
 // The tensor map of one chunk's FP32 increments, viewed as [TU][U][npaths] with rows of `rowlen`
@@ -329,9 +320,10 @@ uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t un
   return paths < cap ? paths : cap;
 }
 
-}  // namespace
+}  // namespace bk
 
 size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
+  using namespace bk;
   const size_t S = n_scen > 0 ? (size_t)n_scen : 1;
   const size_t U = (size_t)(r->universe.n_assets > 0 ? r->universe.n_assets : 1);
   const size_t TU = (size_t)(r->universe_steps > 0 ? r->universe_steps : 1);
@@ -352,6 +344,8 @@ size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
 
 namespace {
 
+using namespace bk;
+
 // Prices (records == nullptr) or replays [first, first + count) of the book.
 void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* sc, int n_scen,
               rg_price_result* out, uint64_t first, uint64_t count, rg_path_record* records) {
@@ -360,7 +354,14 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
   plan_book(r, sc, n_scen, B);
   const int pairs = B.n_trades * B.S;
   const bool fp32 = r->config.precision == RG_PRECISION_FP32 && !records;
-  BookStaged st = stage_book(E, r, B);
+  BookStaged st = stage_book_static(E->book_bufs[BK_TABLES], E->stream, r, B);
+  {
+    const ScenarioPack sp = pack_book_scenarios(B);
+    uint8_t* dev = static_cast<uint8_t*>(book_buf(E, BK_SCEN, sp.pk.host.size()));
+    cuda_check(cudaMemcpyAsync(dev, sp.pk.host.data(), sp.pk.host.size(), cudaMemcpyHostToDevice, E->stream),
+               "book scenarios H2D");
+    point_scenarios(sp, dev, B.S, st.bk);
+  }
   const uint64_t path_base = r->config.first_path + first;
   const uint64_t P = records ? count : r->config.paths;
   cudaStream_t s0 = E->stream, s1 = E->gen_stream;

@@ -334,6 +334,10 @@ SIGNATURES = {
                              C.POINTER(PriceResult)]),
     "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,
                                  C.POINTER(PathRecord)]),
+    "rg_book_create": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(_vp)]),
+    "rg_book_price": (_i32, [_vp, C.POINTER(Market), _i32, C.POINTER(PriceResult)]),
+    "rg_book_tuned_stage": (_i32, [_vp, _i32, C.POINTER(_i32)]),
+    "rg_book_destroy": (None, [_vp]),
     "rg_server_create": (_i32, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "rg_server_destroy": (None, [_vp]),
     "rg_server_submit_price": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32,

@@ -63,6 +63,10 @@ class Engine:
         check(self.lib, self.lib.rg_price_book(self.handle, a.ptr, arr, n, out))
         return list(out)
 
+    def resident_book(self, book: BookRequest) -> "ResidentBook":
+        """Upload `book` once (rg_book_create); price it under many scenario sets."""
+        return ResidentBook(self, book)
+
     def book_run_paths_raw(self, book: BookRequest, scenarios, first: int, count: int) -> list:
         """Per-path records ``out[(p * n_trades + j) * S + s]`` of paths [first, first + count)."""
         a = book.to_abi()
@@ -144,3 +148,39 @@ def price_put_leg(request: PriceRequest) -> dict:
 
 def price_risk_batch(request: PriceRequest, config=None):
     return default_engine().price_risk_batch_raw(request, config)
+
+
+class ResidentBook:
+    """A book resident on the engine's device (rg_book_*): priced by CUDA-graph replay."""
+
+    def __init__(self, engine: Engine, book: BookRequest):
+        self.engine = engine
+        self.lib = engine.lib
+        self.n_trades = len(book.trades)
+        a = book.to_abi()
+        h = C.c_void_p()
+        check(self.lib, self.lib.rg_book_create(engine.handle, a.ptr, C.byref(h)))
+        self.handle = h
+
+    def price_raw(self, scenarios=None) -> list:
+        keep = []
+        arr, n = markets_to_abi(scenarios, keep.append)
+        out = (abi.PriceResult * (self.n_trades * max(1, n)))()
+        check(self.lib, self.lib.rg_book_price(self.handle, arr, n, out))
+        return list(out)
+
+    def tuned_stage(self, n_scenarios: int) -> int:
+        v = C.c_int32()
+        check(self.lib, self.lib.rg_book_tuned_stage(self.handle, n_scenarios, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.handle:
+            self.lib.rg_book_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -121,3 +121,32 @@ def test_book_errors_keep_the_reference_codes(engine):
     with pytest.raises(abi.RigaError) as e:
         engine.price_book_raw(b)
     assert e.value.code == "invalid_market_shape"
+
+
+def test_resident_book_replays_equal_the_one_shot_price(engine):
+    """rg_book_create / rg_book_price: the graph-replayed price equals rg_price_book bit for bit,
+    for several scenario sets and counts, whatever stage depth the autotuner picked."""
+    b = workloads.small_book(paths=1 << 13, n_trades=9, steps_per_year=52, max_years=3, fp32=True)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)]
+    with engine.resident_book(b) as rb:
+        for subset in (sc, sc[:5], sc, sc[3:11], None):
+            got = rb.price_raw(subset)
+            want = engine.price_book_raw(b, subset)
+            assert [bytes(x) for x in got] == [bytes(x) for x in want]
+        assert rb.tuned_stage(16) in (8, 16, 32)
+        assert rb.tuned_stage(5) in (8, 16, 32)
+        assert rb.tuned_stage(7) == 0
+
+
+def test_resident_book_keeps_the_reference_error_codes(engine):
+    b = workloads.small_book(paths=1 << 10, n_trades=2, steps_per_year=12, fp32=True)
+    with engine.resident_book(b) as rb:
+        sc = copy.deepcopy(b.universe)
+        sc.spots = sc.spots[:-1]
+        with pytest.raises(abi.RigaError) as e:
+            rb.price_raw([sc])
+        assert e.value.code == "invalid_market_shape"
+    b64 = workloads.small_book(paths=64, n_trades=1)
+    with pytest.raises(abi.RigaError) as e:
+        engine.resident_book(b64)
+    assert e.value.code == "unsupported"
