@@ -324,6 +324,17 @@ int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
 int32_t rg_run_paths(rg_engine* engine, const rg_price_request* request, uint64_t first_path,
                      uint64_t count, rg_path_record* out);
 
+/* Replay materialisation of a priced trade: the spot paths of [first_path, first_path + count)
+ * under the request's base scenario as an f32 cube in PathCube's [path][time][factor] layout
+ * (crates/riga-engine/src/pathcube.rs:19-35): cube[(i * steps + t) * n + f] = S_f after step t
+ * (the state explain::run_paths holds after its multiplicative step, explain.rs:183-193; spots
+ * keep evolving after a knock-out there and here).  `records` (optional, may be null) receives
+ * the same paths' PathRecord fields.  Always computed by the FP64 kernel (the precision setting
+ * is ignored), each spot rounded to f32 on store; the cube is produced and copied out in chunks
+ * of at most 1 GiB, so `count` is bounded only by the host buffer. */
+int32_t rg_materialize_paths(rg_engine* engine, const rg_price_request* request, uint64_t first_path,
+                             uint64_t count, float* cube, rg_path_record* records);
+
 /* ------------------------------------------------------------------ books --------------------- */
 /* A book: many Phoenix trades on one asset universe, priced under one common CRN scenario set.
  * This entry point has no single counterpart in the reference, which prices one trade per

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
             "or_validate": (i32, [P(abi.PriceRequest)]),
             "or_price_put_leg": (i32, [P(abi.PriceRequest), i32, P(abi.PriceResult)]),
             "or_run_paths": (i32, [P(abi.PriceRequest), u64, u64, P(abi.PathRecord)]),
+            "or_materialize_paths": (i32, [P(abi.PriceRequest), u64, u64, P(C.c_float), P(abi.PathRecord)]),
             "or_price_scenarios": (i32, [P(abi.PriceRequest), P(abi.Scenario), i32, i32,
                                          P(abi.PriceResult)]),
             "or_price_risk_batch": (i32, [P(abi.PriceRequest), P(abi.CentralDifferenceConfig),
@@ -142,6 +143,17 @@ def run_paths(request, first: int, count: int):
     out = (abi.PathRecord * max(1, count))()
     _check(lib().or_run_paths(a.ptr, first, count, out))
     return out
+
+
+def materialize_paths(request, first: int, count: int):
+    """(f32 cube [count * steps * n], PathRecord array) of paths [first, first + count)."""
+    import numpy as np
+    a = request.to_abi()
+    n = len(request.market.spots)
+    cube = np.empty(max(1, count * request.trade.steps * n), dtype=np.float32)
+    out = (abi.PathRecord * max(1, count))()
+    _check(lib().or_materialize_paths(a.ptr, first, count, cube.ctypes.data_as(C.POINTER(C.c_float)), out))
+    return cube[: count * request.trade.steps * n], out
 
 
 def price_scenarios(request, scenarios, threads: int = 0):

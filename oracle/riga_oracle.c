@@ -972,8 +972,9 @@ static void path_increments(const model* m, uint64_t path_id, workspace* ws, cha
 }
 
 /* The Euler step and the Phoenix scan of one path (note.rs:129-259) over increment rows
- * incr[f][0..steps-1]; `stride` is the distance between consecutive steps of one row. */
-static void scan_path(const model* m, const double* const* incr, path_out* o) {
+ * incr[f][0..steps-1].  When `cube` is non-null it receives the spots after every step as
+ * f32, cube[step * n + f] (explain.rs:183-193 state; pathcube.rs:19-35 layout). */
+static void scan_path_cube(const model* m, const double* const* incr, path_out* o, float* cube) {
   const int n = m->n;
   const int64_t T = m->steps;
   const double dt = m->dt;
@@ -993,6 +994,8 @@ static void scan_path(const model* m, const double* const* incr, path_out* o) {
       double drift = (m->rate - m->q[f] - 0.5 * vol * vol) * dt;
       spots[f] *= OEXP(drift + vol * sqrt(dt) * incr[f][step]);
     }
+    if (cube)
+      for (int f = 0; f < n; ++f) cube[step * n + f] = (float)spots[f];
     double worst = spots[0] / m->init[0];
     for (int f = 1; f < n; ++f) worst = fmin(worst, spots[f] / m->init[f]);
     final_worst = worst;
@@ -1063,13 +1066,20 @@ static void scan_path(const model* m, const double* const* incr, path_out* o) {
   o->put_eligible = put_eligible;
   o->received = received;
 }
+static void scan_path(const model* m, const double* const* incr, path_out* o) {
+  scan_path_cube(m, incr, o, NULL);
+}
 
 /* One path of note.rs:81-259. */
-static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chacha8* mc, path_out* o) {
+static void simulate_path_cube(const model* m, uint64_t path_id, workspace* ws, chacha8* mc, path_out* o,
+                               float* cube) {
   path_increments(m, path_id, ws, mc);
   const double* rows[NMAX];
   for (int f = 0; f < m->n; ++f) rows[f] = ws->incr + (size_t)f * (size_t)m->steps;
-  scan_path(m, rows, o);
+  scan_path_cube(m, rows, o, cube);
+}
+static void simulate_path(const model* m, uint64_t path_id, workspace* ws, chacha8* mc, path_out* o) {
+  simulate_path_cube(m, path_id, ws, mc, o, NULL);
 }
 
 /* ---------------------------------------------------------------- aggregation --------------- */
@@ -1292,7 +1302,8 @@ int32_t or_price_put_leg(const rg_price_request* r, int32_t threads, rg_price_re
   return price_market(r, &r->market, NULL, threads, out);
 }
 
-int32_t or_run_paths(const rg_price_request* r, uint64_t first, uint64_t count, rg_path_record* out) {
+static int32_t run_path_range(const rg_price_request* r, uint64_t first, uint64_t count, rg_path_record* out,
+                              float* cube) {
   int32_t st = or_validate(r);
   if (st) return st;
   if ((st = check_lane(r))) return st;
@@ -1312,7 +1323,8 @@ int32_t or_run_paths(const rg_price_request* r, uint64_t first, uint64_t count, 
     for (uint64_t p = 0; p < first; ++p) simulate_path(&m, p, &ws, &g, &o);
   for (uint64_t i = 0; i < count; ++i) {
     uint64_t p = first + i;
-    simulate_path(&m, p, &ws, &g, &o);
+    simulate_path_cube(&m, p, &ws, &g, &o, cube ? cube + i * (uint64_t)m.steps * (uint64_t)m.n : NULL);
+    if (!out) continue;
     rg_path_record* rec = &out[i];
     memset(rec, 0, sizeof *rec);
     rec->path_id = m.first_path + p;
@@ -1334,6 +1346,16 @@ int32_t or_run_paths(const rg_price_request* r, uint64_t first, uint64_t count, 
   ws_free(&ws);
   model_free(&m);
   return RG_OK;
+}
+
+int32_t or_run_paths(const rg_price_request* r, uint64_t first, uint64_t count, rg_path_record* out) {
+  return run_path_range(r, first, count, out, NULL);
+}
+
+/* explain::run_paths with the spot path of every path kept (the replay cube). */
+int32_t or_materialize_paths(const rg_price_request* r, uint64_t first, uint64_t count, float* cube,
+                             rg_path_record* records) {
+  return run_path_range(r, first, count, records, cube);
 }
 
 int32_t or_price_scenarios(const rg_price_request* r, const rg_scenario* sc, int32_t n, int32_t threads,

@@ -75,6 +75,9 @@ int32_t or_price_put_leg(const rg_price_request* req, int32_t threads, rg_price_
 /* explain.rs run_paths over [first, first + count). */
 int32_t or_run_paths(const rg_price_request* req, uint64_t first, uint64_t count,
                      rg_path_record* out);
+/* run_paths plus the f32 spot cube [count][steps][n] (spots after each step); records may be null. */
+int32_t or_materialize_paths(const rg_price_request* req, uint64_t first, uint64_t count, float* cube,
+                             rg_path_record* records);
 /* Scenario batch: each scenario re-priced with the request's seed (CRN). */
 int32_t or_price_scenarios(const rg_price_request* req, const rg_scenario* sc, int32_t n,
                            int32_t threads, rg_price_result* out);

@@ -733,36 +733,63 @@ extern "C" int32_t rg_price_risk_batch(rg_engine* e, const rg_price_request* req
   })
 }
 
+// One path range of the base scenario: records (FP32 or FP64 kernel per the request) or, when
+// `cube` is non-null, the FP64 kernel's spot cube (and records) in chunks of at most 1 GiB of cube.
+static void run_path_range(rg_engine* e, const rg_price_request* req, uint64_t first, uint64_t count,
+                           rg_path_record* out, float* cube) {
+  if (first > req->config.paths || count > req->config.paths - first)
+    raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
+  if (count == 0) return;
+  std::lock_guard<std::mutex> lock(e->mu);
+  cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+  Prepared P;
+  prepare(req, nullptr, 0, P);
+  EngineWorkspace W(e);
+  Staged S = stage(W, req, P);
+  const uint64_t cube_row = (uint64_t)P.trade.steps * (uint64_t)P.n;  // floats per path
+  const uint64_t chunk_cap = cube ? std::max<uint64_t>(1, (uint64_t(1) << 28) / cube_row) : count;
+  for (uint64_t done = 0; done < count;) {
+    const uint64_t m = std::min(chunk_cap, count - done);
+    const double* mcz = mc_lane_normals(W, req, first + done, m);
+    const bool fp32 = req->config.precision == RG_PRECISION_FP32 && !mcz && !cube;
+    LaunchOut lo{};
+    lo.mcz = mcz;
+    Fp32Shape sh{};
+    lo.grid = fp32 ? (sh = phoenix32_shape(P, m, device_info().sm_count)).grid : phoenix64_grid(P, m);
+    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));
+    if (out) lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, m * sizeof(rg_path_record)));
+    if (cube) lo.cube = static_cast<float*>(W.device(WS_CUBE, m * cube_row * sizeof(float)));
+    const uint64_t path0 = req->config.first_path + first + done;
+    if (fp32)
+      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, e->stream);
+    else
+      launch_phoenix64(P, S.tb, S.scen, path0, m, lo, e->stream);
+    if (out)
+      cuda_check(cudaMemcpyAsync(out + done, lo.records, m * sizeof(rg_path_record), cudaMemcpyDeviceToHost,
+                                 e->stream), "D2H records");
+    if (cube)
+      cuda_check(cudaMemcpyAsync(cube + done * cube_row, lo.cube, m * cube_row * sizeof(float),
+                                 cudaMemcpyDeviceToHost, e->stream), "D2H cube");
+    cuda_check(cudaStreamSynchronize(e->stream), "run_paths");
+    done += m;
+  }
+}
+
 extern "C" int32_t rg_run_paths(rg_engine* e, const rg_price_request* req, uint64_t first, uint64_t count,
                                 rg_path_record* out) {
   RG_TRY({
     if (!e || !req || (count && !out)) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
     validate_request(req);
-    if (first > req->config.paths || count > req->config.paths - first)
-      raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
-    if (count == 0) return RG_OK;
-    std::lock_guard<std::mutex> lock(e->mu);
-    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
-    Prepared P;
-    prepare(req, nullptr, 0, P);
-    EngineWorkspace W(e);
-    Staged S = stage(W, req, P);
-    const double* mcz = mc_lane_normals(W, req, first, count);
-    const bool fp32 = req->config.precision == RG_PRECISION_FP32 && !mcz;
-    LaunchOut lo{};
-    lo.mcz = mcz;
-    Fp32Shape sh{};
-    lo.grid = fp32 ? (sh = phoenix32_shape(P, count, device_info().sm_count)).grid : phoenix64_grid(P, count);
-    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));
-    lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, count * sizeof(rg_path_record)));
-    const uint64_t path0 = req->config.first_path + first;
-    if (fp32)
-      launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, count, sh, lo, e->stream);
-    else
-      launch_phoenix64(P, S.tb, S.scen, path0, count, lo, e->stream);
-    cuda_check(cudaMemcpyAsync(out, lo.records, count * sizeof(rg_path_record), cudaMemcpyDeviceToHost,
-                               e->stream), "D2H records");
-    cuda_check(cudaStreamSynchronize(e->stream), "run_paths");
+    run_path_range(e, req, first, count, out, nullptr);
+  })
+}
+
+extern "C" int32_t rg_materialize_paths(rg_engine* e, const rg_price_request* req, uint64_t first,
+                                        uint64_t count, float* cube, rg_path_record* records) {
+  RG_TRY({
+    if (!e || !req || (count && !cube)) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    validate_request(req);
+    run_path_range(e, req, first, count, records, cube);
   })
 }
 

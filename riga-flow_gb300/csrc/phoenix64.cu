@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables t
                                                         double* __restrict__ partial,
                                                         int32_t* __restrict__ ko_steps,
                                                         rg_path_record* __restrict__ records,
-                                                        const double* __restrict__ mcz) {
+                                                        const double* __restrict__ mcz,
+                                                        float* __restrict__ cube) {
   __shared__ double red[128][RG_ACC + 1];
   __shared__ double acc_blk[RG_ACC];
   const int tid = threadIdx.x;
@@ -149,6 +150,11 @@ __global__ void __launch_bounds__(128) phoenix64_kernel(DevTrade tr, DevTables t
                         : vol[f];
           double drift = (rate - qd[f] - 0.5 * v * v) * dt;
           spots[f] *= rg_exp64(drift + v * sqrt_dt * shock[f]);
+        }
+        if (cube) {  // PathCube slice: the spots this step leaves (pathcube.rs:19-35 layout)
+          float* cp = cube + (i * (uint64_t)T + (uint64_t)t) * N;
+#pragma unroll
+          for (int f = 0; f < N; ++f) cp[f] = (float)spots[f];
         }
         double worst = spots[0] / tr.init[0];
 #pragma unroll
@@ -272,10 +278,12 @@ static void launch_n(const Prepared& P, const DevTables& tb, const DevScenario* 
                      uint64_t npaths, const LaunchOut& out, cudaStream_t s) {
   if (out.mcz)
     phoenix64_kernel<N, LV, true><<<out.grid, 128, 0, s>>>(P.trade, tb, scen, path0, npaths, out.partial,
-                                                           out.ko_steps, out.records, out.mcz);
+                                                           out.ko_steps, out.records, out.mcz,
+                                                           out.cube);
   else
     phoenix64_kernel<N, LV, false><<<out.grid, 128, 0, s>>>(P.trade, tb, scen, path0, npaths, out.partial,
-                                                            out.ko_steps, out.records, nullptr);
+                                                            out.ko_steps, out.records, nullptr,
+                                                            out.cube);
 }
 
 void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario* scen,

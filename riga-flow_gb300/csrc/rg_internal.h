@@ -123,6 +123,7 @@ struct Engine;
 enum WsSlot {
   WS_ARENA = 0, WS_CALIB, WS_LVROWS, WS_PARTIAL, WS_SUMS, WS_KOSTEPS, WS_RECORDS,
   WS_MCZ, WS_MCKEYS, WS_MCAUX,  // the pseudo-random lane's normals, keystream and parse tables
+  WS_CUBE,                      // f32 spot cube of a materialised path range
   WS_NSLOTS
 };
 struct Workspace {
@@ -180,6 +181,7 @@ struct LaunchOut {
   rg_path_record* records;  // [npaths] or null
   int grid;
   const double* mcz = nullptr;  // pseudo-random lane: normals [npaths][T][n] of the launch's paths
+  float* cube = nullptr;        // [npaths][T][n] spots after each step (base scenario), or null
 };
 // StandardNormal draws [first, first + count) of ChaCha8Rng::seed_from_u64(seed) into d_out.
 void mc_normals(uint64_t seed, uint64_t first, uint64_t count, double* d_out, Workspace& W);

@@ -328,6 +328,8 @@ SIGNATURES = {
                                    C.POINTER(CentralDifferenceConfig),
                                    C.POINTER(BatchRiskReport)]),
     "rg_run_paths": (_i32, [_vp, C.POINTER(PriceRequest), _u64, _u64, C.POINTER(PathRecord)]),
+    "rg_materialize_paths": (_i32, [_vp, C.POINTER(PriceRequest), _u64, _u64, C.POINTER(C.c_float),
+                                    C.POINTER(PathRecord)]),
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
     "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,

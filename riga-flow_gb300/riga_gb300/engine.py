@@ -110,6 +110,25 @@ class Engine:
         n = request.config.paths - first if count is None else count
         return [record_to_dict(r) for r in self.run_paths_raw(request, first, n)][:n]
 
+    def materialize_paths(self, request: PriceRequest, first: int = 0, count: Optional[int] = None,
+                          with_records: bool = True):
+        """PathCube slice of a priced trade (``rg_materialize_paths``): the f32 spots
+        ``[count][steps][n]`` of paths [first, first + count) under the base scenario, and the
+        same paths' PathRecord dicts (or None)."""
+        import numpy as np
+        from .pathcube import PathCube
+
+        count = request.config.paths - first if count is None else count
+        n = len(request.market.spots)
+        steps = request.trade.steps
+        a = request.to_abi()
+        cube = np.empty(max(1, count * steps * n), dtype=np.float32)
+        recs = (abi.PathRecord * max(1, count))() if with_records else None
+        check(self.lib, self.lib.rg_materialize_paths(self.handle, a.ptr, first, count,
+                                                      cube.ctypes.data_as(C.POINTER(C.c_float)), recs))
+        out = PathCube(count, steps, n, cube[: count * steps * n])
+        return out, ([record_to_dict(r) for r in recs][:count] if with_records else None)
+
     def reconstruct_path(self, request: PriceRequest, path_id: int) -> dict:
         """explain.rs:319-333: one path re-simulated from its identity alone."""
         if path_id >= request.config.paths:

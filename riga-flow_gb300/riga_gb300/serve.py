@@ -9,8 +9,12 @@ JSON-RPC 2.0 ``tools/call`` for ``price_trade`` ({"request": PriceRequest JSON, 
 knobs}), ``risk_batch`` ({"request": ..., "options"?}), ``price_book`` ({"book": BookRequest JSON, "scenarios": [...]}) and
 ``price_book_async`` (returns a task, as the reference's SEP-2663 task path does, main.rs:1000-
 1042), plus ``tasks/get``, ``tasks/result`` and ``tasks/cancel``.  Synchronous tools also go
-through the server, so concurrent clients share its continuous batching.  ``python -m
-riga_gb300.serve`` runs the loop over stdin/stdout, one JSON message per line.
+through the server, so concurrent clients share its continuous batching.  The replay tools
+``reconstruct_path`` ({"request", "path_id"}), ``query_path_cube`` / ``query_pathcube``
+({"request", "percentile", "max_sample"}, main.rs:319-360) and ``materialize_paths`` ({"request",
+"first_path"?, "count"?}: at most 4096 paths, the reference's PathCube cap, main.rs:2134-2160)
+run synchronously on a replay engine of the loop's own.  ``python -m riga_gb300.serve`` runs the
+loop over stdin/stdout, one JSON message per line.
 """
 from __future__ import annotations
 
@@ -33,6 +37,7 @@ class Server:
 
     def __init__(self, device: int = 0, slots: int = 4, memory_budget: int = 0, lib=None):
         self.lib = lib or load_library()
+        self.device = device
         cfg = abi.ServerConfig(device, slots, memory_budget)
         h = C.c_void_p()
         check(self.lib, self.lib.rg_server_create(C.byref(cfg), C.byref(h)))
@@ -190,14 +195,59 @@ def _risk_json(rep: abi.BatchRiskReport) -> dict:
 
 
 # ---------------------------------------------------------------------- the request loop -------
+def cube_checksum(data) -> int:
+    """The PathCube checksum of the reference's generate_paths tool (main.rs:2145-2148): fold of
+    rotate_left(acc, 1) ^ f32 bits over the cube in order."""
+    import numpy as np
+
+    acc = 0
+    mask = (1 << 64) - 1
+    for b in np.ascontiguousarray(data, dtype=np.float32).view(np.uint32).tolist():
+        acc = (((acc << 1) | (acc >> 63)) & mask) ^ b
+    return acc
+
+
 class McpLoop:
     """JSON-RPC 2.0 dispatch of the pricing tools and the task methods onto a ``Server``."""
+
+    REPLAY_TOOLS = ("reconstruct_path", "query_path_cube", "query_pathcube", "materialize_paths")
+    CUBE_CAP = 4096
 
     def __init__(self, server: Server):
         self.server = server
         self._tasks = {}  # task id -> (ticket, tool, request object)
         self._lock = threading.Lock()
         self._next = 1
+        self._replay = None  # Engine for the replay tools, created on first use
+        self._replay_lock = threading.Lock()
+
+    def close(self):
+        if self._replay is not None:
+            self._replay.close()
+            self._replay = None
+
+    def _replay_tool(self, name, args):
+        from .engine import Engine
+
+        opts = EngineOptions(**{k: int(v) for k, v in (args.get("options") or {}).items()})
+        req = PriceRequest.from_json(args["request"], opts)
+        first = int(args.get("first_path", 0))
+        count = int(args.get("count", min(self.CUBE_CAP, max(0, req.config.paths - first))))
+        if name == "materialize_paths" and count > self.CUBE_CAP:
+            raise RigaError("invalid_paths", f"at most {self.CUBE_CAP} paths per materialisation")
+        with self._replay_lock:
+            if self._replay is None:
+                self._replay = Engine(self.server.device)
+            e = self._replay
+            if name == "reconstruct_path":
+                return {"structuredContent": e.reconstruct_path(req, int(args["path_id"]))}
+            if name in ("query_path_cube", "query_pathcube"):
+                return {"structuredContent": e.query_worst_percentile(req, float(args["percentile"]),
+                                                                      int(args["max_sample"]))}
+            cube, recs = e.materialize_paths(req, first, count)
+            return {"structuredContent": {"first_path": first, "paths": cube.paths, "times": cube.times,
+                                          "factors": cube.factors, "checksum": cube_checksum(cube.data),
+                                          "data": [float(v) for v in cube.data], "records": recs}}
 
     def handle(self, msg: dict) -> dict:
         mid = msg.get("id")
@@ -213,6 +263,8 @@ class McpLoop:
     def _dispatch(self, method, params):
         if method == "tools/call":
             name, args = params["name"], params.get("arguments") or {}
+            if name in self.REPLAY_TOOLS:
+                return self._replay_tool(name, args)
             if name == "health":
                 st = self.server.stats()
                 return {"status": "ok", "queued": st.queued, "running": st.running,
@@ -281,6 +333,7 @@ def main(argv=None):
             print(json.dumps({"jsonrpc": "2.0", "id": None, "error": {"code": -32700, "message": str(e)}}), flush=True)
             continue
         print(json.dumps(loop.handle(msg)), flush=True)
+    loop.close()
     server.close()
 
 

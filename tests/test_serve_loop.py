@@ -135,3 +135,24 @@ def test_server_needs_a_gpu():
     with pytest.raises(RigaError) as e:
         Server()
     assert e.value.code == "gpu_unavailable"
+
+
+def test_cube_checksum_is_the_rotate_xor_fold():
+    """main.rs:2145-2148: acc = rotate_left(acc, 1) ^ bits over the f32 cube."""
+    import numpy as np
+
+    from riga_gb300.serve import cube_checksum
+    assert cube_checksum(np.zeros(0, dtype=np.float32)) == 0
+    assert cube_checksum(np.array([1.0], dtype=np.float32)) == 0x3F800000
+    assert cube_checksum(np.array([1.0, 2.0], dtype=np.float32)) == (0x3F800000 << 1) ^ 0x40000000
+    top = np.array([-0.0] + [0.0] * 33, dtype=np.float32)  # sign bit rotated 33 times wraps past bit 63
+    assert cube_checksum(top) == 1
+
+
+def test_materialize_paths_is_capped_before_any_device_work():
+    req = workloads.plain3(1 << 13, steps=63)
+    loop = McpLoop(FakeServer())
+    out = loop.handle({"jsonrpc": "2.0", "id": 9, "method": "tools/call",
+                       "params": {"name": "materialize_paths",
+                                  "arguments": {"request": req.to_json(), "count": 5000}}})
+    assert out["error"]["data"]["code"] == "invalid_paths"

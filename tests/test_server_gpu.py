@@ -11,6 +11,7 @@
 from __future__ import annotations
 
 import copy
+import json
 import threading
 
 import pytest
@@ -189,3 +190,32 @@ def test_concurrent_requests_of_different_launch_shapes(engine):
         got = [srv.results(t) for t in ts]
     for a, g in zip(alone, got):
         assert [bytes(x) for x in a] == [bytes(x) for x in g]
+
+
+def test_mcp_replay_tools(engine):
+    """reconstruct_path / query_path_cube / materialize_paths over the loop's replay engine equal
+    the engine's own answers; the cube's records are the run_paths records of its range."""
+    from riga_gb300.serve import cube_checksum
+    req = workloads.plain3(paths=1 << 10, steps=126)
+    args = {"request": req.to_json(), "options": {"scrambler": req.options.scrambler,
+                                                  "precision": req.options.precision,
+                                                  "dim_mode": req.options.dim_mode}}
+    with Server(slots=1) as srv:
+        loop = McpLoop(srv)
+        try:
+            call = lambda name, **kw: loop.handle({"jsonrpc": "2.0", "id": 1, "method": "tools/call",
+                                                   "params": {"name": name, "arguments": {**args, **kw}}})
+            rec = call("reconstruct_path", path_id=77)["result"]["structuredContent"]
+            q = call("query_path_cube", percentile=0.05, max_sample=4)["result"]["structuredContent"]
+            q2 = call("query_pathcube", percentile=0.05, max_sample=4)["result"]["structuredContent"]
+            cube = call("materialize_paths", first_path=70, count=16)["result"]["structuredContent"]
+        finally:
+            loop.close()
+    same = lambda a, b: json.dumps(a, sort_keys=True) == json.dumps(b, sort_keys=True)  # ko_time NaN
+    assert same(rec, engine.reconstruct_path(req, 77))
+    assert same(q, q2) and same(q, engine.query_worst_percentile(req, 0.05, 4))
+    pc, recs = engine.materialize_paths(req, 70, 16)
+    assert same(cube["records"], recs) and same(cube["records"][7], rec)
+    assert cube["data"] == [float(v) for v in pc.data]
+    assert cube["checksum"] == cube_checksum(pc.data)
+    assert (cube["paths"], cube["times"], cube["factors"]) == (16, 126, 3)
