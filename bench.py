@@ -231,6 +231,41 @@ def fp64_plain_rate(eng):
     return float(1 << 16) * 756 / wall
 
 
+# ----------------------------------------------------------------------------- large (cfg 4) ---
+def large_measure(eng, paths: int = 1 << 24, sample_paths: int = 1 << 16):
+    """The large fused configuration: 5-asset worst-of Phoenix under Dupire local vol (64x32 SVI
+    grid, 64-point Dupire grid), 2-factor correlation, 1260 steps, `paths` Sobol paths in one FP32
+    launch with host inputs (rg_price_put_leg), cross-checked by the same run on scrambled Halton
+    points; FP32 against the FP64 parity kernel on the first `sample_paths` points."""
+    from riga_gb300 import workloads
+
+    out = {"workload": f"large fused: 5-asset worst-of Phoenix, Dupire local vol (seeded SVI 64x32, "
+                       f"64-point grid), 2-factor correlation, 5y x 1260 daily steps, {paths} paths, "
+                       f"one scenario, FP32 path state, FP64 sums, no path cube",
+           "paths": paths, "steps": 1260, "assets": 5}
+    res = {}
+    for kind in ("sobol", "halton"):
+        req = workloads.lv5_large(paths=paths, kind=kind)
+        warm = workloads.lv5_large(paths=1 << 12, kind=kind)
+        eng.price_raw(warm)
+        t0 = time.perf_counter()
+        r = eng.price_raw(req)
+        wall = time.perf_counter() - t0
+        tm = eng.last_timing()
+        res[kind] = r
+        out[kind] = {"pv": r.pv, "mc_error": r.mc_error, "wall_s": wall, "kernel_ms": tm.kernel_ms,
+                     "path_steps_per_s": float(paths) * 1260 / wall,
+                     "kernel_path_steps_per_s": float(paths) * 1260 / (tm.kernel_ms / 1e3)}
+    s, h = res["sobol"], res["halton"]
+    out["halton_vs_sobol_in_se"] = abs(s.pv - h.pv) / math.sqrt(s.mc_error ** 2 + h.mc_error ** 2)
+    r32 = eng.price_raw(workloads.lv5_large(paths=sample_paths))
+    r64 = eng.price_raw(workloads.lv5_large(paths=sample_paths, fp32=False))
+    out["accuracy"] = {"abs_err_vs_fp64": abs(r32.pv - r64.pv), "bound_min_0.1se_1bp": min(0.1 * r64.mc_error, 1e-4),
+                       "within_bound": abs(r32.pv - r64.pv) <= min(0.1 * r64.mc_error, 1e-4),
+                       "sample": f"first {sample_paths} Sobol points, FP32 kernel vs FP64 parity kernel"}
+    return out
+
+
 # ----------------------------------------------------------------------------- serving (cfg 3) -
 def serving_measure(duration_s: float = 5.0, rate_per_s: float = 200.0, seed: int = 7):
     """Seeded Poisson arrivals into the continuous-batching server (4 slots): 90% single trades
@@ -402,6 +437,8 @@ def run_gpu(args):
                                        "2^16 paths x 756 steps, rg_price_put_leg")
         book["throughput_vs_fp64_plain"] = book["path_steps_per_s"] / plain
         line["book"] = book
+    if world == 1 and not args.no_large:
+        line["large"] = large_measure(eng)
     if world == 1 and not args.no_serving:
         line["serving"] = serving_measure()
     if world == 1 and not args.no_cpu_baseline:
@@ -424,7 +461,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-book", action="store_true", help="skip the book (cfg 2) measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (cfg 3) measurement")
-    ap.add_argument("--only", choices=["book", "serving"], default=None,
+    ap.add_argument("--no-large", action="store_true", help="skip the large fused (cfg 4) measurement")
+    ap.add_argument("--only", choices=["book", "serving", "large"], default=None,
                     help="run one secondary measurement alone (for profiling) and print its JSON")
     ap.add_argument("--book-trades", type=int, default=4096)
     ap.add_argument("--book-paths", type=int, default=1 << 18)
@@ -439,6 +477,8 @@ def main():
         build_library()
         if args.only == "book":
             print(json.dumps(book_measure(Engine(0), args.book_trades, args.book_paths)), flush=True)
+        elif args.only == "large":
+            print(json.dumps(large_measure(Engine(0))), flush=True)
         else:
             print(json.dumps(serving_measure()), flush=True)
         return

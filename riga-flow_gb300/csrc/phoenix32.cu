@@ -403,6 +403,14 @@ static const void* select_kernel(int n, bool lv, bool rec) {
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
   if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
+  if (P.n_scen <= kP32DirectMaxScen) {
+    // nothing for the scenarios to share: the per-thread kernel without shared-memory tiles
+    sh.direct = 1;
+    sh.Sb = P.n_scen;
+    sh.threads = 256;
+    sh.grid = phoenix32d_grid(P, npaths, sm_count);
+    return sh;
+  }
   int sb = 1;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
@@ -452,6 +460,10 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                       const DevScen32* scen32, uint64_t path0, uint64_t npaths, const Fp32Shape& sh,
                       const LaunchOut& out, cudaStream_t st) {
+  if (sh.direct) {
+    launch_phoenix32d(P, tb, scen, scen32, path0, npaths, sh.grid, out, st);
+    return;
+  }
   const float ln_ko = (float)P.ln_ko, ln_cb = (float)P.ln_cb, ln_ki = (float)P.ln_ki;
   const int NNmax = sh.TT + P.stack_max;
 #define RG_LAUNCH(NN, LVV)                                                                        \

@@ -1,0 +1,329 @@
+// phoenix32d.cu — the FP32 kernel for launches with few CRN scenarios: one thread per (path,
+// scenario), everything in registers, no shared-memory time tiles and no CTA barriers.
+//
+// The tiled kernel (phoenix32.cu) stages a tile's normals and Brownian increments in shared
+// memory so that the scenarios of a path share one generation; with one or two scenarios there is
+// nothing to share and the staging costs occupancy (a 5-asset single-scenario launch fits one
+// 256-thread CTA per SM).  Here a warp walks 32 consecutive paths of one scenario through time:
+//   * Sobol points by warp cooperation: x(n) for the warp's first point is the XOR of the
+//     direction numbers at the set bits of its Gray code (lane k contributes bit k, a shuffle
+//     reduction), and the other lanes' points follow by the Gray recurrence
+//     x(n) = x(n-1) ^ v[ctz(n)] as an inclusive XOR scan over the lanes;
+//   * the digital shift (or Owen scramble) and the FP32 inverse normal of rg_common.cuh;
+//   * the streamed Brownian bridge per factor with its anchor stack in thread-local memory (the
+//     stack depth is warp-uniform, so every access is one coalesced line);
+//   * the correlation with the scenario's Cholesky factor, the log-space GBM / Dupire step and the
+//     Phoenix state machine.
+// Every operation of the per-path arithmetic is the one phoenix32.cu performs, in the same order,
+// so a path's FP32 payoff values are identical in both kernels.  The 32 paths of a warp are summed
+// by the same FP32 shuffle butterfly; above that, lane k of each warp keeps an FP64 running sum of
+// quantity k over the warp's path groups, and each CTA adds its warps' sums in warp order, so a
+// launch of a given shape is bit-reproducible.
+#include "rg_internal.h"
+
+namespace rg {
+
+#define P32D_THREADS 256
+#define P32D_WARPS (P32D_THREADS / 32)
+
+// Sobol integers x(n1 + lane) of one QMC dimension (direction numbers `row`) for the 32 lanes.
+__device__ __forceinline__ uint32_t warp_sobol(const uint32_t* __restrict__ row, uint64_t n1, int lane) {
+  const uint32_t g = (uint32_t)(n1 ^ (n1 >> 1));
+  uint32_t v = ((g >> lane) & 1u) ? __ldg(row + lane) : 0u;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, off);
+  // lanes past the request's last point may reach n = 2^32 (ctz 32); their values are never used
+  uint32_t d = lane == 0 ? v : __ldg(row + ((__ffsll((long long)(n1 + (uint64_t)lane)) - 1) & 31));
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, d, off);
+    if (lane >= off) d ^= t;
+  }
+  return d;
+}
+
+template <int N, bool LV, bool REC>
+__global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
+    DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
+    const DevScen32* __restrict__ scen32, int S, float ln_ko, float ln_cb, float ln_ki, uint64_t path0,
+    uint64_t npaths, double* __restrict__ partial, int32_t* __restrict__ ko_steps,
+    rg_path_record* __restrict__ records) {
+  __shared__ float4 s_lv[32 * RG_NMAX];
+  __shared__ double s_acc[P32D_WARPS][RG_ACC];
+  const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+  const int T = (int)tr.steps;
+  const int gx = tr.gx;
+  const float gxm1 = (float)(gx - 1);
+  const float nhdt = (float)(-0.5 * tr.dt);
+  const uint32_t x_lo = tr.x_lo, x_hi = tr.x_hi;
+  // the grid holds a multiple of S warps: warp w serves scenario w % S, path groups w / S + k·(W / S)
+  const int gw = blockIdx.x * P32D_WARPS + wib;
+  const int nw = gridDim.x * P32D_WARPS;
+  const int s = gw % S;
+  for (int i = tid; i < S * N; i += blockDim.x) {
+    const DevScen32& s3 = scen32[i / N];
+    const int f = i % N;
+    const float inv_gxm1 = 1.0f / (float)(tr.gx - 1);
+    s_lv[i] = make_float4(s3.a_u[f] * inv_gxm1, s3.inv_h[f] * inv_gxm1,
+                          __int_as_float((int)((uint32_t)s3.surf_off[f] - 0x4B000000u)), s3.x0[f]);
+  }
+  float Lf[N * (N + 1) / 2], mu[N], sig[N];
+  {
+    const DevScenario& sc = scen[s];
+    const DevScen32& s3 = scen32[s];
+    int q = 0;
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+      for (int b = 0; b <= a; ++b) Lf[q++] = (float)sc.L[a * N + b];
+#pragma unroll
+    for (int f = 0; f < N; ++f) {
+      mu[f] = s3.mu_dt[f];
+      sig[f] = s3.sig[f];
+    }
+  }
+  const float4* lvc = s_lv + s * N;
+  __syncthreads();
+
+  double lane_sum = 0.0;  // lane k < RG_ACC: this warp's FP64 sum of quantity k
+  const uint64_t groups = (npaths + 31) / 32;
+  for (uint64_t grp = (uint64_t)(gw / S); grp < groups; grp += (uint64_t)(nw / S)) {
+    const uint64_t gi = grp * 32 + lane;
+    const bool ok = gi < npaths;
+    const uint64_t n1 = path0 + grp * 32 + 1;  // Sobol point of the warp's first path
+    float x[N], wcur[N], stk[RG_STACK_MAX][N];
+#pragma unroll
+    for (int f = 0; f < N; ++f) {
+      x[f] = lvc[f].w;
+      wcur[f] = 0.0f;
+    }
+    int sp = 0;
+    bool alive = true, received = false;
+    int qual = 0, unpaid = 0, ko_step = -1, qualified = 0, paid = 0;
+    float cpv = 0.0f, mpv = 0.0f;
+    float worst = 0.0f;
+    for (int t = 0; t < T; ++t) {
+      // bridge nodes consumed at this step: normals, then the streamed bridge (qmc.rs:158-191)
+      const int c0 = __ldg(tb.node_off + t), c1 = __ldg(tb.node_off + t + 1);
+      for (int c = c0; c < c1; ++c) {
+        const float cf = __ldg(tb.node_cf + c);
+#pragma unroll
+        for (int f = 0; f < N; ++f) {
+          float z;
+          if (tr.vr == RG_VR_SOBOL) {
+            const uint32_t xs = warp_sobol(tb.sobol + 32 * (size_t)__ldg(tb.nf_row + c * N + f), n1, lane);
+            if (tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT)
+              z = rg_probit32(xs ^ __ldg(tb.nf_shift + c * N + f), x_lo, x_hi);
+            else
+              z = rg_probit32(rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed), x_lo, x_hi);
+          } else {
+            z = (float)rg_qmc_normal64(tr, tb, path0 + gi, (uint64_t)__ldg(tb.node_k + c) * N + f);
+          }
+          stk[sp][f] = c == 0 ? z * cf : fmaf(z, cf, 0.5f * (wcur[f] + stk[sp - 1][f]));
+        }
+        ++sp;
+      }
+      --sp;
+      float d[N], y[N];
+#pragma unroll
+      for (int f = 0; f < N; ++f) {
+        const float wn = stk[sp][f];
+        d[f] = wn - wcur[f];
+        wcur[f] = wn;
+      }
+      const int tg = t * gx;
+      int q = 0;
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        float acc_y = 0.0f;
+#pragma unroll
+        for (int b = 0; b <= a; ++b) acc_y = fmaf(Lf[q++], d[b], acc_y);
+        y[a] = acc_y;
+      }
+      float wmin = INFINITY;
+#pragma unroll
+      for (int f = 0; f < N; ++f) {
+        float sg;
+        if (LV) {
+          // the saturating grid lookup of phoenix32.cu: u01 clamped by the FMA's saturation, the
+          // grid index from a round-down FMA's bit pattern (bias folded into c4.z), one gather
+          const float4 c4 = lvc[f];
+          const float u01 = __saturatef(fmaf(x[f], c4.y, c4.x));
+          const float fl = __fmaf_rd(u01, gxm1, 8388608.0f);
+          const float w = fmaf(u01, gxm1, 8388608.0f - fl);
+          const uint32_t idx = (uint32_t)__float_as_int(c4.z) + (uint32_t)tg + (uint32_t)__float_as_int(fl);
+          const float2 r = __ldg(tb.lv_rows + idx);
+          sg = fmaf(w, r.y, r.x);
+        } else {
+          sg = sig[f];
+        }
+        x[f] = fmaf(sg, fmaf(nhdt, sg, y[f]), x[f]) + mu[f];
+        wmin = fminf(wmin, x[f]);
+      }
+      worst = wmin;
+      if (alive) {
+        // Phoenix state machine (note.rs:150-218)
+        const uint32_t fl = __ldg(tb.step_flags + t);
+        if (fl & STEP_PERIOD_RESET) qual = 0;
+        if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
+          ++qual;
+          if (REC) ++qualified;
+        }
+        if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
+          alive = false;
+          ko_step = t;
+          const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                                  : (float)qual * (float)__ldg(tb.accr_inc + __ldg(tb.step_period + t));
+          const float carry = due > 0.0f ? (float)unpaid * (float)tr.coupon_rate : 0.0f;
+          if (due + carry > 0.0f) {
+            const float df = (float)__ldg(tb.df + (size_t)s * T + t);
+            cpv = fmaf(due, df, cpv);
+            mpv = fmaf(carry, df, mpv);
+            received = true;
+            if (REC) ++paid;
+          }
+        } else if (fl & STEP_PERIOD_END) {
+          const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                                  : (float)qual * (float)__ldg(tb.accr_inc + __ldg(tb.step_period + t));
+          if (due > 0.0f) {
+            const float df = (float)__ldg(tb.df + (size_t)s * T + t);
+            cpv = fmaf(due, df, cpv);
+            mpv = fmaf((float)unpaid * (float)tr.coupon_rate, df, mpv);
+            unpaid = 0;
+            received = true;
+            if (REC) ++paid;
+          } else if (tr.memory) {
+            ++unpaid;
+          }
+        }
+      }
+    }
+    // path close (note.rs:221-258)
+    float out[RG_ACC];
+#pragma unroll
+    for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0f;
+    if (ok) {
+      const bool ko = ko_step >= 0;
+      const float df_mat = (float)__ldg(tb.df_mat + s);
+      const float funding = ko ? (float)__ldg(tb.df + (size_t)s * T + ko_step) : df_mat;
+      const bool hit_ki = worst <= ln_ki;
+      const bool put_ok = hit_ki && !ko;
+      const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * df_mat : 0.0f;
+      const float cn = cpv + mpv;
+      const float pv1 = (funding - 1.0f) + cn - put;
+      out[ACC_PV] = pv1;
+      out[ACC_PV2] = pv1 * pv1;
+      if (ko) {
+        out[ACC_KOF] = funding - 1.0f;
+        out[ACC_KOF2] = (funding - 1.0f) * (funding - 1.0f);
+        out[ACC_NKO] = 1.0f;
+      }
+      if (hit_ki) {
+        out[ACC_KIPUT] = put;
+        out[ACC_KIPUT2] = put * put;
+        out[ACC_NKI] = 1.0f;
+      }
+      if (received) {
+        out[ACC_CPN] = cn;
+        out[ACC_CPN2] = cn * cn;
+        out[ACC_NCPN] = 1.0f;
+      }
+      out[ACC_PUT] = put;
+      out[ACC_FUND] = funding;
+      out[ACC_CQ] = cpv * 10.0f;
+      out[ACC_MQ] = mpv * 10.0f;
+      out[ACC_NPUT] = put_ok ? 1.0f : 0.0f;
+      if (s == 0 && ko_steps) ko_steps[gi] = ko_step;
+      if (REC && s == 0 && records) {
+        const double df_mat = __ldg(tb.df_mat + s);
+        const double funding = ko ? __ldg(tb.df + (size_t)s * T + ko_step) : df_mat;
+        const double wf = exp((double)worst);
+        const double put = put_ok ? fmax(tr.strike - wf, 0.0) * df_mat : 0.0;
+        const double cn = (double)cpv + (double)mpv;
+        const double pv = funding + cn - put;
+        rg_path_record r;
+        r.path_id = path0 + gi;
+        r.rng_seed = tr.seed;
+        r.sobol_index = path0 + gi + 1;
+        r.worst_final = wf;
+        r.knocked_out = ko;
+        r.ko_step = ko_step;
+        r.ko_time = ko ? (double)(ko_step + 1) * tr.dt : __longlong_as_double(0x7ff8000000000000LL);
+        r.ki_hit = hit_ki;
+        r.qualified_steps = qualified;
+        r.paid_periods = paid;
+        r.put_payoff = put;
+        r.coupon_pv = cn;
+        r.memory_coupon_pv = (double)mpv;
+        r.funding = funding;
+        r.pv = pv;
+        records[gi] = r;
+      }
+    }
+    // the same FP32 butterfly over the warp's 32 paths as phoenix32.cu, then lane k keeps quantity k
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int k = 0; k < RG_ACC; ++k) out[k] += __shfl_xor_sync(0xffffffffu, out[k], off);
+    float mine = 0.0f;
+#pragma unroll
+    for (int k = 0; k < RG_ACC; ++k) mine = lane == k ? out[k] : mine;
+    lane_sum += (double)mine;
+  }
+  if (lane < RG_ACC) s_acc[wib][lane] = lane_sum;
+  __syncthreads();
+  // this CTA's sums per scenario, its warps added in warp order
+  for (int j = tid; j < S * RG_ACC; j += blockDim.x) {
+    const int ss = j / RG_ACC, k = j % RG_ACC;
+    double v = 0.0;
+    for (int w = 0; w < P32D_WARPS; ++w)
+      if ((blockIdx.x * P32D_WARPS + w) % S == ss) v += s_acc[w][k];
+    partial[(size_t)blockIdx.x * S * RG_ACC + j] = v;
+  }
+}
+
+template <int N, bool LV, bool REC>
+static void launch_n(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
+                     uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st) {
+  phoenix32d_kernel<N, LV, REC><<<grid, P32D_THREADS, 0, st>>>(
+      P.trade, tb, scen, scen32, P.n_scen, (float)P.ln_ko, (float)P.ln_cb, (float)P.ln_ki, path0, npaths,
+      out.partial, out.ko_steps, out.records);
+}
+
+// Grid of the direct kernel: enough warps for every (path group, scenario) pair up to a few waves
+// of resident CTAs, rounded so that the warp count is a multiple of the scenario count.
+int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count) {
+  const int S = P.n_scen;
+  if (S < 1 || S > 32) raise(RG_ERR_INVALID_ARGUMENT, "1 to 32 scenarios per fused launch");
+  int step = 1;  // CTAs per repeat of the scenario cycle: the smallest k with k·P32D_WARPS % S == 0
+  while ((step * P32D_WARPS) % S) ++step;
+  const uint64_t units = (npaths + 31) / 32 * (uint64_t)S;
+  uint64_t ctas = (units + P32D_WARPS - 1) / P32D_WARPS;
+  const uint64_t cap = (uint64_t)sm_count * 3 * 4;  // 3 resident CTAs per SM, 4 waves
+  if (ctas > cap) ctas = cap;
+  ctas = (ctas + step - 1) / step * step;
+  return (int)(ctas < 1 ? step : ctas);
+}
+
+void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
+                       uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st) {
+  const bool lv = P.trade.has_lv != 0, rec = out.records != nullptr;
+#define RG_CASE(NN)                                                                          \
+  case NN:                                                                                   \
+    if (lv) {                                                                                \
+      if (rec) launch_n<NN, true, true>(P, tb, scen, scen32, path0, npaths, grid, out, st);  \
+      else launch_n<NN, true, false>(P, tb, scen, scen32, path0, npaths, grid, out, st);     \
+    } else {                                                                                 \
+      if (rec) launch_n<NN, false, true>(P, tb, scen, scen32, path0, npaths, grid, out, st); \
+      else launch_n<NN, false, false>(P, tb, scen, scen32, path0, npaths, grid, out, st);    \
+    }                                                                                        \
+    break;
+  switch (P.n) {
+    RG_CASE(1) RG_CASE(2) RG_CASE(3) RG_CASE(4) RG_CASE(5)
+    default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
+  }
+#undef RG_CASE
+  cuda_check(cudaGetLastError(), "phoenix32d_kernel launch");
+}
+
+}  // namespace rg

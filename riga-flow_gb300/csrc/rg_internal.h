@@ -190,7 +190,13 @@ void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario*
                       uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);
 struct Fp32Shape {
   int Sb, Pb, TT, threads, grid, smem;
+  int direct;  // 1: the per-thread kernel of phoenix32d.cu (few scenarios), the other fields unused but grid/threads
 };
+// Scenario counts up to this value run on the direct kernel (phoenix32d.cu).
+constexpr int kP32DirectMaxScen = 2;
+int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
+void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
+                       uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
                       const DevScen32* scen32_dev, uint64_t path0, uint64_t npaths,

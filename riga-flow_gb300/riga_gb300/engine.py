@@ -48,6 +48,12 @@ class Engine:
         check(self.lib, self.lib.rg_price_put_leg(self.handle, a.ptr, C.byref(out)))
         return out
 
+    def last_timing(self) -> abi.Timing:
+        """Device-time breakdown of this engine's last call (rg_engine_last_timing)."""
+        tm = abi.Timing()
+        check(self.lib, self.lib.rg_engine_last_timing(self.handle, C.byref(tm)))
+        return tm
+
     def price_put_leg(self, request: PriceRequest) -> dict:
         return result_to_json(self.price_raw(request), request)
 

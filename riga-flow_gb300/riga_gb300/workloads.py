@@ -12,6 +12,11 @@
   +1 vol point per asset, +1bp rate, two cross-gamma corners (+1%, +1%) on pairs (0,1) and (0,2),
   −1 vol point per asset).
 
+* ``lv5_large`` — the large fused run: a 5-asset worst-of Phoenix (same terms, 5y, 1260 daily
+  steps, 20 quarterly coupons) under Dupire local vol, seeded SVI smiles (SplitMix64 seed 5) on
+  64 log-moneyness × 32 expiries with a 64-point Dupire grid, correlation from a seeded 2-factor
+  model (the book's loading rule), 2^24 Sobol or Halton points.
+
 There is no public dataset or evaluation suite for this path; these seeded inputs stand in for
 the configurations' shapes, sizes and value distributions.
 """
@@ -104,6 +109,23 @@ def lv3(paths: int = 1 << 20, steps: int = 756, fp32: bool = True) -> PriceReque
     req.options = production_options(40) if fp32 else EngineOptions(
         scrambler=abi.SCRAMBLE_DIGITAL_SHIFT, precision=abi.PRECISION_FP64_PARITY,
         dim_mode=abi.DIM_FULL, lv_grid_x=40)
+    return req
+
+
+def lv5_large(paths: int = 1 << 24, steps: int = 1260, fp32: bool = True, kind: str = "sobol") -> PriceRequest:
+    n = 5
+    as_of = "2026-01-02"
+    years = 5.0 * steps / 1260
+    grids, _ = svi_grids(n, seed=5, n_k=64, n_t=32, years=years)
+    corr = book_universe(n_assets=n, n_factors=2, seed=4, as_of=as_of).correlation
+    req = PriceRequest(
+        trade=phoenix_trade(n, steps, years, "lv5_large"),
+        market=MarketSnapshot(as_of, [100.0] * n, [0.25] * n, 0.03, [0.01] * n, corr),
+        config=SimulationConfig(paths, 4096, 1, "off", VarianceReduction(kind, n * steps)),
+        as_of=as_of, local_vol=grids)
+    req.options = production_options(64) if fp32 else EngineOptions(
+        scrambler=abi.SCRAMBLE_DIGITAL_SHIFT, precision=abi.PRECISION_FP64_PARITY,
+        dim_mode=abi.DIM_FULL, lv_grid_x=64)
     return req
 
 

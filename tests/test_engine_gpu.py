@@ -240,6 +240,54 @@ def test_fp32_crn_batch_matches_fp64_scenarios(engine):
         assert abs(dg - de) <= _fp32_bound(exp[0]), (i, dg, de)
 
 
+@pytest.mark.parametrize("steps,n_scen", [(1, 1), (2, 16), (5, 1), (63, 16), (64, 3), (65, 16),
+                                          (129, 32), (300, 1), (1000, 16)])
+def test_fp32_time_tiles_at_awkward_step_counts(engine, steps, n_scen):
+    """The FP32 kernel walks time in subtrees of the bridge's bisection tree; step counts around
+    and between the tile sizes, and 1-32 scenarios (256- and 1024-thread blocks, 32-256 paths per
+    CTA), all price within the FP32 bound of the FP64 oracle.  One step makes every path pay the
+    same (standard error 0), so the bound has a floor of 1e-7 of notional, about FP32's
+    resolution at 1."""
+    r = workloads.plain3(2048, steps=steps, fp32=True)
+    r.trade.coupon_periods = max(1, min(12, steps // 3))
+    r.trade.call_start_step = min(63, steps // 2)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(r)]
+    scen = (scen * 2)[:n_scen]
+    got = engine.price_scenarios_raw(r, scen)
+    r64 = copy.deepcopy(r)
+    r64.options.precision = abi.PRECISION_FP64_PARITY
+    exp = O.price_scenarios(r64, scen, threads=8)
+    for i, (g, e) in enumerate(zip(got, exp)):
+        bound = max(_fp32_bound(e), 1e-7)
+        assert abs(g.pv - e.pv) <= bound, (i, g.pv, e.pv, bound)
+
+
+def test_large_fused_config_fp64_parity():
+    """The large fused configuration's shape (5 assets, 64x32 SVI smiles, 64-point Dupire grid,
+    2-factor correlation, 1260 steps) in the FP64 parity kernel, per path against the oracle."""
+    eng = Engine(0)
+    try:
+        r = workloads.lv5_large(paths=128, fp32=False)
+        assert_records_match(eng.run_paths_raw(r, 0, 128), O.run_paths(r, 0, 128))
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("kind", ["sobol", "halton"])
+def test_large_fused_config_fp32_within_bound(engine, kind):
+    """FP32 production kernel on the large configuration (Sobol, and the Halton cross-check
+    points) within min(0.1 SE, 1bp) of FP64 on the same 2^16 points.  The FP64 side is the parity
+    kernel, whose per-path equality with the oracle on this shape is the test above: at a few
+    thousand paths one knock-out event flipped by FP32 rounding moves the price by more than 1bp,
+    so the bound needs a path count the CPU oracle cannot price within a test."""
+    r = workloads.lv5_large(paths=1 << 16, kind=kind)
+    r64 = workloads.lv5_large(paths=1 << 16, fp32=False, kind=kind)
+    got = engine.price_raw(r)
+    exp = engine.price_raw(r64)
+    bound = _fp32_bound(exp)
+    assert abs(got.pv - exp.pv) <= bound, (got.pv, exp.pv, bound)
+
+
 def test_fp64_risk_batch_matches_the_oracle(engine, termsheet1):
     """crates/riga-risk/src/lib.rs:573-626 on the device: every scenario price within 1e-12."""
     r = _termsheet(termsheet1, 512)
