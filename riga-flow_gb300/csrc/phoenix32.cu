@@ -1,7 +1,8 @@
 // phoenix32.cu — the FP32 production kernel: one fused launch prices S common-random-number
 // scenarios of one trade.
 //
-// A CTA owns Pb consecutive paths × Sb scenario slots (Sb = S rounded up to a power of two); thread
+// A CTA owns Pb consecutive paths × Sb scenario slots (Sb = S rounded up to a power of two, at least
+// 4; a single scenario runs on the direct kernel of phoenix32d.cu); thread
 // t serves scenario t / Pb and path t % Pb, so a warp is 32 paths of one scenario and its
 // local-vol lookups all read one surface.  Time is walked in tiles of TT steps, each in three
 // phases separated by CTA barriers:
@@ -403,24 +404,32 @@ static const void* select_kernel(int n, bool lv, bool rec) {
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
   if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
-  if (P.n_scen <= kP32DirectMaxScen) {
+  if (P.n_scen <= kP32DirectMaxScen && npaths >= p32_direct_min_paths(P.n)) {
     // nothing for the scenarios to share: the per-thread kernel without shared-memory tiles
     sh.direct = 1;
     sh.Sb = P.n_scen;
     sh.threads = 256;
     sh.grid = phoenix32d_grid(P, npaths, sm_count);
+    sh.smem = P.stack_max * P.n * 256 * (int)sizeof(float);  // the bridge stacks (dynamic)
     return sh;
   }
-  int sb = 1;
+  // scenario slots: S rounded up to a power of two, at least 4 (two scenarios run padded: a CTA
+  // of 1024 threads on half the slots beats both the direct kernel and a smaller CTA); the
+  // largest block of 1024, 512 or 256 threads whose shared-memory layout fits
+  int sb = 4;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
-  sh.threads = sb >= 8 ? 1024 : 256;
-  sh.Pb = sh.threads / sb;
-  const int N = P.n, PbN = sh.Pb * N;
-  int tt = (32768 / PbN - P.stack_max) / 2;
-  tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
-  sh.TT = tt;
-  sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
+  const int N = P.n;
+  for (int threads = 1024; threads >= 256; threads >>= 1) {
+    sh.threads = threads;
+    sh.Pb = threads / sb;
+    const int PbN = sh.Pb * N;
+    int tt = (32768 / PbN - P.stack_max) / 2;
+    tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
+    sh.TT = tt;
+    sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, threads).total;
+    if (sh.smem <= 227 * 1024 || threads == 256) break;
+  }
   // Function attributes are process-wide: raise every instantiation's dynamic shared-memory limit
   // to the device maximum once, so engines pricing concurrently never lower it under each other.
   {

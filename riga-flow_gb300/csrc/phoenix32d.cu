@@ -1,17 +1,20 @@
-// phoenix32d.cu — the FP32 kernel for launches with few CRN scenarios: one thread per (path,
-// scenario), everything in registers, no shared-memory time tiles and no CTA barriers.
+// phoenix32d.cu — the FP32 kernel for single-scenario launches: one thread per (path, scenario),
+// everything in registers, no shared-memory time tiles and no CTA barriers.
 //
 // The tiled kernel (phoenix32.cu) stages a tile's normals and Brownian increments in shared
-// memory so that the scenarios of a path share one generation; with one or two scenarios there is
-// nothing to share and the staging costs occupancy (a 5-asset single-scenario launch fits one
-// 256-thread CTA per SM).  Here a warp walks 32 consecutive paths of one scenario through time:
+// memory so that the scenarios of a path share one generation; with one scenario there is nothing
+// to share and the staging only costs occupancy.  (Measured on the 3-asset local-vol trade at 2^20
+// paths: 17.5 ms here against 24.4 ms for the tiled kernel on four padded scenario slots; the
+// tiled kernel wins with two or more scenarios, and below about 2^18 paths, where one path per
+// thread leaves too few warps to hide the per-step latency.)  Here a warp walks 32 consecutive
+// paths of one scenario through time:
 //   * Sobol points by warp cooperation: x(n) for the warp's first point is the XOR of the
 //     direction numbers at the set bits of its Gray code (lane k contributes bit k, a shuffle
 //     reduction), and the other lanes' points follow by the Gray recurrence
 //     x(n) = x(n-1) ^ v[ctz(n)] as an inclusive XOR scan over the lanes;
 //   * the digital shift (or Owen scramble) and the FP32 inverse normal of rg_common.cuh;
-//   * the streamed Brownian bridge per factor with its anchor stack in thread-local memory (the
-//     stack depth is warp-uniform, so every access is one coalesced line);
+//   * the streamed Brownian bridge per factor with its anchor stack in shared memory, laid out
+//     [depth][factor][thread] so that a warp's accesses (the depth is warp-uniform) hit 32 banks;
 //   * the correlation with the scenario's Cholesky factor, the log-space GBM / Dupire step and the
 //     Phoenix state machine.
 // Every operation of the per-path arithmetic is the one phoenix32.cu performs, in the same order,
@@ -50,6 +53,7 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
     rg_path_record* __restrict__ records) {
   __shared__ float4 s_lv[32 * RG_NMAX];
   __shared__ double s_acc[P32D_WARPS][RG_ACC];
+  extern __shared__ float s_stk[];  // [stack depth][N][P32D_THREADS]
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
   const int T = (int)tr.steps;
   const int gx = tr.gx;
@@ -91,7 +95,8 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
     const uint64_t gi = grp * 32 + lane;
     const bool ok = gi < npaths;
     const uint64_t n1 = path0 + grp * 32 + 1;  // Sobol point of the warp's first path
-    float x[N], wcur[N], stk[RG_STACK_MAX][N];
+    float x[N], wcur[N];
+    float* const stk = s_stk + tid;  // entry (depth d, factor f) at stk[(d * N + f) * P32D_THREADS]
 #pragma unroll
     for (int f = 0; f < N; ++f) {
       x[f] = lvc[f].w;
@@ -119,7 +124,8 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
           } else {
             z = (float)rg_qmc_normal64(tr, tb, path0 + gi, (uint64_t)__ldg(tb.node_k + c) * N + f);
           }
-          stk[sp][f] = c == 0 ? z * cf : fmaf(z, cf, 0.5f * (wcur[f] + stk[sp - 1][f]));
+          stk[(sp * N + f) * P32D_THREADS] =
+              c == 0 ? z * cf : fmaf(z, cf, 0.5f * (wcur[f] + stk[((sp - 1) * N + f) * P32D_THREADS]));
         }
         ++sp;
       }
@@ -127,7 +133,7 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
       float d[N], y[N];
 #pragma unroll
       for (int f = 0; f < N; ++f) {
-        const float wn = stk[sp][f];
+        const float wn = stk[(sp * N + f) * P32D_THREADS];
         d[f] = wn - wcur[f];
         wcur[f] = wn;
       }
@@ -282,12 +288,33 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
   }
 }
 
+static size_t stack_bytes(const Prepared& P) {
+  return (size_t)P.stack_max * P.n * P32D_THREADS * sizeof(float);
+}
+
 template <int N, bool LV, bool REC>
 static void launch_n(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                      uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st) {
-  phoenix32d_kernel<N, LV, REC><<<grid, P32D_THREADS, 0, st>>>(
+  phoenix32d_kernel<N, LV, REC><<<grid, P32D_THREADS, stack_bytes(P), st>>>(
       P.trade, tb, scen, scen32, P.n_scen, (float)P.ln_ko, (float)P.ln_cb, (float)P.ln_ki, path0, npaths,
       out.partial, out.ko_steps, out.records);
+}
+
+template <int N, bool LV>
+static const void* kernel_ptr(bool rec) {
+  return rec ? reinterpret_cast<const void*>(&phoenix32d_kernel<N, LV, true>)
+             : reinterpret_cast<const void*>(&phoenix32d_kernel<N, LV, false>);
+}
+
+static const void* select_kernel(int n, bool lv, bool rec) {
+  switch (n) {
+    case 1: return lv ? kernel_ptr<1, true>(rec) : kernel_ptr<1, false>(rec);
+    case 2: return lv ? kernel_ptr<2, true>(rec) : kernel_ptr<2, false>(rec);
+    case 3: return lv ? kernel_ptr<3, true>(rec) : kernel_ptr<3, false>(rec);
+    case 4: return lv ? kernel_ptr<4, true>(rec) : kernel_ptr<4, false>(rec);
+    case 5: return lv ? kernel_ptr<5, true>(rec) : kernel_ptr<5, false>(rec);
+    default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
+  }
 }
 
 // Grid of the direct kernel: enough warps for every (path group, scenario) pair up to a few waves
@@ -295,11 +322,38 @@ static void launch_n(const Prepared& P, const DevTables& tb, const DevScenario* 
 int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count) {
   const int S = P.n_scen;
   if (S < 1 || S > 32) raise(RG_ERR_INVALID_ARGUMENT, "1 to 32 scenarios per fused launch");
+  // function attributes are process-wide: raise every instantiation's dynamic shared-memory limit
+  // to the device maximum once, so concurrent engines never lower it under each other
+  {
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (!done[dev]) {
+      int optin = 0;
+      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem opt-in");
+      const int dyn = optin - (int)(sizeof(float4) * 32 * RG_NMAX + sizeof(double) * P32D_WARPS * RG_ACC);
+      for (int n = 1; n <= RG_NMAX; ++n)
+        for (int lv = 0; lv < 2; ++lv)
+          for (int rec = 0; rec < 2; ++rec)
+            cuda_check(cudaFuncSetAttribute(select_kernel(n, lv != 0, rec != 0),
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, dyn),
+                       "phoenix32d smem attribute");
+      done[dev] = 1;
+    }
+  }
+  int per_sm = 0;
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel(P.n, P.trade.has_lv != 0, false),
+                                                           P32D_THREADS, stack_bytes(P)),
+             "phoenix32d occupancy");
+  if (per_sm < 1) raise(RG_ERR_GPU_ERROR, "phoenix32d: launch shape does not fit on an SM");
   int step = 1;  // CTAs per repeat of the scenario cycle: the smallest k with k·P32D_WARPS % S == 0
   while ((step * P32D_WARPS) % S) ++step;
   const uint64_t units = (npaths + 31) / 32 * (uint64_t)S;
   uint64_t ctas = (units + P32D_WARPS - 1) / P32D_WARPS;
-  const uint64_t cap = (uint64_t)sm_count * 3 * 4;  // 3 resident CTAs per SM, 4 waves
+  const uint64_t cap = (uint64_t)sm_count * per_sm * 4;  // up to 4 waves of resident CTAs
   if (ctas > cap) ctas = cap;
   ctas = (ctas + step - 1) / step * step;
   return (int)(ctas < 1 ? step : ctas);

@@ -190,10 +190,13 @@ void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario*
                       uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);
 struct Fp32Shape {
   int Sb, Pb, TT, threads, grid, smem;
-  int direct;  // 1: the per-thread kernel of phoenix32d.cu (few scenarios), the other fields unused but grid/threads
+  int direct;  // 1: the per-thread kernel of phoenix32d.cu; then only grid and threads are used
 };
-// Scenario counts up to this value run on the direct kernel (phoenix32d.cu).
-constexpr int kP32DirectMaxScen = 2;
+// Scenario counts up to this value run on the direct kernel (phoenix32d.cu), when the launch has
+// at least p32_direct_min_paths(n) paths: one path per thread needs enough warps to fill the GPU
+// (measured crossover against the tiled kernel: about 2^18 paths for 1-3 assets, 2^16 for 4-5).
+constexpr int kP32DirectMaxScen = 1;
+inline uint64_t p32_direct_min_paths(int n) { return n >= 4 ? (uint64_t(1) << 16) : (uint64_t(3) << 16); }
 int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                        uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);

@@ -262,6 +262,33 @@ def test_fp32_time_tiles_at_awkward_step_counts(engine, steps, n_scen):
         assert abs(g.pv - e.pv) <= bound, (i, g.pv, e.pv, bound)
 
 
+@pytest.mark.parametrize("n,lv", [(1, False), (3, False), (3, True), (5, True)])
+def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv):
+    """A single scenario at 2^18 paths runs on the direct kernel (one path per thread); the same
+    scenario twice runs on the tiled kernel.  Both compute every path's FP32 payoff with the same
+    operations in the same order and sum warps of 32 paths by the same butterfly, so the prices
+    agree to FP64 summation order (1e-12 relative)."""
+    if lv:
+        r = workloads.lv5_large(paths=1 << 18, steps=252) if n == 5 else workloads.lv3(paths=1 << 18, steps=252)
+    else:
+        r = workloads.plain3(1 << 18, steps=252, fp32=True)
+        if n != 3:
+            r.trade.initial_spots = [100.0] * n
+            r.market.spots = [100.0 + 3 * i for i in range(n)]
+            r.market.vols = [0.2 + 0.03 * i for i in range(n)]
+            r.market.dividend_yields = [0.01] * n
+            r.market.correlation = [[1.0 if i == j else 0.3 for j in range(n)] for i in range(n)]
+            r.config.variance_reduction = VarianceReduction("sobol", n * 252)
+    one = engine.price_raw(r)
+    assert engine.last_timing().smem_bytes < 64 * 1024 and engine.last_timing().block == 256
+    base = (copy.deepcopy(r.market), [0.0] * n)
+    two = engine.price_scenarios_raw(r, [base, base])
+    assert engine.last_timing().block == 1024
+    for t in two:
+        assert abs(t.pv - one.pv) <= 1e-12 * abs(one.pv), (t.pv, one.pv)
+        assert t.ki_probability == one.ki_probability
+
+
 def test_large_fused_config_fp64_parity():
     """The large fused configuration's shape (5 assets, 64x32 SVI smiles, 64-point Dupire grid,
     2-factor correlation, 1260 steps) in the FP64 parity kernel, per path against the oracle."""
