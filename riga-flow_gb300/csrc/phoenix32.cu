@@ -404,7 +404,7 @@ static const void* select_kernel(int n, bool lv, bool rec) {
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
   if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
-  if (P.n_scen <= kP32DirectMaxScen && npaths >= p32_direct_min_paths(P.n)) {
+  if (p32_direct(P, npaths)) {
     // nothing for the scenarios to share: the per-thread kernel without shared-memory tiles
     sh.direct = 1;
     sh.Sb = P.n_scen;

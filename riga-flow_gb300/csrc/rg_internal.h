@@ -197,6 +197,9 @@ struct Fp32Shape {
 // (measured crossover against the tiled kernel: about 2^18 paths for 1-3 assets, 2^16 for 4-5).
 constexpr int kP32DirectMaxScen = 1;
 inline uint64_t p32_direct_min_paths(int n) { return n >= 4 ? (uint64_t(1) << 16) : (uint64_t(3) << 16); }
+inline bool p32_direct(const Prepared& P, uint64_t npaths) {
+  return P.n_scen <= kP32DirectMaxScen && npaths >= p32_direct_min_paths(P.n);
+}
 int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                        uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);
