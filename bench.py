@@ -394,13 +394,13 @@ def run_gpu(args):
     fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
     kern_avg_s = statistics.mean(ker_ms) / 1e3
     achieved = flops_per_launch(P, T, 3, n_scen) / kern_avg_s / 1e12
+    # DRAM bytes per launch of the fused kernel, from the committed ncu capture at this size
     traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get("phoenix32_lv3_bytes_per_launch")
-        except Exception:
-            traffic = None
+    tfile = ROOT / "profiles" / "phoenix32_lv3_crn16_dram.md"
+    if tfile.exists() and P == 1 << 20 and T == 756 and n_scen == 16:
+        for ln in tfile.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
     clocks = clk.summary()
     tm = timings[-1]
     line = {
@@ -438,7 +438,7 @@ def run_gpu(args):
         book["throughput_vs_fp64_plain"] = book["path_steps_per_s"] / plain
         line["book"] = book
     if world == 1 and not args.no_large:
-        line["large"] = large_measure(eng)
+        line["large"] = large_measure(eng, paths=args.large_paths, sample_paths=min(1 << 16, args.large_paths))
     if world == 1 and not args.no_serving:
         line["serving"] = serving_measure()
     if world == 1 and not args.no_cpu_baseline:
@@ -464,6 +464,7 @@ def main():
     ap.add_argument("--no-large", action="store_true", help="skip the large fused (cfg 4) measurement")
     ap.add_argument("--only", choices=["book", "serving", "large"], default=None,
                     help="run one secondary measurement alone (for profiling) and print its JSON")
+    ap.add_argument("--large-paths", type=int, default=1 << 24, help="paths of the large fused (cfg 4) run")
     ap.add_argument("--book-trades", type=int, default=4096)
     ap.add_argument("--book-paths", type=int, default=1 << 18)
     args = ap.parse_args()
@@ -478,7 +479,8 @@ def main():
         if args.only == "book":
             print(json.dumps(book_measure(Engine(0), args.book_trades, args.book_paths)), flush=True)
         elif args.only == "large":
-            print(json.dumps(large_measure(Engine(0))), flush=True)
+            print(json.dumps(large_measure(Engine(0), paths=args.large_paths,
+                                           sample_paths=min(1 << 16, args.large_paths))), flush=True)
         else:
             print(json.dumps(serving_measure()), flush=True)
         return
