@@ -424,7 +424,8 @@ def run_gpu(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(tm.h2d_bytes),
                 "d2h_bytes_per_step": int(tm.d2h_bytes)},
         "gpu_launches": int(tm.kernel_launches) * args.steps,
-        "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes},
+        "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes,
+                   "tile_steps": tm.tile_steps, "tile_steps_from": "autotuner (rg_set_autotune), tuned during warm-up"},
         "clocks": clocks,
     }
     if merged_pv is not None:

@@ -316,8 +316,17 @@ typedef struct rg_timing {
   uint64_t h2d_bytes, d2h_bytes;
   int32_t kernel_launches; /* kernels this call launched (prologue + fused + reduce) */
   int32_t grid, block, smem_bytes; /* launch shape of the fused kernel */
+  int32_t tile_steps; /* steps per time tile of the tiled FP32 kernel (0 for the other kernels) */
 } rg_timing;
 int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
+
+/* The FP32 kernel's step-tiling autotuner (on by default, process-wide).  The first pricing call
+ * of a launch shape (asset count, local vol, scenario slots, steps, QMC lane, grid width) with at
+ * least eight waves of path tiles times the candidate tile depths on a prefix of its paths and
+ * keeps the fastest for that shape; later calls reuse it.  The tile depth changes the schedule,
+ * not the arithmetic, so prices are the same with the autotuner on or off.  Calls through
+ * rg_price_put_leg_static never tune.  Disabling also clears the tuned depths. */
+int32_t rg_set_autotune(int32_t enabled);
 
 /* explain::run_paths restricted to [first_path, first_path + count),
  * crates/riga-engine/src/explain.rs:90-316 (reconstruct_path :319-333 is count == 1). */

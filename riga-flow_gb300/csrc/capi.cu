@@ -468,6 +468,7 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     }
     const uint64_t path0 = req->config.first_path;
     if (fp32) {
+      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.may_tune(), W.stream);
       launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.stream);
     } else {
       launch_phoenix64(P, S.tb, S.scen, path0, paths, lo, W.stream);
@@ -475,6 +476,7 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     if (W.timing) {
       W.timing->block = fp32 ? sh.threads : 128;
       W.timing->smem_bytes = fp32 ? sh.smem : 0;
+      W.timing->tile_steps = fp32 && !sh.direct ? sh.TT : 0;
       W.timing->grid = grid;
       W.timing->kernel_launches += 2;
       W.timing->d2h_bytes += sums_bytes;
@@ -760,8 +762,10 @@ static void run_path_range(rg_engine* e, const rg_price_request* req, uint64_t f
     if (out) lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, m * sizeof(rg_path_record)));
     if (cube) lo.cube = static_cast<float*>(W.device(WS_CUBE, m * cube_row * sizeof(float)));
     const uint64_t path0 = req->config.first_path + first + done;
-    if (fp32)
+    if (fp32) {
+      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, false, e->stream);  // cached depth only
       launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, e->stream);
+    }
     else
       launch_phoenix64(P, S.tb, S.scen, path0, m, lo, e->stream);
     if (out)
@@ -791,6 +795,10 @@ extern "C" int32_t rg_materialize_paths(rg_engine* e, const rg_price_request* re
     validate_request(req);
     run_path_range(e, req, first, count, records, cube);
   })
+}
+
+extern "C" int32_t rg_set_autotune(int32_t enabled) {
+  RG_TRY({ p32_set_autotune(enabled != 0); })
 }
 
 extern "C" int32_t rg_sobol_directions(int64_t dim, uint32_t* out) {

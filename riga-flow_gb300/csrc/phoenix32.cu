@@ -22,6 +22,11 @@
 // launch of a given shape is bit-reproducible.  With 16 scenarios a CTA is 1024 threads (64 paths
 // × 16 scenarios, one CTA per SM): each scenario has two warps on the same paths, which share
 // its local-vol rows in L1.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
 #include "rg_internal.h"
 
 namespace rg {
@@ -464,6 +469,87 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   sh.grid = (int)(tiles < cap ? tiles : cap);
   if (sh.grid < 1) sh.grid = 1;
   return sh;
+}
+
+// ---------------------------------------------------------------------- tile-depth autotuner --
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<int64_t>, int> g_tuned;  // launch shape -> tile depth
+bool g_tune_enabled = true;
+
+// Sets the tile depth of a tiled-kernel shape if its layout fits next to the same block size.
+bool p32_with_tt(const Prepared& P, Fp32Shape& sh, int tt) {
+  const int smem = (int)p32_layout(P.n_scen, P.n, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
+  if (smem > 227 * 1024) return false;
+  sh.TT = tt;
+  sh.smem = smem;
+  return true;
+}
+}  // namespace
+
+void p32_set_autotune(bool enabled) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_enabled = enabled;
+  g_tuned.clear();
+}
+
+Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
+                         const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
+                         const LaunchOut& out, bool may_tune, cudaStream_t st) {
+  // only the 1024-thread shapes, which hold one CTA per SM whatever the tile depth (the grid, the
+  // partial-sum buffer and the block's path grouping stay as they are)
+  if (sh.direct || sh.threads != 1024) return sh;
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  const std::vector<int64_t> key{dev, P.n, P.trade.has_lv, P.n_scen, sh.Sb, P.T, P.stack_max,
+                                 P.trade.vr, P.trade.scrambler, P.trade.gx};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (!g_tune_enabled) return sh;
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      Fp32Shape t = sh;
+      if (p32_with_tt(P, t, it->second)) t.tuned = 1;
+      return t.tuned ? t : sh;
+    }
+  }
+  // a tuning pass costs about (candidates × 2) launches over two waves of tiles: only for
+  // launches of at least eight waves
+  const uint64_t prefix = (uint64_t)sh.grid * (uint64_t)sh.Pb * 2;
+  if (!may_tune || npaths < prefix * 4) return sh;
+  std::vector<int> cand;
+  for (int tt : {sh.TT, 24, 32, 48, 64, 80, 96, 128}) {
+    Fp32Shape c = sh;
+    if (std::find(cand.begin(), cand.end(), tt) == cand.end() && p32_with_tt(P, c, tt)) cand.push_back(tt);
+  }
+  LaunchOut lo = out;  // the partial sums are overwritten by the real launch afterwards
+  lo.ko_steps = nullptr;
+  lo.records = nullptr;
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event");
+  cuda_check(cudaEventCreate(&e1), "event");
+  std::vector<float> best(cand.size(), 1e30f);
+  for (int rep = 0; rep < 2; ++rep)
+    for (size_t i = 0; i < cand.size(); ++i) {
+      Fp32Shape c = sh;
+      p32_with_tt(P, c, cand[i]);
+      cuda_check(cudaEventRecord(e0, st), "event");
+      launch_phoenix32(P, tb, scen, scen32, path0, prefix, c, lo, st);
+      cuda_check(cudaEventRecord(e1, st), "event");
+      cuda_check(cudaEventSynchronize(e1), "autotune");
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event time");
+      best[i] = std::min(best[i], ms);
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const size_t win = (size_t)(std::min_element(best.begin(), best.end()) - best.begin());
+  Fp32Shape t = sh;
+  p32_with_tt(P, t, cand[win]);
+  t.tuned = 1;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[key] = cand[win];
+  return t;
 }
 
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen,

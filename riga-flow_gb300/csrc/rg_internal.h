@@ -136,6 +136,9 @@ struct Workspace {
   virtual void* host(size_t bytes) = 0;  // landing area of the FP64 sums
   // whether slots keep their contents across fused launches (false for a bump allocator)
   virtual bool persistent() const { return true; }
+  // whether extra timed launches (the tile-depth autotuner) may run on this stream; not for the
+  // static entry point, which may be called under stream capture
+  virtual bool may_tune() const { return true; }
   virtual ~Workspace() = default;
 };
 // validate → host tables → H2D → prologue → fused kernel → reduce → D2H → PriceResults
@@ -190,6 +193,7 @@ void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario*
                       uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);
 struct Fp32Shape {
   int Sb, Pb, TT, threads, grid, smem;
+  int tuned;   // 1: TT came from the autotuner's cache
   int direct;  // 1: the per-thread kernel of phoenix32d.cu; then only grid and threads are used
 };
 // Scenario counts up to this value run on the direct kernel (phoenix32d.cu), when the launch has
@@ -204,6 +208,15 @@ int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                        uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count);
+// The tiled kernel's step tiling from the autotuner: a cached choice for the launch's shape, or —
+// when `may_tune` and the launch is large enough to amortise it — one tuning pass that times the
+// candidate tile depths on a prefix of the paths (their results are discarded; the tile depth
+// changes the schedule, never the arithmetic) and caches the fastest.  Returns `sh` with TT set.
+// Enables or disables the autotuner process-wide; either way its cache is cleared.
+void p32_set_autotune(bool enabled);
+Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
+                         const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
+                         const LaunchOut& out, bool may_tune, cudaStream_t st);
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
                       const DevScen32* scen32_dev, uint64_t path0, uint64_t npaths,
                       const Fp32Shape& shape, const LaunchOut& out, cudaStream_t s);

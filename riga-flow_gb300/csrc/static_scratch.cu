@@ -36,6 +36,7 @@ struct StaticWorkspace : rg::Workspace {
   double sums[RG_MAX_SCEN * RG_ACC];
   void begin_launch() override { off = 0; }
   bool persistent() const override { return false; }
+  bool may_tune() const override { return false; }
   void* device(int slot, size_t bytes) override {
     (void)slot;
     const size_t o = (off + 255) & ~(size_t)255;

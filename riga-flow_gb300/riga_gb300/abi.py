@@ -185,7 +185,7 @@ class Timing(C.Structure):
                 ("reduce_ms", C.c_double), ("d2h_ms", C.c_double), ("device_ms", C.c_double),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("kernel_launches", C.c_int32), ("grid", C.c_int32), ("block", C.c_int32),
-                ("smem_bytes", C.c_int32)]
+                ("smem_bytes", C.c_int32), ("tile_steps", C.c_int32)]
 
 
 class Scenario(C.Structure):
@@ -332,6 +332,7 @@ SIGNATURES = {
                                     C.POINTER(PathRecord)]),
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
+    "rg_set_autotune": (_i32, [_i32]),
     "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
                              C.POINTER(PriceResult)]),
     "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,

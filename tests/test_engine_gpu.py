@@ -289,6 +289,27 @@ def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv):
         assert t.ki_probability == one.ki_probability
 
 
+def test_autotuned_tile_depth_keeps_prices(engine):
+    """The step-tiling autotuner changes the tiled kernel's time-tile depth, never its arithmetic:
+    16 CRN scenarios priced with the autotuner off (the default depth), then on (the first call
+    tunes, the second reuses the tuned depth) are identical byte for byte."""
+    lib = engine.lib
+    r = workloads.lv3(paths=1 << 19, steps=252)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(r)]
+    abi.check(lib, lib.rg_set_autotune(0))
+    try:
+        off = engine.price_scenarios_raw(r, scen)
+        t_off = engine.last_timing().tile_steps
+    finally:
+        abi.check(lib, lib.rg_set_autotune(1))
+    first = engine.price_scenarios_raw(r, scen)
+    second = engine.price_scenarios_raw(r, scen)
+    t_on = engine.last_timing().tile_steps
+    assert t_off > 0 and t_on in (t_off, 24, 32, 48, 64, 80, 96, 128)
+    for a, b, c in zip(off, first, second):
+        assert bytes(a) == bytes(b) == bytes(c)
+
+
 def test_large_fused_config_fp64_parity():
     """The large fused configuration's shape (5 assets, 64x32 SVI smiles, 64-point Dupire grid,
     2-factor correlation, 1260 steps) in the FP64 parity kernel, per path against the oracle."""
