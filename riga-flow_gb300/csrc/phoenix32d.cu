@@ -23,6 +23,7 @@
 // by the same FP32 shuffle butterfly; above that, lane k of each warp keeps an FP64 running sum of
 // quantity k over the warp's path groups, and each CTA adds its warps' sums in warp order, so a
 // launch of a given shape is bit-reproducible.
+#include "p32_path.cuh"
 #include "rg_internal.h"
 
 namespace rg {
@@ -235,66 +236,8 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
     }
     // path close (note.rs:221-258)
     float out[RG_ACC];
-#pragma unroll
-    for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0f;
-    if (ok) {
-      const bool ko = ko_step >= 0;
-      const float df_mat = (float)__ldg(tb.df_mat + s);
-      const float funding = ko ? (float)__ldg(tb.df + (size_t)s * T + ko_step) : df_mat;
-      const bool hit_ki = worst <= ln_ki;
-      const bool put_ok = hit_ki && !ko;
-      const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * df_mat : 0.0f;
-      const float cn = cpv + mpv;
-      const float pv1 = (funding - 1.0f) + cn - put;
-      out[ACC_PV] = pv1;
-      out[ACC_PV2] = pv1 * pv1;
-      if (ko) {
-        out[ACC_KOF] = funding - 1.0f;
-        out[ACC_KOF2] = (funding - 1.0f) * (funding - 1.0f);
-        out[ACC_NKO] = 1.0f;
-      }
-      if (hit_ki) {
-        out[ACC_KIPUT] = put;
-        out[ACC_KIPUT2] = put * put;
-        out[ACC_NKI] = 1.0f;
-      }
-      if (received) {
-        out[ACC_CPN] = cn;
-        out[ACC_CPN2] = cn * cn;
-        out[ACC_NCPN] = 1.0f;
-      }
-      out[ACC_PUT] = put;
-      out[ACC_FUND] = funding;
-      out[ACC_CQ] = cpv * 10.0f;
-      out[ACC_MQ] = mpv * 10.0f;
-      out[ACC_NPUT] = put_ok ? 1.0f : 0.0f;
-      if (s == 0 && ko_steps) ko_steps[gi] = ko_step;
-      if (REC && s == 0 && records) {
-        const double df_mat = __ldg(tb.df_mat + s);
-        const double funding = ko ? __ldg(tb.df + (size_t)s * T + ko_step) : df_mat;
-        const double wf = exp((double)worst);
-        const double put = put_ok ? fmax(tr.strike - wf, 0.0) * df_mat : 0.0;
-        const double cn = (double)cpv + (double)mpv;
-        const double pv = funding + cn - put;
-        rg_path_record r;
-        r.path_id = path0 + gi;
-        r.rng_seed = tr.seed;
-        r.sobol_index = path0 + gi + 1;
-        r.worst_final = wf;
-        r.knocked_out = ko;
-        r.ko_step = ko_step;
-        r.ko_time = ko ? (double)(ko_step + 1) * tr.dt : __longlong_as_double(0x7ff8000000000000LL);
-        r.ki_hit = hit_ki;
-        r.qualified_steps = qualified;
-        r.paid_periods = paid;
-        r.put_payoff = put;
-        r.coupon_pv = cn;
-        r.memory_coupon_pv = (double)mpv;
-        r.funding = funding;
-        r.pv = pv;
-        records[gi] = r;
-      }
-    }
+    p32_close_path<REC>(tr, tb, s, T, ok, s == 0, path0, gi, ko_step, worst, ln_ki, cpv, mpv, received,
+                        qualified, paid, ko_steps, records, out);
     // the same FP32 butterfly over the warp's 32 paths as phoenix32.cu, then lane k keeps quantity k
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
