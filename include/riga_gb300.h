@@ -424,6 +424,9 @@ typedef struct rg_server_config {
   int32_t device;
   int32_t slots;                 /* concurrent requests (engines); 0 = 4 */
   uint64_t device_memory_budget; /* bytes for the slots' workspaces; 0 = 80% of free memory */
+  int32_t max_large_slots;       /* slots large requests may hold at once; 0 = half the slots */
+  uint64_t large_work;           /* paths × steps × scenarios (summed over a book's trades, plus its
+                                    universe generation) at which a request is large; 0 = 2^31 */
 } rg_server_config;
 
 enum { RG_JOB_QUEUED = 0, RG_JOB_RUNNING = 1, RG_JOB_DONE = 2, RG_JOB_FAILED = 3, RG_JOB_CANCELLED = 4 };

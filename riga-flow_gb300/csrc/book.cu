@@ -331,7 +331,16 @@ size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
   const uint64_t P = r->config.paths;
   const bool fp32 = r->config.precision == RG_PRECISION_FP32;
   const size_t elem = fp32 ? sizeof(float) : sizeof(double);
-  const uint64_t unit = fp32 ? (uint64_t)book32_shape((int)std::min<size_t>(S, 32), device_sm_count()).blk_paths : 128;
+  int group[RG_NMAX] = {0};
+  for (int32_t j = 0; j < r->n_trades; ++j) {
+    const int n = r->trades[j].terms.n_assets;
+    if (n >= 1 && n <= RG_NMAX) ++group[n - 1];
+  }
+  int gmin = 0;
+  for (int n = 0; n < RG_NMAX; ++n)
+    if (group[n] > 0 && (gmin == 0 || group[n] < gmin)) gmin = group[n];
+  const uint64_t unit =
+      fp32 ? (uint64_t)book32_shape((int)std::min<size_t>(S, 32), device_sm_count(), P, gmin).blk_paths : 128;
   const uint64_t PC = chunk_paths(P, (int)U, (int64_t)TU, elem, unit);
   const uint64_t chunks = (P + PC - 1) / PC;
   size_t b = (size_t)PC * U * TU * elem * (fp32 && chunks > 1 ? 2 : 1);
@@ -347,6 +356,27 @@ namespace {
 using namespace bk;
 
 // Prices (records == nullptr) or replays [first, first + count) of the book.
+// Every input of the FP32 universe increments of paths [path_base, path_base + P): the universe
+// correlation and grid, the QMC settings and the path range (spots, vols, rates and the trades
+// enter only the scans).
+static std::vector<uint8_t> universe_key_bytes(const rg_book_request* r, uint64_t path_base, uint64_t P) {
+  std::vector<uint8_t> b;
+  auto put = [&b](const void* p, size_t n) {
+    const uint8_t* c = static_cast<const uint8_t*>(p);
+    b.insert(b.end(), c, c + n);
+  };
+  const int64_t U = r->universe.n_assets;
+  const int64_t ints[8] = {U, r->universe_steps, (int64_t)r->config.seed, r->config.variance_reduction,
+                           (int64_t)r->config.qmc_dimension, r->config.scrambler, r->config.dim_mode,
+                           (int64_t)r->config.precision};
+  const uint64_t range[2] = {path_base, P};
+  put(ints, sizeof ints);
+  put(range, sizeof range);
+  put(&r->universe_maturity_years, sizeof(double));
+  put(r->universe.correlation, sizeof(double) * (size_t)(U * U));
+  return b;
+}
+
 void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* sc, int n_scen,
               rg_price_result* out, uint64_t first, uint64_t count, rg_path_record* records) {
   validate_book(r, sc, n_scen);
@@ -366,7 +396,7 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
   const uint64_t P = records ? count : r->config.paths;
   cudaStream_t s0 = E->stream, s1 = E->gen_stream;
   if (fp32) {
-    const Book32Shape sh = book32_shape(B.S, device_sm_count());
+    const Book32Shape sh = book32_shape(B.S, device_sm_count(), P, B.min_group());
     const uint64_t PC = chunk_paths(P, B.U, B.TU, sizeof(float), (uint64_t)sh.blk_paths);
     const uint64_t n_chunks = (P + PC - 1) / PC;
     const uint64_t blocks_per_chunk = (PC + sh.blk_paths - 1) / sh.blk_paths;
@@ -379,6 +409,16 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
     int32_t* scratch = static_cast<int32_t*>(book_buf(E, BK_SCRATCH, 256));
     int* status = scratch + 1;
     cuda_check(cudaMemsetAsync(scratch, 0, 256, s0), "book status reset");
+    // a book of one path chunk whose universe increments this engine generated last time (same
+    // universe correlation, grid, QMC settings and paths) scans them again without regenerating
+    std::vector<uint8_t> ukey;
+    bool resident = false;
+    if (n_chunks == 1) {
+      ukey = universe_key_bytes(r, path_base, P);
+      resident = E->universe_ptr == incr[0] && E->universe_key == ukey;
+    }
+    E->universe_key.clear();  // set again only when this call completes
+    E->universe_ptr = nullptr;
     // the generation stream waits for the tables and the Cholesky factor
     cuda_check(cudaEventRecord(E->book_ev[0], s0), "event");
     cuda_check(cudaStreamWaitEvent(s1, E->book_ev[0], 0), "stream wait");
@@ -390,9 +430,11 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
         cuda_check(cudaStreamWaitEvent(s1, E->book_ev[2 + (c & 1)], 0), "stream wait");
       }
       const uint64_t rowlen = (np + 63) / 64 * 64;
-      launch_book_gen32(B.gen, st.tb, st.L32, B.U, path_base + p0, np, rowlen, buf, s1);
-      cuda_check(cudaEventRecord(E->book_ev[1], s1), "event");
-      cuda_check(cudaStreamWaitEvent(s0, E->book_ev[1], 0), "stream wait");
+      if (!resident) {
+        launch_book_gen32(B.gen, st.tb, st.L32, B.U, path_base + p0, np, rowlen, buf, s1);
+        cuda_check(cudaEventRecord(E->book_ev[1], s1), "event");
+        cuda_check(cudaStreamWaitEvent(s0, E->book_ev[1], 0), "stream wait");
+      }
       const CUtensorMap tmap = increments_map(buf, np, rowlen, B.U, B.TU, sh.Pb, sh.TT);
       launch_book_trade32(st.bk, sh, tmap, np, c * blocks_per_chunk, B.group_lo, B.group_n, partial, scratch, status, s0);
       cuda_check(cudaEventRecord(E->book_ev[2 + (c & 1)], s0), "event");
@@ -409,8 +451,14 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
     for (size_t k = 0; k < hs.size(); ++k)
       if (!std::isfinite(hs[k])) raise(RG_ERR_GPU_ERROR, "book: non-finite path sums");
     for (int p = 0; p < pairs; ++p) finish(hs.data() + (size_t)p * RG_ACC, P, r->config.seed, &out[p]);
+    if (n_chunks == 1) {
+      E->universe_key.swap(ukey);
+      E->universe_ptr = incr[0];
+    }
     return;
   }
+  E->universe_key.clear();  // the FP64 path writes its own increments into the same buffer
+  E->universe_ptr = nullptr;
   // FP64 parity: generation then scan per chunk on the engine stream
   const uint64_t PC = chunk_paths(P, B.U, B.TU, sizeof(double), 128);
   const uint64_t n_chunks = (P + PC - 1) / PC;

@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(1024, 1) book_trade32_kernel(const __grid_cons
   }
 }
 
-Book32Shape book32_shape(int S, int sm_count) {
+Book32Shape book32_shape(int S, int sm_count, uint64_t paths, int min_group_trades) {
   Book32Shape sh{};
   if (S > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per book launch");
   int sb = 1;
@@ -347,7 +347,13 @@ Book32Shape book32_shape(int S, int sm_count) {
   sh.Pb = sh.threads / sb;
   sh.TT = std::min(32, 4096 / sh.Pb);
   sh.grid = sm_count * (sh.threads == 1024 ? 1 : 4);
-  sh.blk_paths = sh.Pb * 32;
+  // a work item is one trade over a block of 32 path tiles; a small book (few paths, or an
+  // underlying-count group of few trades) takes smaller blocks, so that the smallest group's launch
+  // still has two items per SM instead of running as long as one long item
+  int k = 32;
+  const uint64_t g = (uint64_t)(min_group_trades > 0 ? min_group_trades : 1);
+  while (k > 1 && (paths + (uint64_t)sh.Pb * k - 1) / ((uint64_t)sh.Pb * k) * g < 2 * (uint64_t)sm_count) k >>= 1;
+  sh.blk_paths = sh.Pb * k;
   sh.smem = 2 * 5 * sh.TT * sh.Pb * 4 + 64;
   return sh;
 }

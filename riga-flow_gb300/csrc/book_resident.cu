@@ -124,7 +124,7 @@ void price_resident(rg_book* b, const rg_market_snapshot* sc, int n_scen, rg_pri
     memcpy(g.scen_host.ptr, sp.pk.host.data(), scen_bytes);
     cuda_check(cudaMemcpyAsync(g.scen_dev.ptr, g.scen_host.ptr, scen_bytes, cudaMemcpyHostToDevice, E->stream), "H2D");
     point_scenarios(sp, static_cast<uint8_t*>(g.scen_dev.ptr), S, b->st.bk);
-    Book32Shape sh = book32_shape(S, device_sm_count());
+    Book32Shape sh = book32_shape(S, device_sm_count(), b->P, b->B.min_group());
     sh.TT = autotune_stage(b, sh);
     sh.smem = 2 * 5 * sh.TT * sh.Pb * 4 + 64;
     b->tuned[S] = sh.TT;

@@ -203,6 +203,72 @@ struct Staged {
   DevScen32* scen32 = nullptr;
 };
 
+// Every input of one surface's calibration, as bytes: the cache key of a resident surface.
+static std::vector<uint8_t> surface_key_bytes(const rg_implied_vol_grid& g, const SurfaceKey& k, int gx) {
+  std::vector<uint8_t> b;
+  auto put = [&b](const void* p, size_t n) {
+    const uint8_t* c = static_cast<const uint8_t*>(p);
+    b.insert(b.end(), c, c + n);
+  };
+  const int32_t dims[3] = {g.n_maturities, g.n_strikes, gx};
+  const double mkt[3] = {k.spot, k.rate, k.shift};
+  put(dims, sizeof dims);
+  put(mkt, sizeof mkt);
+  put(g.maturities_years, sizeof(double) * (size_t)g.n_maturities);
+  put(g.strikes, sizeof(double) * (size_t)g.n_strikes);
+  put(g.vols, sizeof(double) * (size_t)g.n_maturities * (size_t)g.n_strikes);
+  return b;
+}
+
+double* SurfaceCache::lookup(const std::vector<uint8_t>& key, size_t bytes, bool& hit) {
+  ++tick;
+  hit = false;
+  int victim = -1;
+  for (int i = 0; i < kEntries; ++i) {
+    Entry& e = entries[i];
+    if (e.ready && e.key == key && e.buf.bytes >= bytes) {
+      e.used = tick;
+      hit = true;
+      return static_cast<double*>(e.buf.ptr);
+    }
+    // an entry this call is already filling is not available
+    if (std::find(pending.begin(), pending.end(), i) != pending.end()) continue;
+    if (victim < 0 || e.used < entries[victim].used) victim = i;
+  }
+  if (victim < 0) return nullptr;  // more new surfaces in one call than entries: calibrate only
+  // not resident: the least recently used entry takes this surface once the call completes
+  Entry& e = entries[victim];
+  e.ready = false;
+  e.key = key;
+  e.used = tick;
+  e.buf.ensure(bytes);
+  pending.push_back(victim);
+  return static_cast<double*>(e.buf.ptr);
+}
+
+void SurfaceCache::begin_call() { pending.clear(); }
+
+void SurfaceCache::commit() {
+  for (int i : pending) entries[i].ready = true;
+  pending.clear();
+}
+
+size_t SurfaceCache::device_bytes() const {
+  size_t b = 0;
+  for (const Entry& e : entries) b += e.buf.bytes;
+  return b;
+}
+
+void SurfaceCache::release() {
+  for (Entry& e : entries) {
+    e.buf.release();
+    e.key.clear();
+    e.ready = false;
+    e.used = 0;
+  }
+  pending.clear();
+}
+
 static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   Pack pk;
   const DevTrade& tr = P.trade;
@@ -260,6 +326,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   }
   uint8_t* base = static_cast<uint8_t*>(W.device(WS_ARENA, pk.host.size()));
   if (tr.has_lv) {
+    if (SurfaceCache* cache = W.surfaces()) cache->begin_call();
     double* sc = static_cast<double*>(W.device(WS_CALIB, scratch * sizeof(double)));
     size_t cell_off = 0, sc_off = 0;
     for (int j = 0; j < P.n_surf; ++j) {
@@ -279,6 +346,14 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
       J.out_vf = reinterpret_cast<float2*>(base + o_lvf) + cell_off;
       J.out_logs = reinterpret_cast<double*>(base + o_logs) + (size_t)j * gx;
       J.scratch = sc + sc_off;
+      J.cache_src = nullptr;
+      J.cache_dst = nullptr;
+      if (SurfaceCache* cache = W.surfaces()) {
+        bool hit = false;
+        double* e = cache->lookup(surface_key_bytes(g, key, gx), surface_entry_bytes(J.n_t, gx), hit);
+        if (hit) J.cache_src = e;
+        else J.cache_dst = e;
+      }
       cell_off += (size_t)J.n_t * gx;
       sc_off += (size_t)4 * J.n_t * gx + gx + (size_t)6 * J.n_t * J.n_k;
     }
@@ -488,6 +563,7 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     cuda_check(cudaMemcpyAsync(hs, dsums, sums_bytes, cudaMemcpyDeviceToHost, W.stream), "D2H sums");
     if (W.ev) cuda_check(cudaEventRecord(W.ev[5], W.stream), "event");
     cuda_check(cudaStreamSynchronize(W.stream), "pricing");
+    if (SurfaceCache* cache = W.surfaces()) cache->commit();
     if (W.ev && W.timing) {
       float ms[5];
       for (int k = 0; k < 5; ++k) cuda_check(cudaEventElapsedTime(&ms[k], W.ev[k], W.ev[k + 1]), "event time");
@@ -527,6 +603,7 @@ struct EngineWorkspace : Workspace {
     E->host_sums.ensure(bytes);
     return E->host_sums.ptr;
   }
+  SurfaceCache* surfaces() override { return &E->surfaces; }
 };
 
 size_t estimate_price_bytes(const rg_price_request* r, int n_scen) {
@@ -557,7 +634,7 @@ size_t engine_device_bytes(rg_engine* E) {
   size_t b = 0;
   for (const DevBuf& d : E->bufs) b += d.bytes;
   for (const DevBuf& d : E->book_bufs) b += d.bytes;
-  return b;
+  return b + E->surfaces.device_bytes();
 }
 
 void engine_trim(rg_engine* E) {
@@ -567,6 +644,9 @@ void engine_trim(rg_engine* E) {
   cuda_check(cudaStreamSynchronize(E->gen_stream), "trim");
   for (DevBuf& d : E->bufs) d.release();
   for (DevBuf& d : E->book_bufs) d.release();
+  E->surfaces.release();
+  E->universe_key.clear();
+  E->universe_ptr = nullptr;
 }
 
 static void price(rg_engine* E, const rg_price_request* req, const rg_scenario* sc, int n_scen,
@@ -775,6 +855,7 @@ static void run_path_range(rg_engine* e, const rg_price_request* req, uint64_t f
       cuda_check(cudaMemcpyAsync(cube + done * cube_row, lo.cube, m * cube_row * sizeof(float),
                                  cudaMemcpyDeviceToHost, e->stream), "D2H cube");
     cuda_check(cudaStreamSynchronize(e->stream), "run_paths");
+    e->surfaces.commit();
     done += m;
   }
 }

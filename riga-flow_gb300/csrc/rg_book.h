@@ -25,6 +25,13 @@ struct BookPlan {
   std::vector<double> df, dfm;
   std::vector<int32_t> order;
   int group_lo[RG_NMAX], group_n[RG_NMAX];
+  // trades in the smallest non-empty underlying-count group
+  int min_group() const {
+    int m = 0;
+    for (int n = 0; n < RG_NMAX; ++n)
+      if (group_n[n] > 0 && (m == 0 || group_n[n] < m)) m = group_n[n];
+    return m;
+  }
 };
 
 // Request checks (each trade with the reference's own request validation on its slice of the

@@ -126,6 +126,7 @@ enum WsSlot {
   WS_CUBE,                      // f32 spot cube of a materialised path range
   WS_NSLOTS
 };
+struct SurfaceCache;
 struct Workspace {
   cudaStream_t stream = nullptr;
   cudaEvent_t* ev = nullptr;    // six events for the timing breakdown, or null
@@ -139,6 +140,8 @@ struct Workspace {
   // whether extra timed launches (the tile-depth autotuner) may run on this stream; not for the
   // static entry point, which may be called under stream capture
   virtual bool may_tune() const { return true; }
+  // the engine's resident calibrated surfaces, or null (the static entry point keeps none)
+  virtual SurfaceCache* surfaces() { return nullptr; }
   virtual ~Workspace() = default;
 };
 // validate → host tables → H2D → prologue → fused kernel → reduce → D2H → PriceResults
@@ -170,6 +173,37 @@ struct CalibJob {
   float2* out_vf;
   double* out_logs;
   double* scratch;  // 4 * n_t * gx + gx + 6 * n_t * n_k doubles
+  // resident-surface cache entry ([v][logs][vf], surface_entry_bytes): copy the surface from it
+  // instead of calibrating (cache_src), or calibrate and also store it there (cache_dst)
+  const double* cache_src;
+  double* cache_dst;
+};
+inline size_t surface_entry_bytes(int n_t, int gx) {
+  return (size_t)n_t * gx * sizeof(double) + (size_t)gx * sizeof(double) + (size_t)n_t * gx * sizeof(float2);
+}
+
+// Calibrated Dupire surfaces kept on the device between calls of one engine, keyed by every input
+// of the calibration (implied grid, spot, rate, implied-vol shift, grid width).  A copy is
+// bit-identical to a recalibration.  Entries found by a call become usable only when the call
+// completes (commit), so a failed call never leaves a half-written surface behind.
+struct SurfaceCache {
+  struct Entry {
+    std::vector<uint8_t> key;
+    DevBuf buf;
+    uint64_t used = 0;
+    bool ready = false;
+  };
+  static constexpr int kEntries = 64;
+  Entry entries[kEntries];
+  uint64_t tick = 0;
+  std::vector<int> pending;
+  // The entry for `key`: `hit` says whether it holds the calibrated surface already.
+  // (null when every entry is being filled by this call: then the surface is only calibrated)
+  double* lookup(const std::vector<uint8_t>& key, size_t bytes, bool& hit);
+  void begin_call();  // forget the entries of a call that did not complete
+  void commit();      // the entries this call filled hold their surfaces now
+  size_t device_bytes() const;
+  void release();
 };
 void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s);
 void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s);
@@ -279,7 +313,8 @@ void launch_book_trade64(const DevTrade& gen, const BookDev& bk, const double* i
 struct Book32Shape {
   int threads, Sb, Pb, TT, grid, blk_paths, smem;
 };
-Book32Shape book32_shape(int S, int sm_count);
+// `paths`: the book's path count; `min_group_trades`: trades in its smallest underlying-count group.
+Book32Shape book32_shape(int S, int sm_count, uint64_t paths, int min_group_trades);
 // `tmap` views the chunk's increments as [TU][U][npaths] floats (boxes of Pb paths × 1 asset × TT
 // steps) for the kernel's TMA stages.
 // One persistent launch per underlying count n with trades order[group_lo[n-1], + group_n[n-1]).
@@ -329,6 +364,11 @@ struct rg_engine {
   rg::DevBuf book_bufs[8];
   rg::HostBuf host_sums;
   std::vector<uint8_t> host_pack;
+  rg::SurfaceCache surfaces;
+  // the universe increments held in the first book increment buffer (a book of one path chunk),
+  // by the bytes of every input of their generation; empty when the buffer holds anything else
+  std::vector<uint8_t> universe_key;
+  const void* universe_ptr = nullptr;
   cudaEvent_t ev[6] = {};
   cudaEvent_t book_ev[4] = {};
   rg_timing timing{};

@@ -5,7 +5,11 @@
 // head of the queue when the head's device-memory estimate fits: the budget is compared with the
 // sum over slots of what each holds (a running slot counts max(held, its request's estimate)); when
 // the head does not fit, idle slots release their buffers first.  Requests therefore enter as
-// slots and memory free up, and the ones admitted run concurrently on their own streams.  Each
+// slots and memory free up, and the ones admitted run concurrently on their own streams.  Requests
+// whose work (paths × steps × scenarios, summed over a book's trades) reaches the large-work mark
+// may hold at most max_large_slots slots at once; a worker takes the first queued request it may
+// start, so small requests pass large ones that are waiting for a large slot, and a request that
+// waits for memory is never passed.  Each
 // request runs through the same entry points as a direct call (rg_price_scenarios,
 // rg_price_risk_batch, rg_price_book), so its results are independent of what runs beside it.
 #include <algorithm>
@@ -146,6 +150,8 @@ struct Job {
   std::vector<OwnedMarket> book_scen;
   std::vector<rg_market_snapshot> book_scen_views;
   size_t est = 0;
+  double work = 0;     // path-steps × scenarios the request prices
+  bool large = false;  // work at or above the server's large-work mark
   uint64_t n_results = 0;
   int state = RG_JOB_QUEUED;
   int32_t status = RG_OK;
@@ -183,6 +189,9 @@ struct rg_server {
   std::vector<double> latencies_ms;
   int n_running = 0;
   double busy_s = 0, busy_since = 0;
+  int max_large = 1;        // slots large requests may hold at once
+  double large_work = 0;    // work at which a request counts as large
+  int n_large = 0;          // large requests running
 };
 
 namespace rg {
@@ -238,18 +247,29 @@ void run_job(rg_engine* E, Job* job) {
   }
 }
 
+// Under S->mu: the queued request slot k starts next, or null.  Requests go in arrival order,
+// except that a large one waiting for a large slot is passed; one that does not fit the memory
+// budget stops the scan (later requests never overtake it on memory).
+Job* next_job(rg_server* S, int k) {
+  for (Job* j : S->queue) {
+    if (j->large && S->n_large >= S->max_large) continue;
+    return admit(S, k, j) ? j : nullptr;
+  }
+  return nullptr;
+}
+
 void worker(rg_server* S, int k) {
   std::unique_lock<std::mutex> lock(S->mu);
   for (;;) {
     Job* job = nullptr;
     S->cv_work.wait(lock, [&] {
       if (S->stopping) return true;
-      if (S->queue.empty()) return false;
-      return admit(S, k, S->queue.front());
+      job = next_job(S, k);
+      return job != nullptr;
     });
     if (S->stopping) return;
-    job = S->queue.front();
-    S->queue.pop_front();
+    S->queue.erase(std::find(S->queue.begin(), S->queue.end(), job));
+    if (job->large) ++S->n_large;
     Slot& slot = S->slots[k];
     slot.busy = true;
     slot.running = job->est;
@@ -264,6 +284,7 @@ void worker(rg_server* S, int k) {
     const size_t held = engine_device_bytes(slot.engine);
     lock.lock();
     job->t_end = now_s(S);
+    if (job->large) --S->n_large;
     if (--S->n_running == 0) S->busy_s += job->t_end - S->busy_since;
     slot.busy = false;
     slot.running = 0;
@@ -291,6 +312,7 @@ uint64_t enqueue(rg_server* S, std::unique_ptr<Job> job) {
                                        std::to_string(S->budget >> 20) + " MiB");
   std::lock_guard<std::mutex> lock(S->mu);
   if (S->stopping) raise(RG_ERR_CANCELLED, "the server is shutting down");
+  job->large = job->work >= S->large_work;
   job->id = S->next_id++;
   job->t_submit = now_s(S);
   Job* raw = job.get();
@@ -348,6 +370,9 @@ extern "C" int32_t rg_server_create(const rg_server_config* cfg, rg_server** out
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
     S->budget = cfg && cfg->device_memory_budget ? (size_t)cfg->device_memory_budget : free_b / 10 * 8;
+    S->max_large = cfg && cfg->max_large_slots > 0 ? std::min(cfg->max_large_slots, n_slots)
+                                                   : std::max(1, n_slots / 2);
+    S->large_work = cfg && cfg->large_work > 0 ? (double)cfg->large_work : 2147483648.0;
     S->slots.resize(n_slots);
     for (int k = 0; k < n_slots; ++k) {
       int32_t st = rg_engine_create(device, &S->slots[k].engine);
@@ -408,6 +433,7 @@ extern "C" int32_t rg_server_submit_price(rg_server* S, const rg_price_request* 
     job->n_results = n > 0 ? (uint64_t)n : 1;
     job->results.resize(job->n_results);
     job->est = estimate_price_bytes(&job->req.r, n);
+    job->work = (double)req->config.paths * (double)req->trade.steps * (double)job->n_results;
     *ticket = enqueue(S, std::move(job));
   })
 }
@@ -423,6 +449,7 @@ extern "C" int32_t rg_server_submit_risk(rg_server* S, const rg_price_request* r
     job->risk_cfg = *cfg;
     job->n_results = 0;
     job->est = estimate_price_bytes(&job->req.r, 1 + 4 * req->market.n_assets + 4);
+    job->work = (double)req->config.paths * (double)req->trade.steps * (double)(1 + 4 * req->market.n_assets + 4);
     *ticket = enqueue(S, std::move(job));
   })
 }
@@ -444,6 +471,9 @@ extern "C" int32_t rg_server_submit_book(rg_server* S, const rg_book_request* re
     job->n_results = (uint64_t)(req->n_trades > 0 ? req->n_trades : 0) * S_;
     job->results.resize(job->n_results);
     job->est = estimate_book_bytes(&job->book.r, n);
+    double steps = (double)req->universe_steps * (double)req->universe.n_assets;  // the universe generation
+    for (int32_t j = 0; j < req->n_trades; ++j) steps += (double)req->trades[j].terms.steps * (double)S_;
+    job->work = (double)req->config.paths * steps;
     *ticket = enqueue(S, std::move(job));
   })
 }

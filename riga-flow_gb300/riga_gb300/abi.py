@@ -278,7 +278,8 @@ class BookRequest(C.Structure):
 
 
 class ServerConfig(C.Structure):
-    _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("device_memory_budget", C.c_uint64)]
+    _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("device_memory_budget", C.c_uint64),
+                ("max_large_slots", C.c_int32), ("large_work", C.c_uint64)]
 
 
 class JobInfo(C.Structure):

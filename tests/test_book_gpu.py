@@ -150,3 +150,28 @@ def test_resident_book_keeps_the_reference_error_codes(engine):
     with pytest.raises(abi.RigaError) as e:
         engine.resident_book(b64)
     assert e.value.code == "unsupported"
+
+
+def test_resident_universe_increments_equal_a_fresh_generation(engine):
+    """An engine keeps the universe increments of its last one-chunk FP32 book; a book on the same
+    universe, grid and path set scans them again without regenerating, and prices exactly as a
+    fresh engine that generates them.  A changed correlation is generated afresh."""
+    b = workloads.small_book(paths=1 << 13, n_trades=7, steps_per_year=52, max_years=2, fp32=True)
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:4]
+    engine.price_book_raw(b, sc)
+    sub = copy.deepcopy(b)
+    sub.trades = b.trades[2:5]
+    fresh = Engine(0)
+    try:
+        reused = engine.price_book_raw(sub, sc)
+        assert [bytes(x) for x in reused] == [bytes(x) for x in fresh.price_book_raw(sub, sc)]
+        b2 = copy.deepcopy(sub)
+        n = len(b2.universe.correlation)
+        b2.universe.correlation = [[1.0 if i == j else 0.98 * b2.universe.correlation[i][j] for j in range(n)]
+                                   for i in range(n)]
+        sc2 = [m for _, m in workloads.book_scenarios(b2.universe)][:4]
+        r2 = engine.price_book_raw(b2, sc2)
+        assert [bytes(x) for x in r2] == [bytes(x) for x in fresh.price_book_raw(b2, sc2)]
+        assert r2[0].pv != reused[0].pv
+    finally:
+        fresh.close()

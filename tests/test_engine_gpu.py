@@ -310,6 +310,35 @@ def test_autotuned_tile_depth_keeps_prices(engine):
         assert bytes(a) == bytes(b) == bytes(c)
 
 
+def test_resident_surfaces_reproduce_the_calibration():
+    """Calibrated Dupire surfaces stay resident on the engine: a repeated request copies them
+    instead of recalibrating (shorter prologue) and prices byte for byte the same; a request whose
+    implied grid differs is calibrated afresh and matches a new engine's price of it."""
+    r = workloads.lv3(paths=1 << 14, steps=252)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(r)]
+    e1, e2 = Engine(0), Engine(0)
+    try:
+        a = e1.price_scenarios_raw(r, scen)
+        t_cal = e1.last_timing().prologue_ms
+        b = e1.price_scenarios_raw(r, scen)
+        t_res = e1.last_timing().prologue_ms
+        assert [bytes(x) for x in a] == [bytes(x) for x in b]
+        assert t_res < t_cal, (t_res, t_cal)
+        r2 = copy.deepcopy(r)
+        r2.local_vol[0].vols = [[v + 0.001 for v in row] for row in r2.local_vol[0].vols]
+        c = e1.price_scenarios_raw(r2, scen)
+        assert c[0].pv != a[0].pv
+        d = e2.price_scenarios_raw(r2, scen)
+        assert [bytes(x) for x in c] == [bytes(x) for x in d]
+        # the FP64 parity kernel reads the same resident surfaces
+        r64 = workloads.lv3(256, steps=126, fp32=False)
+        assert_records_match(e1.run_paths_raw(r64, 0, 256), e2.run_paths_raw(r64, 0, 256), rel=0.0)
+        assert_records_match(e1.run_paths_raw(r64, 0, 256), O.run_paths(r64, 0, 256))
+    finally:
+        e1.close()
+        e2.close()
+
+
 def test_large_fused_config_fp64_parity():
     """The large fused configuration's shape (5 assets, 64x32 SVI smiles, 64-point Dupire grid,
     2-factor correlation, 1260 steps) in the FP64 parity kernel, per path against the oracle."""

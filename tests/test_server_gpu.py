@@ -219,3 +219,21 @@ def test_mcp_replay_tools(engine):
     assert cube["data"] == [float(v) for v in pc.data]
     assert cube["checksum"] == cube_checksum(pc.data)
     assert (cube["paths"], cube["times"], cube["factors"]) == (16, 126, 3)
+
+
+def test_small_requests_pass_large_ones_waiting_for_a_large_slot():
+    """Two slots, one of which large requests may hold: two large CRN batches and then a small
+    request are submitted; the small one runs beside the first large one and finishes before the
+    second large one starts, and the two large ones never overlap."""
+    big = workloads.lv3(paths=1 << 20, steps=756)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(big)]
+    small = workloads.lv3(paths=1 << 12, steps=126)
+    with Server(slots=2, max_large_slots=1, large_work=1 << 28) as srv:
+        t1 = srv.submit_price(big, scen)
+        t2 = srv.submit_price(big, scen)
+        t3 = srv.submit_price(small)
+        i3 = srv.wait(t3)
+        i2 = srv.wait(t2)
+        i1 = srv.wait(t1)
+    assert i3.end_s <= i2.start_s, (i3.end_s, i2.start_s)
+    assert i2.start_s >= i1.end_s, (i2.start_s, i1.end_s)
