@@ -4,6 +4,55 @@
 
 namespace rg {
 
+// The Phoenix state of one FP32 path of one scenario.
+struct P32Phoenix {
+  bool alive = true, received = false;
+  int qual = 0, unpaid = 0, ko_step = -1, qualified = 0, paid = 0;
+  float cpv = 0.0f, mpv = 0.0f;
+};
+
+// One step of the Phoenix state machine (crates/riga-engine/src/note.rs:150-218) for a live path:
+// `fl` is the step's schedule flags, `wmin` the log worst-of performance after the step, `df` the
+// scenario's discount factors by step, `period()` the step's coupon period (read only when a
+// coupon is due).  Barriers compare in log space (ln_cb, ln_ko).
+template <bool REC, class Period>
+__device__ __forceinline__ void p32_phoenix_step(P32Phoenix& st, uint32_t fl, int t, float wmin, float ln_cb,
+                                                 float ln_ko, const DevTrade& tr, const DevTables& tb,
+                                                 const double* __restrict__ df, Period period) {
+  if (fl & STEP_PERIOD_RESET) st.qual = 0;
+  if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
+    ++st.qual;
+    if (REC) ++st.qualified;
+  }
+  if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
+    st.alive = false;
+    st.ko_step = t;
+    const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                            : (float)st.qual * (float)__ldg(tb.accr_inc + period());
+    const float carry = due > 0.0f ? (float)st.unpaid * (float)tr.coupon_rate : 0.0f;
+    if (due + carry > 0.0f) {
+      const float d = (float)__ldg(df + t);
+      st.cpv = fmaf(due, d, st.cpv);
+      st.mpv = fmaf(carry, d, st.mpv);
+      st.received = true;
+      if (REC) ++st.paid;
+    }
+  } else if (fl & STEP_PERIOD_END) {
+    const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
+                                            : (float)st.qual * (float)__ldg(tb.accr_inc + period());
+    if (due > 0.0f) {
+      const float d = (float)__ldg(df + t);
+      st.cpv = fmaf(due, d, st.cpv);
+      st.mpv = fmaf((float)st.unpaid * (float)tr.coupon_rate, d, st.mpv);
+      st.unpaid = 0;
+      st.received = true;
+      if (REC) ++st.paid;
+    } else if (tr.memory) {
+      ++st.unpaid;
+    }
+  }
+}
+
 // Path close (crates/riga-engine/src/note.rs:221-258) of one FP32 path of scenario `sc`: its
 // payoff values into out[RG_ACC] (zero when `ok` is false), and for scenario 0 (`first`) its KO
 // step for the trace events and, in the records variant, its PathRecord (explain.rs:90-316) with

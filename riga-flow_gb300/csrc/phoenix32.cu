@@ -149,9 +149,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
     float x[N];
 #pragma unroll
     for (int f = 0; f < N; ++f) x[f] = lvc[f].w;
-    bool alive = true, received = false;
-    int qual = 0, unpaid = 0, ko_step = -1, qualified = 0, paid = 0;
-    float cpv = 0.0f, mpv = 0.0f;
+    P32Phoenix ph;
     float worst = 0.0f;
     int sp = 0;
     for (int t0 = 0; t0 < T; t0 += TT) {
@@ -267,50 +265,17 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
             wmin = fminf(wmin, x[f]);
           }
           worst = wmin;
-          if (alive) {
-            const uint32_t fl = s_flags[tt];
-            const int t = t0 + tt;
-            if (fl & STEP_PERIOD_RESET) qual = 0;
-            if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
-              ++qual;
-              if (REC) ++qualified;
-            }
-            if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
-              alive = false;
-              ko_step = t;
-              const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                                      : (float)qual * (float)__ldg(tb.accr_inc + s_per[tt]);
-              const float carry = due > 0.0f ? (float)unpaid * (float)tr.coupon_rate : 0.0f;
-              if (due + carry > 0.0f) {
-                const float df = (float)__ldg(tb.df + (size_t)ss * T + t);
-                cpv = fmaf(due, df, cpv);
-                mpv = fmaf(carry, df, mpv);
-                received = true;
-                if (REC) ++paid;
-              }
-            } else if (fl & STEP_PERIOD_END) {
-              const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                                      : (float)qual * (float)__ldg(tb.accr_inc + s_per[tt]);
-              if (due > 0.0f) {
-                const float df = (float)__ldg(tb.df + (size_t)ss * T + t);
-                cpv = fmaf(due, df, cpv);
-                mpv = fmaf((float)unpaid * (float)tr.coupon_rate, df, mpv);
-                unpaid = 0;
-                received = true;
-                if (REC) ++paid;
-              } else if (tr.memory) {
-                ++unpaid;
-              }
-            }
-          }
+          if (ph.alive)
+            p32_phoenix_step<REC>(ph, s_flags[tt], t0 + tt, wmin, ln_cb, ln_ko, tr, tb, tb.df + (size_t)ss * T,
+                                  [&] { return s_per[tt]; });
         }
       }
       __syncthreads();
     }
     // ---- path close (note.rs:221-258) and the per-tile reduction
     float out[RG_ACC];
-    p32_close_path<REC>(tr, tb, ss, T, ok, s == 0, path0, gi, ko_step, worst, ln_ki, cpv, mpv, received,
-                        qualified, paid, ko_steps, records, out);
+    p32_close_path<REC>(tr, tb, ss, T, ok, s == 0, path0, gi, ph.ko_step, worst, ln_ki, ph.cpv, ph.mpv,
+                        ph.received, ph.qualified, ph.paid, ko_steps, records, out);
     // butterfly within each group of lanes that share a scenario (g = min(32, Pb) lanes)
     const int g = Pb < 32 ? Pb : 32;
     for (int off = g >> 1; off > 0; off >>= 1)

@@ -108,9 +108,7 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
       wcur[f] = 0.0f;
     }
     int sp = 0;
-    bool alive = true, received = false;
-    int qual = 0, unpaid = 0, ko_step = -1, qualified = 0, paid = 0;
-    float cpv = 0.0f, mpv = 0.0f;
+    P32Phoenix ph;
     float worst = 0.0f;
     for (int t = 0; t < T; ++t) {
       // bridge nodes consumed at this step: normals, then the streamed bridge (qmc.rs:158-191)
@@ -197,47 +195,14 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
         wmin = fminf(wmin, x[f]);
       }
       worst = wmin;
-      if (alive) {
-        // Phoenix state machine (note.rs:150-218)
-        const uint32_t fl = __ldg(tb.step_flags + t);
-        if (fl & STEP_PERIOD_RESET) qual = 0;
-        if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
-          ++qual;
-          if (REC) ++qualified;
-        }
-        if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
-          alive = false;
-          ko_step = t;
-          const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                                  : (float)qual * (float)__ldg(tb.accr_inc + __ldg(tb.step_period + t));
-          const float carry = due > 0.0f ? (float)unpaid * (float)tr.coupon_rate : 0.0f;
-          if (due + carry > 0.0f) {
-            const float df = (float)__ldg(tb.df + (size_t)s * T + t);
-            cpv = fmaf(due, df, cpv);
-            mpv = fmaf(carry, df, mpv);
-            received = true;
-            if (REC) ++paid;
-          }
-        } else if (fl & STEP_PERIOD_END) {
-          const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                                  : (float)qual * (float)__ldg(tb.accr_inc + __ldg(tb.step_period + t));
-          if (due > 0.0f) {
-            const float df = (float)__ldg(tb.df + (size_t)s * T + t);
-            cpv = fmaf(due, df, cpv);
-            mpv = fmaf((float)unpaid * (float)tr.coupon_rate, df, mpv);
-            unpaid = 0;
-            received = true;
-            if (REC) ++paid;
-          } else if (tr.memory) {
-            ++unpaid;
-          }
-        }
-      }
+      if (ph.alive)  // Phoenix state machine (note.rs:150-218)
+        p32_phoenix_step<REC>(ph, __ldg(tb.step_flags + t), t, wmin, ln_cb, ln_ko, tr, tb, tb.df + (size_t)s * T,
+                              [&] { return __ldg(tb.step_period + t); });
     }
     // path close (note.rs:221-258)
     float out[RG_ACC];
-    p32_close_path<REC>(tr, tb, s, T, ok, s == 0, path0, gi, ko_step, worst, ln_ki, cpv, mpv, received,
-                        qualified, paid, ko_steps, records, out);
+    p32_close_path<REC>(tr, tb, s, T, ok, s == 0, path0, gi, ph.ko_step, worst, ln_ki, ph.cpv, ph.mpv,
+                        ph.received, ph.qualified, ph.paid, ko_steps, records, out);
     // the same FP32 butterfly over the warp's 32 paths as phoenix32.cu, then lane k keeps quantity k
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
