@@ -185,8 +185,8 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
     if (!mbar_wait(&full[b], (G >> 1) & 1u, status)) return false;
     const float* buf = bufs + b * stage_floats;
     const int t0 = k * TT, tn = min(TT, T - t0);
-    for (int tt = 0; tt < tn; ++tt) {
-      const int t = t0 + tt;
+    // one step of the path: log-space Euler on the staged increments, the worst-of performance
+    auto advance = [&](int tt) -> float {
       float wmin = INFINITY;
 #pragma unroll
       for (int f = 0; f < N; ++f) {
@@ -194,40 +194,70 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
         wmin = fminf(wmin, x[f]);
       }
       worst = wmin;
-      if (alive) {
-        if (!fixed && wmin >= tr.ln_cb) ++qual;
-        if (t >= tr.call_start && wmin >= tr.ln_ko) {
-          alive = false;
-          ko_step = t;
-          const float due = fixed ? tr.coupon_f : (float)qual * inc;
-          const float carry = due > 0.0f ? (float)unpaid * tr.coupon_f : 0.0f;
-          if (due + carry > 0.0f) {
-            const float d = (float)__ldg(df + t);
-            cpv = fmaf(due, d, cpv);
-            mpv = fmaf(carry, d, mpv);
-            received = true;
-          }
-        } else if (t == pend) {
-          const float due = fixed ? tr.coupon_f : (float)qual * inc;
-          if (due > 0.0f) {
-            const float d = (float)__ldg(df + t);
-            cpv = fmaf(due, d, cpv);
-            mpv = fmaf((float)unpaid * tr.coupon_f, d, mpv);
-            unpaid = 0;
-            received = true;
-          } else if (tr.memory) {
-            ++unpaid;
-          }
+      return wmin;
+    };
+    auto knock_out = [&](int t) {
+      alive = false;
+      ko_step = t;
+      const float due = fixed ? tr.coupon_f : (float)qual * inc;
+      const float carry = due > 0.0f ? (float)unpaid * tr.coupon_f : 0.0f;
+      if (due + carry > 0.0f) {
+        const float d = (float)__ldg(df + t);
+        cpv = fmaf(due, d, cpv);
+        mpv = fmaf(carry, d, mpv);
+        received = true;
+      }
+    };
+    // The schedule is the trade's, the same for every thread: the stage splits into runs of plain
+    // steps (no period end) before and after the call start, and the period-end step, which alone
+    // pays coupons and moves to the next period.
+    int tt = 0;
+    while (tt < tn) {
+      const int seg = min(tn, pend - t0 + 1);           // through the next period end, or the stage end
+      const int plain = pend - t0 < tn ? seg - 1 : seg;  // steps [tt, plain) are not a period end
+      const int ko_from = max(tt, min(plain, tr.call_start - t0));
+      for (; tt < ko_from; ++tt) {
+        const float wmin = advance(tt);
+        if (alive && !fixed && wmin >= tr.ln_cb) ++qual;
+      }
+      for (; tt < plain; ++tt) {
+        const float wmin = advance(tt);
+        if (alive) {
+          if (!fixed && wmin >= tr.ln_cb) ++qual;
+          if (wmin >= tr.ln_ko) knock_out(t0 + tt);
         }
       }
-      if (t == pend && t + 1 < T) {
-        int64_t q = (int64_t)(t + 1) * PER / T;
-        if (q > PER - 1) q = PER - 1;
-        per = (int)q;
-        pend = per == PER - 1 ? T - 1 : (int)(((int64_t)T * (per + 1) + PER - 1) / PER) - 1;
-        inc = accr(per);
-        fixed = false;
-        qual = 0;
+      if (tt < seg) {
+        // the period-end step (note.rs:150-218 at a period boundary)
+        const int t = t0 + tt;
+        const float wmin = advance(tt);
+        if (alive) {
+          if (!fixed && wmin >= tr.ln_cb) ++qual;
+          if (t >= tr.call_start && wmin >= tr.ln_ko) {
+            knock_out(t);
+          } else {
+            const float due = fixed ? tr.coupon_f : (float)qual * inc;
+            if (due > 0.0f) {
+              const float d = (float)__ldg(df + t);
+              cpv = fmaf(due, d, cpv);
+              mpv = fmaf((float)unpaid * tr.coupon_f, d, mpv);
+              unpaid = 0;
+              received = true;
+            } else if (tr.memory) {
+              ++unpaid;
+            }
+          }
+        }
+        if (t + 1 < T) {
+          int64_t q = (int64_t)(t + 1) * PER / T;
+          if (q > PER - 1) q = PER - 1;
+          per = (int)q;
+          pend = per == PER - 1 ? T - 1 : (int)(((int64_t)T * (per + 1) + PER - 1) / PER) - 1;
+          inc = accr(per);
+          fixed = false;
+          qual = 0;
+        }
+        ++tt;
       }
     }
     // this warp is done with the buffer
