@@ -297,6 +297,16 @@ int32_t rg_price_scenarios(rg_engine* engine, const rg_price_request* request,
                            const rg_scenario* scenarios, int32_t n_scenarios,
                            rg_price_result* out);
 
+/* Calibrates, on the device in FP64, the Dupire surfaces a local-vol request needs — one per
+ * (asset, market) of the request and of its `n_scenarios` CRN scenarios with their implied-vol
+ * shifts (crates/riga-market/src/lib.rs:210-299, crates/riga-risk/src/lib.rs:260-279) — and keeps
+ * them resident on the engine, so that pricing calls with the same inputs copy them instead of
+ * recalibrating.  The engine keeps the 64 most recently used surfaces (pricing calls add theirs
+ * too); a resident surface is byte-identical to a fresh calibration.  `*resident` (optional)
+ * receives the number of distinct surfaces.  A request without local vol uploads nothing. */
+int32_t rg_surfaces_upload(rg_engine* engine, const rg_price_request* request, const rg_scenario* scenarios,
+                           int32_t n_scenarios, int32_t* resident);
+
 /* riga_risk::price_risk_batch, crates/riga-risk/src/lib.rs:573-626 (with the central Greeks of
  * price_central_greeks, :117-186): base + spot/vol up/down per asset + rate up/down +
  * correlation up/down, all priced in one CRN launch. */

@@ -678,6 +678,40 @@ extern "C" int32_t rg_price_scenarios(rg_engine* e, const rg_price_request* req,
   })
 }
 
+extern "C" int32_t rg_surfaces_upload(rg_engine* e, const rg_price_request* req, const rg_scenario* sc,
+                                      int32_t n, int32_t* resident) {
+  RG_TRY({
+    if (!e || !req || (n > 0 && !sc) || n < 0) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    validate_request(req);
+    for (int i = 0; i < n; ++i) {
+      if (sc[i].market.n_assets != req->market.n_assets)
+        raise(RG_ERR_INVALID_MARKET_SHAPE, "scenario asset count differs from the request's");
+      rg_price_request r2 = *req;
+      r2.market = sc[i].market;
+      r2.market.as_of = req->market.as_of;
+      validate_request(&r2);
+    }
+    if (resident) *resident = 0;
+    if (req->n_local_vol == 0) return RG_OK;
+    std::lock_guard<std::mutex> lock(e->mu);
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    EngineWorkspace W(e);
+    int total = 0;
+    // the same staging as a pricing call (tables, calibration into the resident entries), no kernel
+    for (int first = 0; first < (n > 0 ? n : 1); first += 32) {
+      const int cnt = n > 0 ? std::min(32, n - first) : 0;
+      Prepared P;
+      prepare(req, n > 0 ? sc + first : nullptr, cnt, P);
+      W.begin_launch();
+      stage(W, req, P);
+      cuda_check(cudaStreamSynchronize(e->stream), "surface upload");
+      e->surfaces.commit();
+      total += P.n_surf;
+    }
+    if (resident) *resident = total;
+  })
+}
+
 namespace rg {
 // validate_configuration, crates/riga-risk/src/lib.rs:338-457 (N-asset form).
 static void validate_risk(const rg_price_request* r, const rg_central_difference_config* c) {

@@ -334,6 +334,7 @@ SIGNATURES = {
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
     "rg_set_autotune": (_i32, [_i32]),
+    "rg_surfaces_upload": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32, C.POINTER(_i32)]),
     "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
                              C.POINTER(PriceResult)]),
     "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,

@@ -98,6 +98,23 @@ class Engine:
         check(self.lib, self.lib.rg_price_scenarios(self.handle, a.ptr, arr, len(scenarios), out))
         return list(out)
 
+    def upload_surfaces(self, request: PriceRequest, scenarios=None) -> int:
+        """Calibrates the request's (and its scenarios') Dupire surfaces on the device and keeps
+        them resident on this engine (rg_surfaces_upload); returns the number of surfaces."""
+        a = request.to_abi()
+        keep = []
+        scenarios = scenarios or []
+        arr = (abi.Scenario * max(1, len(scenarios)))()
+        for i, (mk, shift) in enumerate(scenarios):
+            arr[i].market = market_to_abi(mk, lambda x: (keep.append(x), x)[1])
+            if shift is not None:
+                buf = (C.c_double * len(shift))(*shift)
+                keep.append(buf)
+                arr[i].implied_vol_shift = C.cast(buf, C.POINTER(C.c_double))
+        n = C.c_int32(0)
+        check(self.lib, self.lib.rg_surfaces_upload(self.handle, a.ptr, arr, len(scenarios), C.byref(n)))
+        return n.value
+
     def price_risk_batch_raw(self, request: PriceRequest, config: Optional[abi.CentralDifferenceConfig] = None):
         cfg = config or abi.CentralDifferenceConfig(0.01, 0.01, 1e-4, 0.01, abi.CRN)
         a = request.to_abi()

@@ -339,6 +339,27 @@ def test_resident_surfaces_reproduce_the_calibration():
         e2.close()
 
 
+def test_uploaded_surfaces_are_resident():
+    """rg_surfaces_upload calibrates the 16-scenario batch's surfaces ahead of pricing: the first
+    priced call then copies them (prologue as short as a repeat's) and prices byte for byte what a
+    fresh engine computes."""
+    r = workloads.lv3(paths=1 << 14, steps=252)
+    scen = [(m, s) for _, m, s in workloads.crn15_scenarios(r)]
+    e1, e2 = Engine(0), Engine(0)
+    try:
+        n = e1.upload_surfaces(r, scen)
+        assert n >= 3
+        a = e1.price_scenarios_raw(r, scen)
+        t_first = e1.last_timing().prologue_ms
+        b = e2.price_scenarios_raw(r, scen)
+        t_cal = e2.last_timing().prologue_ms
+        assert [bytes(x) for x in a] == [bytes(x) for x in b]
+        assert t_first < t_cal, (t_first, t_cal)
+    finally:
+        e1.close()
+        e2.close()
+
+
 def test_large_fused_config_fp64_parity():
     """The large fused configuration's shape (5 assets, 64x32 SVI smiles, 64-point Dupire grid,
     2-factor correlation, 1260 steps) in the FP64 parity kernel, per path against the oracle."""
