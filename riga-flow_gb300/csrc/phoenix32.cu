@@ -196,8 +196,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
           }
         } else {
           const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
-          for (int q = 0; q < GEN_CH; ++q)
-            zo[q * nch] = (float)rg_qmc_normal64(tr, tb, path0 + g0 + q, dim);
+          for (int q = 0; q < GEN_CH; ++q) zo[q * nch] = rg_qmc_normal32(tr, tb, path0 + g0 + q, dim);
         }
       }
       __syncthreads();

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(P32D_THREADS, 3) phoenix32d_kernel(
         } else {
 #pragma unroll
           for (int f = 0; f < N; ++f)
-            zf[f] = (float)rg_qmc_normal64(tr, tb, path0 + gi, (uint64_t)__ldg(tb.node_k + c) * N + f);
+            zf[f] = rg_qmc_normal32(tr, tb, path0 + gi, (uint64_t)__ldg(tb.node_k + c) * N + f);
         }
 #pragma unroll
         for (int f = 0; f < N; ++f)

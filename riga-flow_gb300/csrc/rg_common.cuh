@@ -229,6 +229,27 @@ __device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevT
   return rg_probit64(u);
 }
 
+// The scrambled Halton normal of the FP32 lanes.  The reference's permuted radical inverse
+// (qmc.rs:143-153) is the sum over the k digits d_i of the point (least significant first) of
+// perm[d_i] / b^(i+1); here it is accumulated exactly as the integer R = Σ perm[d_i] b^(k-1-i)
+// (Horner over the digits, 32-bit divisions) over b^k, so the only FP64 operation is one
+// division; then the FP32 inverse normal of its 32-bit fixed-point value, with the reference's
+// clamp to [1e-12, 1 - 1e-12] taken by the FP64 inverse normal.  The FP64 parity lane keeps the
+// reference's own accumulation (rg_halton_u).
+__device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, const uint32_t* __restrict__ perm,
+                                                    uint32_t x_lo, uint32_t x_hi) {
+  uint64_t R = 0, Bk = 1;
+  while (n) {
+    const uint32_t q = n / b;
+    R = R * b + __ldg(perm + (n - q * b));
+    Bk *= b;
+    n = q;
+  }
+  const double u = (double)R / (double)Bk;
+  if (!(u >= 1.0e-12 && u <= 1.0 - 1.0e-12)) return (float)rg_probit64(u < 1.0e-12 ? 1.0e-12 : 1.0 - 1.0e-12);
+  return rg_probit32((uint32_t)(u * 4294967296.0), x_lo, x_hi);
+}
+
 // FP32 normal of the QMC lanes.
 __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTables& tb,
                                                  uint64_t point, uint64_t dim) {
@@ -236,7 +257,9 @@ __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTa
     uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
     return rg_probit32(x, tr.x_lo, tr.x_hi);
   }
-  return (float)rg_qmc_normal64(tr, tb, point, dim);
+  const uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
+  return rg_halton_normal32((uint32_t)(point + 1), __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx),
+                            tr.x_lo, tr.x_hi);
 }
 
 // ------------------------------------------------------------------ kernels (launchers) -------
