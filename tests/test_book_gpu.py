@@ -69,6 +69,37 @@ def test_fp64_book_prices_match_the_oracle(engine):
         assert _rel(g.mc_error, w.mc_error) <= 1e-9
 
 
+def _halton(b):
+    b.config.variance_reduction = workloads.VarianceReduction("halton", b.config.variance_reduction.dimension)
+    return b
+
+
+def test_fp64_halton_book_matches_the_oracle(engine):
+    """The book lanes on scrambled Halton points (the universe's normals by the FP64 permuted
+    radical inverse, qmc.rs:93-153): per-path records against the oracle."""
+    b = _halton(workloads.small_book(paths=256, n_trades=5))
+    sc = [m for _, m in workloads.book_scenarios(b.universe)][:2]
+    got = engine.book_run_paths_raw(b, sc, 0, 64)
+    want = O.book_run_paths(b, sc, 0, 64)
+    for g, w in zip(got, want):
+        assert (g.ko_step, g.qualified_steps, g.paid_periods) == (w.ko_step, w.qualified_steps, w.paid_periods)
+        for f in ("pv", "worst_final"):
+            assert _rel(getattr(g, f), getattr(w, f)) <= 1e-12, f
+
+
+def test_fp32_halton_book_within_a_tenth_of_the_standard_error(engine):
+    """FP32 Halton books take the integer radical inverse; every price stays within min(0.1 SE,
+    1bp) of the FP64 book on the same points."""
+    b64 = _halton(workloads.small_book(paths=1 << 14, n_trades=6, steps_per_year=52, max_years=2))
+    b32 = copy.deepcopy(b64)
+    b32.options = workloads.production_options()
+    sc = [m for _, m in workloads.book_scenarios(b64.universe)][:4]
+    r64 = engine.price_book_raw(b64, sc)
+    r32 = engine.price_book_raw(b32, sc)
+    for a, w in zip(r32, r64):
+        assert abs(a.pv - w.pv) <= min(0.1 * w.mc_error, 1e-4)
+
+
 def test_one_trade_book_is_bit_identical_to_price_put_leg(engine):
     req = workloads.plain3(paths=2048, steps=126)
     n = len(req.market.spots)
