@@ -262,8 +262,9 @@ def test_fp32_time_tiles_at_awkward_step_counts(engine, steps, n_scen):
         assert abs(g.pv - e.pv) <= bound, (i, g.pv, e.pv, bound)
 
 
-@pytest.mark.parametrize("n,lv", [(1, False), (3, False), (3, True), (5, True)])
-def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv):
+@pytest.mark.parametrize("n,lv,owen", [(1, False, False), (3, False, False), (3, True, False), (5, True, False),
+                                        (3, True, True)])
+def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv, owen):
     """A single scenario at 2^18 paths runs on the direct kernel (one path per thread); the same
     scenario twice runs on the tiled kernel.  Both compute every path's FP32 payoff with the same
     operations in the same order and sum warps of 32 paths by the same butterfly, so the prices
@@ -279,6 +280,8 @@ def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv):
             r.market.dividend_yields = [0.01] * n
             r.market.correlation = [[1.0 if i == j else 0.3 for j in range(n)] for i in range(n)]
             r.config.variance_reduction = VarianceReduction("sobol", n * 252)
+    if owen:
+        r.options.scrambler = abi.SCRAMBLE_OWEN
     one = engine.price_raw(r)
     assert engine.last_timing().smem_bytes < 64 * 1024 and engine.last_timing().block == 256
     base = (copy.deepcopy(r.market), [0.0] * n)
