@@ -229,28 +229,34 @@ double* SurfaceCache::lookup(const std::vector<uint8_t>& key, size_t bytes, bool
     if (e.ready && e.key == key && e.buf.bytes >= bytes) {
       e.used = tick;
       hit = true;
+      in_use.push_back(i);
       return static_cast<double*>(e.buf.ptr);
     }
-    // an entry this call is already filling is not available
-    if (std::find(pending.begin(), pending.end(), i) != pending.end()) continue;
+    // an entry this call reads or fills is not available: one launch serves all of them
+    if (std::find(in_use.begin(), in_use.end(), i) != in_use.end()) continue;
     if (victim < 0 || e.used < entries[victim].used) victim = i;
   }
-  if (victim < 0) return nullptr;  // more new surfaces in one call than entries: calibrate only
+  if (victim < 0) return nullptr;  // more surfaces in one call than entries: calibrate only
   // not resident: the least recently used entry takes this surface once the call completes
   Entry& e = entries[victim];
   e.ready = false;
   e.key = key;
   e.used = tick;
   e.buf.ensure(bytes);
+  in_use.push_back(victim);
   pending.push_back(victim);
   return static_cast<double*>(e.buf.ptr);
 }
 
-void SurfaceCache::begin_call() { pending.clear(); }
+void SurfaceCache::begin_call() {
+  pending.clear();
+  in_use.clear();
+}
 
 void SurfaceCache::commit() {
   for (int i : pending) entries[i].ready = true;
   pending.clear();
+  in_use.clear();
 }
 
 size_t SurfaceCache::device_bytes() const {
@@ -267,6 +273,7 @@ void SurfaceCache::release() {
     e.used = 0;
   }
   pending.clear();
+  in_use.clear();
 }
 
 static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {

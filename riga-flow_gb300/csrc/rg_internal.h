@@ -196,9 +196,10 @@ struct SurfaceCache {
   static constexpr int kEntries = 64;
   Entry entries[kEntries];
   uint64_t tick = 0;
-  std::vector<int> pending;
+  std::vector<int> pending;  // entries this call fills
+  std::vector<int> in_use;   // entries this call reads or fills (never evicted during it)
   // The entry for `key`: `hit` says whether it holds the calibrated surface already.
-  // (null when every entry is being filled by this call: then the surface is only calibrated)
+  // (null when every entry is in use by this call: then the surface is only calibrated)
   double* lookup(const std::vector<uint8_t>& key, size_t bytes, bool& hit);
   void begin_call();  // forget the entries of a call that did not complete
   void commit();      // the entries this call filled hold their surfaces now

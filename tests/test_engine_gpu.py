@@ -342,6 +342,29 @@ def test_resident_surfaces_reproduce_the_calibration():
         e2.close()
 
 
+def test_more_surfaces_than_resident_entries():
+    """32 scenarios on 5 assets, every spot shifted per scenario: 160 surfaces in one launch, more
+    than the engine keeps.  Priced twice on one engine (the second call mixes resident copies,
+    fresh calibrations and evictions inside one calibration launch) and once on a fresh engine:
+    all three identical byte for byte."""
+    r = workloads.lv5_large(paths=1 << 12, steps=63)
+    scen = []
+    for k in range(32):
+        m = copy.deepcopy(r.market)
+        m.spots = [sp * (1.0 + 0.001 * (k + 1) * (i + 1)) for i, sp in enumerate(m.spots)]
+        scen.append((m, [0.0] * 5))
+    e1, e2 = Engine(0), Engine(0)
+    try:
+        a = e1.price_scenarios_raw(r, scen)
+        b = e1.price_scenarios_raw(r, scen[::-1])[::-1]
+        c = e2.price_scenarios_raw(r, scen)
+        assert [bytes(x) for x in a] == [bytes(x) for x in c]
+        assert [x.pv for x in b] == [x.pv for x in c]
+    finally:
+        e1.close()
+        e2.close()
+
+
 def test_uploaded_surfaces_are_resident():
     """rg_surfaces_upload calibrates the 16-scenario batch's surfaces ahead of pricing: the first
     priced call then copies them (prologue as short as a repeat's) and prices byte for byte what a
