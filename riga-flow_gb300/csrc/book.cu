@@ -311,6 +311,12 @@ CUtensorMap increments_map(const float* incr, uint64_t npaths, uint64_t rowlen, 
   return map;
 }
 
+void increments_maps(const float* incr, uint64_t npaths, uint64_t rowlen, int U, int64_t TU, const Book32Shape& sh,
+                     CUtensorMap* maps) {
+  for (int n = 1; n <= RG_NMAX; ++n)
+    maps[n - 1] = increments_map(incr, npaths, rowlen, U, TU, sh.Pb, book_stage_steps(n, sh.TT));
+}
+
 // Paths per generation chunk: a multiple of `unit` whose increments fit the budget.
 uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t unit) {
   const uint64_t per_path = (uint64_t)U * (uint64_t)TU * elem;
@@ -435,8 +441,9 @@ void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* 
         cuda_check(cudaEventRecord(E->book_ev[1], s1), "event");
         cuda_check(cudaStreamWaitEvent(s0, E->book_ev[1], 0), "stream wait");
       }
-      const CUtensorMap tmap = increments_map(buf, np, rowlen, B.U, B.TU, sh.Pb, sh.TT);
-      launch_book_trade32(st.bk, sh, tmap, np, c * blocks_per_chunk, B.group_lo, B.group_n, partial, scratch, status, s0);
+      CUtensorMap maps[RG_NMAX];
+      increments_maps(buf, np, rowlen, B.U, B.TU, sh, maps);
+      launch_book_trade32(st.bk, sh, maps, np, c * blocks_per_chunk, B.group_lo, B.group_n, partial, scratch, status, s0);
       cuda_check(cudaEventRecord(E->book_ev[2 + (c & 1)], s0), "event");
     }
     double* dsums = static_cast<double*>(book_buf(E, BK_SUMS, sizeof(double) * pairs * RG_ACC));

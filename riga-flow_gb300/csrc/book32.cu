@@ -137,7 +137,7 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
   const int ntiles = (int)((p_hi - p_lo + Pb - 1) / Pb);
   const int ntt = (T + TT - 1) / TT;
   const int nst = ntiles * ntt;
-  const uint32_t stage_floats = (uint32_t)(5 * TT * Pb);
+  const uint32_t stage_floats = (uint32_t)(N * TT * Pb);
   const uint32_t bytes = (uint32_t)(N * TT * Pb * 4);
   // the producer: stage st of this item into buffer g & 1 (the (g >> 1)-th use of that buffer)
   auto produce = [&](uint32_t g, int st) -> bool {
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(1024, 1) book_trade32_kernel(const __grid_cons
   __shared__ int s_item;
   __shared__ double s_red[32][RG_ACC];
   float* bufs = reinterpret_cast<float*>(smem_raw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + (size_t)2 * 5 * TT * Pb * 4);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + (size_t)2 * N * TT * Pb * 4);
   uint64_t* full = bars;
   uint64_t* empty = bars + 2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -388,6 +388,14 @@ Book32Shape book32_shape(int S, int sm_count, uint64_t paths, int min_group_trad
   return sh;
 }
 
+// Steps per stage for trades on n underlyings: the stage buffers hold 5 × base steps of one
+// underlying, so fewer underlyings take proportionally deeper stages (fewer hand-overs per step) in
+// the same shared memory; at most 160 steps (a box edge may not exceed 256).
+int book_stage_steps(int n, int base) {
+  const int tt = base * 5 / (n > 0 ? n : 1);
+  return tt < 160 ? tt : 160;
+}
+
 template <int N>
 static void launch_group(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
                          uint64_t block0, int g_lo, int ng, double* partial, int32_t* counter, int* status,
@@ -407,19 +415,22 @@ static void launch_group(const BookDev& bk, const Book32Shape& sh, const CUtenso
       done[dev] = 1;
     }
   }
+  const int tt = book_stage_steps(N, sh.TT);
+  const int smem = 2 * N * tt * sh.Pb * 4 + 64;
+  if (smem > 176 * 1024) raise(RG_ERR_GPU_ERROR, "book stage buffers exceed the shared-memory limit");
   cuda_check(cudaMemsetAsync(counter, 0, sizeof(int32_t), s), "book counter reset");
-  book_trade32_kernel<N><<<sh.grid, sh.threads, sh.smem, s>>>(tmap, bk, npaths, block0, sh.blk_paths, sh.Pb, sh.TT,
-                                                              g_lo, ng, partial, counter, status);
+  book_trade32_kernel<N><<<sh.grid, sh.threads, smem, s>>>(tmap, bk, npaths, block0, sh.blk_paths, sh.Pb, tt,
+                                                           g_lo, ng, partial, counter, status);
   cuda_check(cudaGetLastError(), "book_trade32_kernel launch");
 }
 
-void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
+void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap* maps, uint64_t npaths,
                          uint64_t block0, const int* group_lo, const int* group_n, double* partial,
                          int32_t* counter, int* status, cudaStream_t s) {
-  if (sh.smem > 176 * 1024) raise(RG_ERR_GPU_ERROR, "book stage buffers exceed the shared-memory limit");
   for (int n = 1; n <= RG_NMAX; ++n) {
     const int lo = group_lo[n - 1], ng = group_n[n - 1];
     if (ng == 0) continue;
+    const CUtensorMap& tmap = maps[n - 1];
     switch (n) {
       case 1: launch_group<1>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;
       case 2: launch_group<2>(bk, sh, tmap, npaths, block0, lo, ng, partial, counter, status, s); break;

@@ -80,13 +80,14 @@ int autotune_stage(rg_book* b, const Book32Shape& base) {
     Book32Shape sh = base;
     sh.TT = tt;
     sh.smem = 2 * 5 * tt * sh.Pb * 4 + 64;
-    const CUtensorMap tmap = increments_map(static_cast<float*>(b->incr.ptr), b->P, b->rowlen, b->B.U, b->B.TU, sh.Pb, tt);
+    CUtensorMap maps[RG_NMAX];
+    increments_maps(static_cast<float*>(b->incr.ptr), b->P, b->rowlen, b->B.U, b->B.TU, sh, maps);
     int32_t* scr = static_cast<int32_t*>(b->scratch.ptr);
     float ms = 0;
     for (int rep = 0; rep < 2; ++rep) {  // the first run warms the caches
       cuda_check(cudaMemsetAsync(scr, 0, 256, E->stream), "tune status");
       cuda_check(cudaEventRecord(e0, E->stream), "event");
-      launch_book_trade32(bkd, sh, tmap, np, 0, b->B.group_lo, b->B.group_n, static_cast<double*>(tpartial.ptr),
+      launch_book_trade32(bkd, sh, maps, np, 0, b->B.group_lo, b->B.group_n, static_cast<double*>(tpartial.ptr),
                           scr, scr + 1, E->stream);
       cuda_check(cudaEventRecord(e1, E->stream), "event");
       cuda_check(cudaEventSynchronize(e1), "tune");
@@ -132,7 +133,8 @@ void price_resident(rg_book* b, const rg_market_snapshot* sc, int n_scen, rg_pri
     g.partial.ensure(sizeof(double) * blocks * pairs * RG_ACC);
     g.sums.ensure(sizeof(double) * pairs * RG_ACC);
     g.sums_host.ensure(sizeof(double) * pairs * RG_ACC + 64);
-    const CUtensorMap tmap = increments_map(static_cast<float*>(b->incr.ptr), b->P, b->rowlen, b->B.U, b->B.TU, sh.Pb, sh.TT);
+    CUtensorMap maps[RG_NMAX];
+    increments_maps(static_cast<float*>(b->incr.ptr), b->P, b->rowlen, b->B.U, b->B.TU, sh, maps);
     int32_t* scr = static_cast<int32_t*>(b->scratch.ptr);
     cuda_check(cudaStreamSynchronize(E->stream), "book before capture");
     cudaGraph_t graph = nullptr;
@@ -141,7 +143,7 @@ void price_resident(rg_book* b, const rg_market_snapshot* sc, int n_scen, rg_pri
       cuda_check(cudaMemcpyAsync(g.scen_dev.ptr, g.scen_host.ptr, scen_bytes, cudaMemcpyHostToDevice, E->stream),
                  "scenarios H2D");
       cuda_check(cudaMemsetAsync(scr, 0, 256, E->stream), "status reset");
-      launch_book_trade32(b->st.bk, sh, tmap, b->P, 0, b->B.group_lo, b->B.group_n, static_cast<double*>(g.partial.ptr),
+      launch_book_trade32(b->st.bk, sh, maps, b->P, 0, b->B.group_lo, b->B.group_n, static_cast<double*>(g.partial.ptr),
                           scr, scr + 1, E->stream);
       launch_book_reduce_strided(static_cast<double*>(g.partial.ptr), (int64_t)blocks, (int64_t)pairs * RG_ACC, RG_ACC,
                                  pairs, static_cast<double*>(g.sums.ptr), E->stream);

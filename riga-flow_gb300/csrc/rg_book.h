@@ -61,6 +61,9 @@ void point_scenarios(const ScenarioPack& sp, const uint8_t* dev, int S, BookDev&
 
 void* book_buf(rg_engine* E, int slot, size_t bytes);
 CUtensorMap increments_map(const float* incr, uint64_t npaths, uint64_t rowlen, int U, int64_t TU, int Pb, int TT);
+// One map per underlying count n, with boxes of book_stage_steps(n, sh.TT) steps: maps[n - 1].
+void increments_maps(const float* incr, uint64_t npaths, uint64_t rowlen, int U, int64_t TU, const Book32Shape& sh,
+                     CUtensorMap* maps);
 uint64_t chunk_paths(uint64_t paths, int U, int64_t TU, size_t elem, uint64_t unit);
 
 }  // namespace bk

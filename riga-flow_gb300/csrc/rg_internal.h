@@ -319,9 +319,11 @@ Book32Shape book32_shape(int S, int sm_count, uint64_t paths, int min_group_trad
 // `tmap` views the chunk's increments as [TU][U][npaths] floats (boxes of Pb paths × 1 asset × TT
 // steps) for the kernel's TMA stages.
 // One persistent launch per underlying count n with trades order[group_lo[n-1], + group_n[n-1]).
-void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap& tmap, uint64_t npaths,
+// `maps[n - 1]`: the increments' tensor map with boxes of book_stage_steps(n, sh.TT) steps.
+void launch_book_trade32(const BookDev& bk, const Book32Shape& sh, const CUtensorMap* maps, uint64_t npaths,
                          uint64_t block0, const int* group_lo, const int* group_n, double* partial,
                          int32_t* counter, int* status, cudaStream_t s);
+int book_stage_steps(int n, int base);
 // The FP32 copy of the universe Cholesky factor.
 void launch_book_l32(const double* L, int U, float* L32, cudaStream_t s);
 // Fixed-order sums over path blocks: out[pair][k] = Σ_b partial[b·stride_b + pair·stride_pair + k].
