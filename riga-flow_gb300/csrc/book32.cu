@@ -375,7 +375,9 @@ Book32Shape book32_shape(int S, int sm_count, uint64_t paths, int min_group_trad
   sh.Sb = sb;
   sh.threads = sb >= 8 ? 1024 : 256;
   sh.Pb = sh.threads / sb;
-  sh.TT = std::min(32, 4096 / sh.Pb);
+  // stage depth for five underlyings: 64 steps where the two stage buffers fit 168 KB
+  sh.TT = 64;
+  while (sh.TT > 8 && 2 * 5 * sh.TT * sh.Pb * 4 > 168 * 1024) sh.TT >>= 1;
   sh.grid = sm_count * (sh.threads == 1024 ? 1 : 4);
   // a work item is one trade over a block of 32 path tiles; a small book (few paths, or an
   // underlying-count group of few trades) takes smaller blocks, so that the smallest group's launch

@@ -64,8 +64,8 @@ int autotune_stage(rg_book* b, const Book32Shape& base) {
   rg_engine* E = b->E;
   const int S = b->B.S;
   std::vector<int> cands;
-  for (int tt : {8, 16, 32})
-    if (tt <= 4096 / base.Pb && 2 * 5 * tt * base.Pb * 4 + 64 <= 176 * 1024) cands.push_back(tt);
+  for (int tt : {8, 16, 32, 64})
+    if (2 * 5 * tt * base.Pb * 4 <= 168 * 1024) cands.push_back(tt);
   const uint64_t np = std::min<uint64_t>(b->P, (uint64_t)base.blk_paths * 4);
   const size_t pbytes = sizeof(double) * ((np + base.blk_paths - 1) / base.blk_paths) * b->B.n_trades * S * RG_ACC;
   DevBuf tpartial;
