@@ -124,8 +124,6 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
   g.dt = B.dt;
   g.sqrt_dt = std::sqrt(B.dt);
   g.inv_sqrt_dt = 1.0 / std::sqrt(B.dt);
-  g.x_lo = probit_threshold_lo();
-  g.x_hi = probit_threshold_hi();
   const int64_t need = (int64_t)B.U * B.TU;
   if (g.vr == RG_VR_SOBOL) {
     int64_t d = (int64_t)c.qmc_dimension;

@@ -267,24 +267,6 @@ void bridge_schedule_into(int64_t T, double dt, Prepared& P) {
   P.node_cf.assign(P.node_c.begin(), P.node_c.end());
 }
 
-uint32_t probit_threshold_lo() {
-  // smallest x with (x + 0.5) / 2^32 >= 0.02425 (the central branch of qmc.rs:81)
-  const double plow = 0.02425;
-  uint64_t x = (uint64_t)std::floor(plow * 4294967296.0);
-  while (x > 0 && ((double)(x - 1) + 0.5) / 4294967296.0 >= plow) --x;
-  while (((double)x + 0.5) / 4294967296.0 < plow) ++x;
-  return (uint32_t)x;
-}
-
-uint32_t probit_threshold_hi() {
-  // largest x with (x + 0.5) / 2^32 <= 1 - 0.02425
-  const double phigh = 1.0 - 0.02425;
-  uint64_t x = (uint64_t)std::floor(phigh * 4294967296.0);
-  while (((double)x + 0.5) / 4294967296.0 > phigh) --x;
-  while (x + 1 < 4294967296ULL && ((double)(x + 1) + 0.5) / 4294967296.0 <= phigh) ++x;
-  return (uint32_t)x;
-}
-
 void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepared& P) {
   const rg_phoenix_trade& t = r->trade;
   const rg_simulation_config& c = r->config;
@@ -315,8 +297,6 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
   tr.ki = t.knock_in_barrier;
   tr.memory = t.memory_coupon ? 1 : 0;
   tr.gx = c.lv_grid_x > 0 ? c.lv_grid_x : 96;  // riga-market/src/lib.rs:28
-  tr.x_lo = probit_threshold_lo();
-  tr.x_hi = probit_threshold_hi();
   P.ln_ko = std::log(tr.call_barrier);
   P.ln_cb = std::log(tr.coupon_barrier);
   P.ln_ki = std::log(tr.ki);

@@ -110,7 +110,6 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
   const int gx = tr.gx;
   const float gxm1 = (float)(gx - 1);
   const float nhdt = (float)(-0.5 * tr.dt);
-  const uint32_t x_lo = tr.x_lo, x_hi = tr.x_hi;
 
   // scenario constants: the Cholesky factor and drifts in registers; the per-asset local-vol
   // constants (warp-uniform) in shared memory
@@ -182,7 +181,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
                 ++n;
                 xs ^= __ldg(row + (__ffsll((long long)n) - 1));
               }
-              zo[q * nch] = rg_probit32(xs ^ shift, x_lo, x_hi);
+              zo[q * nch] = rg_probit32(xs ^ shift);
             }
           } else {
             const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
@@ -191,7 +190,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
                 ++n;
                 xs ^= __ldg(row + (__ffsll((long long)n) - 1));
               }
-              zo[q * nch] = rg_probit32(rg_owen(xs, dim, tr.seed), x_lo, x_hi);
+              zo[q * nch] = rg_probit32(rg_owen(xs, dim, tr.seed));
             }
           }
         } else {

@@ -12,8 +12,7 @@
 //     direction numbers at the set bits of its Gray code (lane k contributes bit k, a shuffle
 //     reduction), and the other lanes' points follow by the Gray recurrence
 //     x(n) = x(n-1) ^ v[ctz(n)] as an inclusive XOR scan over the lanes;
-//   * the digital shift (or Owen scramble) and the FP32 inverse normal of rg_common.cuh: its
-//     central branch on every lane, the tail branch for a node's queued tail draws on whole lanes;
+//   * the digital shift (or Owen scramble) and the FP32 inverse normal of rg_common.cuh;
 //   * the streamed Brownian bridge per factor with its anchor stack in shared memory, laid out
 //     [depth][factor][thread] so that a warp's accesses (the depth is warp-uniform) hit 32 banks;
 //   * the correlation with the scenario's Cholesky factor, the log-space GBM / Dupire step and the
@@ -57,16 +56,12 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     rg_path_record* __restrict__ records) {
   __shared__ float4 s_lv[32 * RG_NMAX];
   __shared__ double s_acc[P32D_WARPS][RG_ACC];
-  __shared__ uint32_t s_wq[P32D_WARPS][32 * RG_NMAX];  // per warp: inverse-normal tails of one node
   extern __shared__ float s_stk[];  // [stack depth][N][P32D_THREADS]
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t* const wq = s_wq[wib];
   const int T = (int)tr.steps;
   const int gx = tr.gx;
   const float gxm1 = (float)(gx - 1);
   const float nhdt = (float)(-0.5 * tr.dt);
-  const uint32_t x_lo = tr.x_lo, x_hi = tr.x_hi;
   // the grid holds a multiple of S warps: warp w serves scenario w % S, path groups w / S + k·(W / S)
   const int gw = blockIdx.x * P32D_WARPS + wib;
   const int nw = gridDim.x * P32D_WARPS;
@@ -119,34 +114,12 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
         const float cf = __ldg(tb.node_cf + c);
         float zf[N];
         if (tr.vr == RG_VR_SOBOL) {
-          // the central branch of the inverse normal on every lane; the lanes' tail integers (about
-          // 5% of draws, but some lane of most warps) go to the warp's queue and are resolved by
-          // whole lanes at once instead of one divergent tail pass per factor
-          uint32_t bal[N];
-          int qn = 0;
 #pragma unroll
           for (int f = 0; f < N; ++f) {
             const uint32_t xs = warp_sobol(tb.sobol + 32 * (size_t)__ldg(tb.nf_row + c * N + f), n1, lane);
-            const uint32_t xx = tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT
+            zf[f] = rg_probit32(tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT
                                     ? xs ^ __ldg(tb.nf_shift + c * N + f)
-                                    : rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed);
-            const bool tail = !(xx >= x_lo && xx <= x_hi);
-            zf[f] = rg_probit32_central(xx);
-            bal[f] = __ballot_sync(0xffffffffu, tail);
-            if (tail) wq[qn + __popc(bal[f] & lt_mask)] = xx;
-            qn += __popc(bal[f]);
-          }
-          if (qn) {
-            __syncwarp();
-            for (int j = lane; j < qn; j += 32) wq[j] = __float_as_uint(rg_probit32_tail(wq[j], x_lo));
-            __syncwarp();
-            int o = 0;
-#pragma unroll
-            for (int f = 0; f < N; ++f) {
-              if ((bal[f] >> lane) & 1u) zf[f] = __uint_as_float(wq[o + __popc(bal[f] & lt_mask)]);
-              o += __popc(bal[f]);
-            }
-            __syncwarp();
+                                    : rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed));
           }
         } else {
 #pragma unroll

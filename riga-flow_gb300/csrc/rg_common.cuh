@@ -44,7 +44,6 @@ struct DevTrade {
   double init[RG_NMAX];
   double call_barrier, coupon_barrier, coupon_rate, strike, ki;
   int32_t memory;
-  uint32_t x_lo, x_hi;  // probit branch thresholds on the 32-bit Sobol integer
 };
 
 struct DevScenario {
@@ -156,42 +155,17 @@ __device__ __forceinline__ double rg_probit64(double p) {
   }
 }
 
-// Acklam's approximation in FP32 on the 32-bit scrambled integer x (u = (x + 1/2) / 2^32), split
-// into its branches.  Central branch (x_lo <= x <= x_hi): q = u - 1/2 formed exactly from x.
-__device__ __forceinline__ float rg_probit32_central(uint32_t x) {
-  const float a0 = -3.969683028665376e1f, a1 = 2.209460984245205e2f, a2 = -2.759285104469687e2f,
-              a3 = 1.383577518672690e2f, a4 = -3.066479806614716e1f, a5 = 2.506628277459239e0f;
-  const float b0 = -5.447609879822406e1f, b1 = 1.615858368580409e2f, b2 = -1.556989798598866e2f,
-              b3 = 6.680131188771972e1f, b4 = -1.328068155288572e1f;
-  float q = fmaf((float)(int32_t)(x ^ 0x80000000u), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-  float r = q * q;
-  float num = fmaf(fmaf(fmaf(fmaf(fmaf(a0, r, a1), r, a2), r, a3), r, a4), r, a5) * q;
-  float den = fmaf(fmaf(fmaf(fmaf(fmaf(b0, r, b1), r, b2), r, b3), r, b4), r, 1.0f);
-  return __fdividef(num, den);
-}
-
-// Tail branches (x < x_lo or x > x_hi): the tail probability from x or ~x, no 1 - u cancellation.
-__device__ __forceinline__ float rg_probit32_tail(uint32_t x, uint32_t x_lo) {
-  const float c0 = -7.784894002430293e-3f, c1 = -3.223964580411365e-1f, c2 = -2.400758277161838e0f,
-              c3 = -2.549732539343734e0f, c4 = 4.374664141464968e0f, c5 = 2.938163982698783e0f;
-  const float d0 = 7.784695709041462e-3f, d1 = 3.224671290700398e-1f, d2 = 2.445134137142996e0f,
-              d3 = 3.754408661907416e0f;
-  const bool lower = x < x_lo;
-  const uint32_t t = lower ? x : ~x;
-  float p = fmaf((float)t, 2.3283064365386963e-10f, 1.1641532182693481e-10f);
-  // the fast log: its absolute error (a few 1e-7) is negligible against |ln p| >= 3.7 in the tails
-  float q = sqrtf(-2.0f * __logf(p));
-  float num = fmaf(fmaf(fmaf(fmaf(fmaf(c0, q, c1), q, c2), q, c3), q, c4), q, c5);
-  float den = fmaf(fmaf(fmaf(fmaf(d0, q, d1), q, d2), q, d3), q, 1.0f);
-  float z = __fdividef(num, den);
+// The FP32 inverse normal of u = (x + 1/2) / 2^32: CUDA's normcdfinvf on the lower-tail
+// probability min(u, 1 - u), formed exactly from x or ~x, and the sign by symmetry.  It tracks the
+// exact inverse normal, which the reference's Acklam approximation (qmc.rs:37-91) matches to
+// 1.15e-9 relative, so the FP32 lanes' normals agree with the FP64 lanes' to FP32 rounding; it
+// has no central/tail branch split in this code (Acklam's tails take ~5% of draws, so most warps
+// would run both branches).
+__device__ __forceinline__ float rg_probit32(uint32_t x) {
+  const bool lower = x < 0x80000000u;
+  const float p = fmaf((float)(lower ? x : ~x), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+  const float z = normcdfinvf(p);
   return lower ? z : -z;
-}
-
-// The same approximation in FP32, taking the 32-bit scrambled integer x (u = (x + 1/2) / 2^32).
-// The branch is decided on x against integer thresholds computed in FP64 on the host, so every
-// coordinate takes the same branch as the FP64 reference.
-__device__ __forceinline__ float rg_probit32(uint32_t x, uint32_t x_lo, uint32_t x_hi) {
-  return (x >= x_lo && x <= x_hi) ? rg_probit32_central(x) : rg_probit32_tail(x, x_lo);
 }
 
 // ------------------------------------------------------------------ Halton -------------------
@@ -234,11 +208,10 @@ __device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevT
 // (qmc.rs:143-153) is the sum over the k digits d_i of the point (least significant first) of
 // perm[d_i] / b^(i+1); here it is accumulated exactly as the integer R = Σ perm[d_i] b^(k-1-i)
 // (Horner over the digits, 32-bit divisions) over b^k, so the only FP64 operation is one
-// division; then the FP32 inverse normal of its 32-bit fixed-point value, with the reference's
-// clamp to [1e-12, 1 - 1e-12] taken by the FP64 inverse normal.  The FP64 parity lane keeps the
-// reference's own accumulation (rg_halton_u).
-__device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, const uint32_t* __restrict__ perm,
-                                                    uint32_t x_lo, uint32_t x_hi) {
+// division; then the FP32 inverse normal (as rg_probit32) of the lower-tail probability
+// min(u, 1 - u) taken in FP64, which the reference's clamp of u to [1e-12, 1 - 1e-12] bounds
+// below by 1e-12.  The FP64 parity lane keeps the reference's own accumulation (rg_halton_u).
+__device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, const uint32_t* __restrict__ perm) {
   uint64_t R = 0, Bk = 1;
   while (n) {
     const uint32_t q = n / b;
@@ -247,8 +220,8 @@ __device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, cons
     n = q;
   }
   const double u = (double)R / (double)Bk;
-  if (!(u >= 1.0e-12 && u <= 1.0 - 1.0e-12)) return (float)rg_probit64(u < 1.0e-12 ? 1.0e-12 : 1.0 - 1.0e-12);
-  return rg_probit32((uint32_t)(u * 4294967296.0), x_lo, x_hi);
+  const float z = normcdfinvf((float)fmax(fmin(u, 1.0 - u), 1.0e-12));
+  return u < 0.5 ? z : -z;
 }
 
 // FP32 normal of the QMC lanes.
@@ -256,11 +229,10 @@ __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTa
                                                  uint64_t point, uint64_t dim) {
   if (tr.vr == RG_VR_SOBOL) {
     uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
-    return rg_probit32(x, tr.x_lo, tr.x_hi);
+    return rg_probit32(x);
   }
   const uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
-  return rg_halton_normal32((uint32_t)(point + 1), __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx),
-                            tr.x_lo, tr.x_hi);
+  return rg_halton_normal32((uint32_t)(point + 1), __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx));
 }
 
 // ------------------------------------------------------------------ kernels (launchers) -------

@@ -259,8 +259,6 @@ void launch_reduce(const double* partial, int grid, int n_scen, double* out, cud
 
 // The 32-bit Sobol integers at which the inverse normal switches between its central and tail
 // branches (computed in FP64 so the FP32 kernels branch exactly as the reference does).
-uint32_t probit_threshold_lo();
-uint32_t probit_threshold_hi();
 // Cholesky factor (with the reference's PSD clamp) of one n×n correlation, n <= RG_BOOK_MAX_UNIVERSE,
 // by one device thread; `work` holds 2·n·n doubles.
 void launch_cholesky_big(const double* c, int n, double* l, double* work, cudaStream_t s);
