@@ -159,6 +159,10 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
     d.ln_cb = (float)std::log(d.coupon_barrier);
     d.ln_ki = (float)std::log(d.ki);
     d.coupon_f = (float)d.coupon_rate;
+    d.strike_f = (float)d.strike;
+    d.ps_a = std::max<int32_t>(1, d.T / std::max<int32_t>(d.periods, 1));
+    d.inc_a = (float)(d.coupon_rate / (double)d.ps_a);
+    d.inc_b = (float)(d.coupon_rate / (double)(d.ps_a + 1));
   }
   // work order: grouped by underlying count (one launch each), longest trades first in a group
   B.order.resize(B.n_trades);
@@ -275,6 +279,8 @@ ScenarioPack pack_book_scenarios(const BookPlan& B) {
   sp.o_p32 = sp.pk.add(B.pair32);
   sp.o_df = sp.pk.add(B.df);
   sp.o_dfm = sp.pk.add(B.dfm);
+  sp.o_df_f = sp.pk.add(std::vector<float>(B.df.begin(), B.df.end()));
+  sp.o_dfm_f = sp.pk.add(std::vector<float>(B.dfm.begin(), B.dfm.end()));
   return sp;
 }
 
@@ -284,6 +290,8 @@ void point_scenarios(const ScenarioPack& sp, const uint8_t* dev, int S, BookDev&
   bk.pair32 = reinterpret_cast<const BookPair32*>(dev + sp.o_p32);
   bk.df = reinterpret_cast<const double*>(dev + sp.o_df);
   bk.dfm = reinterpret_cast<const double*>(dev + sp.o_dfm);
+  bk.df_f = reinterpret_cast<const float*>(dev + sp.o_df_f);
+  bk.dfm_f = reinterpret_cast<const float*>(dev + sp.o_dfm_f);
 }
 
 // The tensor map of one chunk's FP32 increments, viewed as [TU][U][npaths] with rows of `rowlen`
@@ -351,7 +359,7 @@ size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
   const uint64_t blocks = fp32 ? (P + unit - 1) / unit : ((PC + 127) / 128) * chunks;
   b += (size_t)blocks * pairs * RG_ACC * 8 + pairs * RG_ACC * 8;
   size_t sob_rows = r->config.dim_mode == RG_DIM_FULL ? U * TU : 512;
-  b += sob_rows * 128 + TU * 32 + S * TU * 8 + pairs * 96 + (size_t)r->n_trades * 256 + (size_t(64) << 10);
+  b += sob_rows * 128 + TU * 32 + S * TU * 12 + pairs * 100 + (size_t)r->n_trades * 256 + (size_t(64) << 10);
   return b + b / 8 + (size_t(1) << 20);
 }
 

@@ -131,8 +131,8 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
     drift[f] = pc.drift[f];
     sig[f] = pc.sig[f];
   }
-  const double* df = bk.df + (size_t)ss * bk.TU;
-  const float dfm = (float)bk.dfm[(size_t)j * bk.S + ss];
+  const float* df = bk.df_f + (size_t)ss * bk.TU;
+  const float dfm = bk.dfm_f[(size_t)j * bk.S + ss];
   const int T = tr.T, PER = tr.periods;
   const int ntiles = (int)((p_hi - p_lo + Pb - 1) / Pb);
   const int ntt = (T + TT - 1) / TT;
@@ -159,9 +159,7 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
   bool fixed = false;
   auto accr = [&](int q) {
     const int64_t a = (int64_t)T * (q + 1) / PER, b = (int64_t)T * q / PER;
-    int64_t ps = a > b ? a - b : 0;
-    if (ps < 1) ps = 1;
-    return (float)(tr.coupon_rate / (double)ps);
+    return a - b <= tr.ps_a ? tr.inc_a : tr.inc_b;  // coupon_rate / max(1, a - b), rounded to FP32
   };
   for (int st = 0; st < nst; ++st, ++G) {
     const int tile = st / ntt, k = st % ntt;
@@ -202,7 +200,7 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
       const float due = fixed ? tr.coupon_f : (float)qual * inc;
       const float carry = due > 0.0f ? (float)unpaid * tr.coupon_f : 0.0f;
       if (due + carry > 0.0f) {
-        const float d = (float)__ldg(df + t);
+        const float d = __ldg(df + t);
         cpv = fmaf(due, d, cpv);
         mpv = fmaf(carry, d, mpv);
         received = true;
@@ -238,7 +236,7 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
           } else {
             const float due = fixed ? tr.coupon_f : (float)qual * inc;
             if (due > 0.0f) {
-              const float d = (float)__ldg(df + t);
+              const float d = __ldg(df + t);
               cpv = fmaf(due, d, cpv);
               mpv = fmaf((float)unpaid * tr.coupon_f, d, mpv);
               unpaid = 0;
@@ -267,10 +265,10 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
       // path close (note.rs:221-258) in FP32; each slot summed over the warp's 32 paths by a
       // fixed butterfly and kept by lane k
       const bool ko = ko_step >= 0;
-      const float funding = ok ? (ko ? (float)__ldg(df + ko_step) : dfm) : 0.0f;
+      const float funding = ok ? (ko ? __ldg(df + ko_step) : dfm) : 0.0f;
       const bool hit_ki = ok && worst <= tr.ln_ki;
       const bool put_ok = hit_ki && !ko;
-      const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * dfm : 0.0f;
+      const float put = put_ok ? fmaxf(tr.strike_f - expf(worst), 0.0f) * dfm : 0.0f;
       const float cn = cpv + mpv;
       const float pv1 = ok ? (funding - 1.0f) + cn - put : 0.0f;
       const bool kof = ok && ko, rec = ok && received;

@@ -297,6 +297,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
          o_ncf = pk.add(P.node_cf), o_nfr = pk.add(P.nf_row), o_nfs = pk.add(P.nf_shift);
   size_t o_ti = pk.add(P.lv_ti), o_tw = pk.add(P.lv_tw), o_twf = pk.add(P.lv_twf);
   size_t o_df = pk.add(P.df), o_dfm = pk.add(P.df_mat);
+  size_t o_acf = pk.add(P.accr_f), o_dff = pk.add(P.df_f), o_dfmf = pk.add(P.df_mat_f);
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
   // local-vol surfaces: inputs (grids) and outputs
   const int gx = tr.gx;
@@ -394,6 +395,9 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   tb.lv_logs = reinterpret_cast<const double*>(base + o_logs);
   tb.df = reinterpret_cast<const double*>(base + o_df);
   tb.df_mat = reinterpret_cast<const double*>(base + o_dfm);
+  tb.accr_f = reinterpret_cast<const float*>(base + o_acf);
+  tb.df_f = reinterpret_cast<const float*>(base + o_dff);
+  tb.df_mat_f = reinterpret_cast<const float*>(base + o_dfmf);
   tb.lv_nt = P.lv_nt_max;
   S.scen = reinterpret_cast<DevScenario*>(base + o_scen);
   S.scen32 = reinterpret_cast<DevScen32*>(base + o_s32);
@@ -619,7 +623,7 @@ size_t estimate_price_bytes(const rg_price_request* r, int n_scen) {
   const size_t T = (size_t)(r->trade.steps > 0 ? r->trade.steps : 1);
   const bool fp32 = r->config.precision == RG_PRECISION_FP32;
   size_t sob_rows = r->config.dim_mode == RG_DIM_FULL ? n * T : 512;
-  size_t b = sob_rows * 128 + n * T * 64 + S * T * 8 + S * 1024 + (size_t(64) << 10);  // tables
+  size_t b = sob_rows * 128 + n * T * 64 + S * T * 12 + S * 1024 + (size_t(64) << 10);  // tables
   if (r->n_local_vol) {
     const size_t gx = (size_t)(r->config.lv_grid_x > 0 ? r->config.lv_grid_x : 96);
     size_t nt = 1, nk = 1;

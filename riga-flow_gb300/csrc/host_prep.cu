@@ -295,6 +295,8 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
   tr.coupon_rate = t.has_coupon_rate ? t.coupon_rate : 0.0;
   tr.strike = t.strike;
   tr.ki = t.knock_in_barrier;
+  tr.coupon_f = (float)tr.coupon_rate;
+  tr.strike_f = (float)tr.strike;
   tr.memory = t.memory_coupon ? 1 : 0;
   tr.gx = c.lv_grid_x > 0 ? c.lv_grid_x : 96;  // riga-market/src/lib.rs:28
   P.ln_ko = std::log(tr.call_barrier);
@@ -337,6 +339,7 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
     int64_t ps = std::max<int64_t>(a > b ? a - b : 0, 1);
     P.accr_inc[p] = tr.coupon_rate / (double)ps;
   }
+  P.accr_f.assign(P.accr_inc.begin(), P.accr_inc.end());
 
   bridge_schedule_into(T, tr.dt, P);
   // per (node, factor): the QMC dimension n·k + f reduced to its table row, and its shift mask
@@ -445,6 +448,8 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
     }
     P.df_mat[i] = rg_exp64(-m.risk_free_rate * t.maturity_years);
   }
+  P.df_f.assign(P.df.begin(), P.df.end());
+  P.df_mat_f.assign(P.df_mat.begin(), P.df_mat.end());
   P.n_surf = (int)P.surfaces.size();
   // surface row offsets in the packed local-vol tables
   if (tr.has_lv) {

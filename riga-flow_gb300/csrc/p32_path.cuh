@@ -18,7 +18,7 @@ struct P32Phoenix {
 template <bool REC, class Period>
 __device__ __forceinline__ void p32_phoenix_step(P32Phoenix& st, uint32_t fl, int t, float wmin, float ln_cb,
                                                  float ln_ko, const DevTrade& tr, const DevTables& tb,
-                                                 const double* __restrict__ df, Period period) {
+                                                 const float* __restrict__ df, Period period) {
   if (fl & STEP_PERIOD_RESET) st.qual = 0;
   if ((fl & STEP_ACCRUE) && wmin >= ln_cb) {
     ++st.qual;
@@ -27,23 +27,21 @@ __device__ __forceinline__ void p32_phoenix_step(P32Phoenix& st, uint32_t fl, in
   if ((fl & STEP_CALL_ACTIVE) && wmin >= ln_ko) {
     st.alive = false;
     st.ko_step = t;
-    const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                            : (float)st.qual * (float)__ldg(tb.accr_inc + period());
-    const float carry = due > 0.0f ? (float)st.unpaid * (float)tr.coupon_rate : 0.0f;
+    const float due = (fl & STEP_FIXED_DUE) ? tr.coupon_f : (float)st.qual * __ldg(tb.accr_f + period());
+    const float carry = due > 0.0f ? (float)st.unpaid * tr.coupon_f : 0.0f;
     if (due + carry > 0.0f) {
-      const float d = (float)__ldg(df + t);
+      const float d = __ldg(df + t);
       st.cpv = fmaf(due, d, st.cpv);
       st.mpv = fmaf(carry, d, st.mpv);
       st.received = true;
       if (REC) ++st.paid;
     }
   } else if (fl & STEP_PERIOD_END) {
-    const float due = (fl & STEP_FIXED_DUE) ? (float)tr.coupon_rate
-                                            : (float)st.qual * (float)__ldg(tb.accr_inc + period());
+    const float due = (fl & STEP_FIXED_DUE) ? tr.coupon_f : (float)st.qual * __ldg(tb.accr_f + period());
     if (due > 0.0f) {
-      const float d = (float)__ldg(df + t);
+      const float d = __ldg(df + t);
       st.cpv = fmaf(due, d, st.cpv);
-      st.mpv = fmaf((float)st.unpaid * (float)tr.coupon_rate, d, st.mpv);
+      st.mpv = fmaf((float)st.unpaid * tr.coupon_f, d, st.mpv);
       st.unpaid = 0;
       st.received = true;
       if (REC) ++st.paid;
@@ -67,11 +65,11 @@ __device__ __forceinline__ void p32_close_path(const DevTrade& tr, const DevTabl
   for (int k = 0; k < RG_ACC; ++k) out[k] = 0.0f;
   if (!ok) return;
   const bool ko = ko_step >= 0;
-  const float df_mat = (float)__ldg(tb.df_mat + sc);
-  const float funding = ko ? (float)__ldg(tb.df + (size_t)sc * T + ko_step) : df_mat;
+  const float df_mat = __ldg(tb.df_mat_f + sc);
+  const float funding = ko ? __ldg(tb.df_f + (size_t)sc * T + ko_step) : df_mat;
   const bool hit_ki = worst <= ln_ki;
   const bool put_ok = hit_ki && !ko;
-  const float put = put_ok ? fmaxf((float)tr.strike - expf(worst), 0.0f) * df_mat : 0.0f;
+  const float put = put_ok ? fmaxf(tr.strike_f - expf(worst), 0.0f) * df_mat : 0.0f;
   const float cn = cpv + mpv;
   const float pv1 = (funding - 1.0f) + cn - put;
   out[ACC_PV] = pv1;

@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
           }
           worst = wmin;
           if (ph.alive)
-            p32_phoenix_step<REC>(ph, s_flags[tt], t0 + tt, wmin, ln_cb, ln_ko, tr, tb, tb.df + (size_t)ss * T,
+            p32_phoenix_step<REC>(ph, s_flags[tt], t0 + tt, wmin, ln_cb, ln_ko, tr, tb, tb.df_f + (size_t)ss * T,
                                   [&] { return s_per[tt]; });
         }
       }

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
       }
       worst = wmin;
       if (ph.alive)  // Phoenix state machine (note.rs:150-218)
-        p32_phoenix_step<REC>(ph, __ldg(tb.step_flags + t), t, wmin, ln_cb, ln_ko, tr, tb, tb.df + (size_t)s * T,
+        p32_phoenix_step<REC>(ph, __ldg(tb.step_flags + t), t, wmin, ln_cb, ln_ko, tr, tb, tb.df_f + (size_t)s * T,
                               [&] { return __ldg(tb.step_period + t); });
     }
     // path close (note.rs:221-258)

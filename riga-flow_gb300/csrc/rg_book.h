@@ -54,7 +54,7 @@ BookStaged stage_book_static(DevBuf& tables, cudaStream_t st, const rg_book_requ
 // The scenario tables packed for one H2D copy; point_scenarios aims `bk` at their device copy.
 struct ScenarioPack {
   Pack pk;
-  size_t o_scen = 0, o_p32 = 0, o_df = 0, o_dfm = 0;
+  size_t o_scen = 0, o_p32 = 0, o_df = 0, o_dfm = 0, o_df_f = 0, o_dfm_f = 0;
 };
 ScenarioPack pack_book_scenarios(const BookPlan& B);
 void point_scenarios(const ScenarioPack& sp, const uint8_t* dev, int S, BookDev& bk);

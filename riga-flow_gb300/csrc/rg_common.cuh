@@ -43,6 +43,7 @@ struct DevTrade {
   double dt, sqrt_dt, inv_sqrt_dt, maturity;
   double init[RG_NMAX];
   double call_barrier, coupon_barrier, coupon_rate, strike, ki;
+  float coupon_f, strike_f;  // coupon_rate and strike rounded to FP32 for the FP32 kernels
   int32_t memory;
 };
 
@@ -79,6 +80,9 @@ struct DevTables {
   const double* lv_logs;       // [surfaces][gx] log-strike axis
   const double* df;            // [scenarios][T] exp(-r_s * (t+1) dt)
   const double* df_mat;        // [scenarios] exp(-r_s * maturity)
+  const float* accr_f;         // accr_inc, df and df_mat rounded to FP32 for the FP32 kernels
+  const float* df_f;
+  const float* df_mat_f;
   int32_t lv_nt;
 };
 

@@ -98,6 +98,7 @@ struct Prepared {
   std::vector<uint32_t> step_flags;
   std::vector<int32_t> step_period;
   std::vector<double> accr_inc;
+  std::vector<float> accr_f;  // accr_inc in FP32 (the FP32 kernels read no FP64 per step)
   std::vector<int32_t> node_off, node_k;
   std::vector<double> node_c;
   std::vector<float> node_cf;
@@ -109,6 +110,7 @@ struct Prepared {
   std::vector<DevScenario> scen;
   std::vector<DevScen32> scen32;
   std::vector<double> df, df_mat;
+  std::vector<float> df_f, df_mat_f;  // the same in FP32
   std::vector<SurfaceKey> surfaces;
   std::vector<int32_t> surf_nt;  // tenor count of each surface
   std::vector<double> asset_log_lo, asset_log_hi;
@@ -271,7 +273,11 @@ struct BookTradeDev {
   int32_t fixed_first, memory;
   double init[RG_NMAX];
   double maturity, call_barrier, coupon_barrier, coupon_rate, strike, ki;
-  float ln_ko, ln_cb, ln_ki, coupon_f;
+  float ln_ko, ln_cb, ln_ki, coupon_f, strike_f;
+  // the FP32 coupon increment coupon_rate / period_steps: a period has ps_a = max(1, T / periods)
+  // steps (inc_a) or ps_a + 1 (inc_b)
+  float inc_a, inc_b;
+  int32_t ps_a;
 };
 // One scenario of a book: a market of the universe.
 struct BookScenDev {
@@ -291,6 +297,8 @@ struct BookDev {
   const BookPair32* pair32;    // [n_trades][S]
   const double* df;            // [S][TU]  exp(-r_s (t+1) dt)
   const double* dfm;           // [n_trades][S] exp(-r_s maturity_j)
+  const float* df_f;           // df and dfm rounded to FP32 for the FP32 scan
+  const float* dfm_f;
   const double* L;             // [U][U] universe Cholesky factor (FP64)
   const float* L32;            // [U][U] the same in FP32
   const int32_t* order;        // [n_trades] trade order of the work items (longest first)
