@@ -298,6 +298,13 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   size_t o_ti = pk.add(P.lv_ti), o_tw = pk.add(P.lv_tw), o_twf = pk.add(P.lv_twf);
   size_t o_df = pk.add(P.df), o_dfm = pk.add(P.df_mat);
   size_t o_acf = pk.add(P.accr_f), o_dff = pk.add(P.df_f), o_dfmf = pk.add(P.df_mat_f);
+  // the FP32 tiled kernel's bridge plans, one per tile depth it may launch with
+  BridgePlans bp;
+  size_t o_bplan = 0;
+  if (req->config.precision == RG_PRECISION_FP32) {
+    p32_bridge_plans(P, bp);
+    o_bplan = pk.add(bp.words);
+  }
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
   // local-vol surfaces: inputs (grids) and outputs
   const int gx = tr.gx;
@@ -398,6 +405,12 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   tb.accr_f = reinterpret_cast<const float*>(base + o_acf);
   tb.df_f = reinterpret_cast<const float*>(base + o_dff);
   tb.df_mat_f = reinterpret_cast<const float*>(base + o_dfmf);
+  tb.bplan = reinterpret_cast<const uint32_t*>(base + o_bplan);
+  tb.n_bplan = bp.n;
+  for (int i = 0; i < RG_BPLAN_MAX; ++i) {
+    tb.bplan_tt[i] = i < bp.n ? bp.tt[i] : 0;
+    tb.bplan_at[i] = i < bp.n ? bp.at[i] : 0;
+  }
   tb.lv_nt = P.lv_nt_max;
   S.scen = reinterpret_cast<DevScenario*>(base + o_scen);
   S.scen32 = reinterpret_cast<DevScen32*>(base + o_s32);
@@ -635,6 +648,7 @@ size_t estimate_price_bytes(const rg_price_request* r, int n_scen) {
     b += surf * ((2 * nt * gx + gx) * 8 + (4 * nt * gx + gx + 6 * nt * nk) * 8);  // calibration
     if (fp32) b += surf * T * gx * 8;                                            // step rows
   }
+  if (fp32) b += T * 160;  // bridge plans of the tiled kernel
   const size_t grid = fp32 ? (size_t)device_info().sm_count * 2 : 152 * 16;
   b += grid * std::min<size_t>(S, 32) * RG_ACC * 8 + S * RG_ACC * 8;  // partial and reduced sums
   if (r->config.trace_level != RG_TRACE_OFF) b += (size_t)r->config.paths * 4;

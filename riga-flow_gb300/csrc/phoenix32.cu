@@ -11,8 +11,10 @@
 //      x(n) = x(n-1) ^ v[ctz(n)] (one load each), the digital shift (or Owen scramble) and the
 //      FP32 inverse normal; the standard normals of every node the tile consumes land in shared
 //      memory.  The step schedule of the tile is staged next to them.
-//   B. bridge — one chain per (path, factor) walks the tile's steps through the streamed
-//      Brownian bridge and writes the uncorrelated increments dW[step][factor][path].
+//   B. bridge — the tile's bridge nodes of every (path, factor) chain, evaluated level by level
+//      from a host plan of the streamed Brownian bridge's dependencies (each warp owns a slice of
+//      the chains, its lanes take one level's nodes at once), then the uncorrelated increments
+//      dW[step][factor][path] and the state carried to the next tile.
 //   S. scenario stepping — every (path, scenario) thread correlates dW with its own Cholesky
 //      factor (the bridge is linear, so L·bridge(z) = bridge(L·z)), steps ln(S/S0) under flat vol
 //      or its scenario's Dupire surface and runs the Phoenix state machine.
@@ -37,7 +39,7 @@ namespace rg {
 // Byte offsets of the kernel's dynamic shared-memory regions, 16-byte aligned, and their total.
 // Computed by the same function on the host (to size the launch) and in the kernel (to carve).
 struct P32Layout {
-  uint32_t acc, lv, flags, per, noff, ncf, wcur, stack, z, dw, total;
+  uint32_t acc, lv, flags, per, noff, ncf, plan, z, dw, total;
 };
 
 __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, int NNmax, int stack_max,
@@ -50,9 +52,11 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
   };
   const uint32_t PbN = (uint32_t)(Pb * N);
   const int g = Pb < 32 ? Pb : 32;
-  // normals of the tile's bridge nodes, one row of Pb + 4 floats per (node, factor): the padding
-  // spreads a generation pass's stores (lanes stride GEN_CH·nch apart) over distinct banks
-  const uint32_t zb = (uint32_t)NNmax * (uint32_t)N * (uint32_t)(Pb + 4) * 4u;
+  // rows of N·(Pb + 4) floats, one float per (factor, path): the normals of the tile's bridge nodes
+  // (rows 0 .. NNmax-1, overwritten by their bridge values), then the bridge state carried between
+  // tiles: the value at the tile start (row NNmax) and the stack (rows NNmax + 1 + slot).  The
+  // padding spreads a generation pass's stores (lanes stride GEN_CH·nch apart) over distinct banks
+  const uint32_t zb = (uint32_t)(NNmax + 1 + stack_max) * (uint32_t)N * (uint32_t)(Pb + 4) * 4u;
   const uint32_t rb = (uint32_t)(threads / g) * RG_ACC * 8u;  // per-tile reduction, aliases Z
   put(L.acc, (uint32_t)S * RG_ACC * 8u);
   put(L.lv, (uint32_t)(S * N) * 16u);
@@ -60,8 +64,8 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
   put(L.per, (uint32_t)TT * 4u);
   put(L.noff, (uint32_t)(TT + 1) * 4u);
   put(L.ncf, (uint32_t)NNmax * 4u);
-  put(L.wcur, PbN * 4u);
-  put(L.stack, (uint32_t)stack_max * PbN * 4u);
+  // the tile's bridge plan: node words, level offsets, step codes, stack entries
+  put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + TT + stack_max) * 4u);
   put(L.z, zb > rb ? zb : rb);
   put(L.dw, (uint32_t)TT * PbN * 4u);
   L.total = o;
@@ -72,12 +76,13 @@ template <int N, bool LV, bool REC>
 __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
     const DevScen32* __restrict__ scen32, int S, int Pb, int TT, int NNmax, int stack_max,
-    float ln_ko, float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths,
+    float ln_ko, float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths, const uint32_t* __restrict__ plan,
     double* __restrict__ partial, int32_t* __restrict__ ko_steps, rg_path_record* __restrict__ records) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, lane = tid & 31;
   const int PbN = Pb * N;
   const int nch = Pb / GEN_CH;
+  const int lg_pb = __ffs(Pb) - 1;  // Pb is a power of two
   const int T = (int)tr.steps;
   // ---- shared-memory carve-up (the host sizes the launch from the same layout)
   const P32Layout L = p32_layout(S, N, Pb, TT, NNmax, stack_max, (int)blockDim.x);
@@ -97,8 +102,10 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
   int32_t* s_per = reinterpret_cast<int32_t*>(smem_raw + L.per);
   int32_t* s_noff = reinterpret_cast<int32_t*>(smem_raw + L.noff);
   float* s_ncf = reinterpret_cast<float*>(smem_raw + L.ncf);
-  float* wcur = reinterpret_cast<float*>(smem_raw + L.wcur);
-  float* stack = reinterpret_cast<float*>(smem_raw + L.stack);
+  uint32_t* s_pnode = reinterpret_cast<uint32_t*>(smem_raw + L.plan);
+  uint32_t* s_plev = s_pnode + NNmax;
+  uint32_t* s_pstep = s_plev + NNmax + 1;
+  uint32_t* s_pstk = s_pstep + TT;
   float* Z = reinterpret_cast<float*>(smem_raw + L.z);
   float* dW = reinterpret_cast<float*>(smem_raw + L.dw);
   double* red = reinterpret_cast<double*>(Z);  // reduction scratch, reused after the time loop
@@ -142,7 +149,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t tile0 = tile * Pb;
-    for (int c = tid; c < PbN; c += blockDim.x) wcur[c] = 0.0f;
+    for (int i = tid; i < N * (Pb + 4); i += blockDim.x) Z[(size_t)NNmax * N * (Pb + 4) + i] = 0.0f;  // W(0)
     const uint64_t gi = tile0 + pl;
     const bool ok = lane_ok && gi < npaths;
     float x[N];
@@ -150,7 +157,6 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
     for (int f = 0; f < N; ++f) x[f] = lvc[f].w;
     P32Phoenix ph;
     float worst = 0.0f;
-    int sp = 0;
     for (int t0 = 0; t0 < T; t0 += TT) {
       const int tn = min(TT, T - t0);
       const int n0 = __ldg(tb.node_off + t0), n1 = __ldg(tb.node_off + t0 + tn);
@@ -162,6 +168,16 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
       }
       for (int i = tid; i <= tn; i += blockDim.x) s_noff[i] = __ldg(tb.node_off + t0 + i);
       for (int i = tid; i < nn; i += blockDim.x) s_ncf[i] = __ldg(tb.node_cf + n0 + i);
+      const uint32_t* hd = plan + 1 + (size_t)(t0 / TT) * 6;
+      const uint32_t nlev = __ldg(hd + 2), stk_cnt = __ldg(hd + 4);
+      {
+        const uint32_t node_base = __ldg(hd), lev_base = __ldg(hd + 1), stk_base = __ldg(hd + 3),
+                       steps_base = __ldg(hd + 5);
+        for (int i = tid; i < nn; i += blockDim.x) s_pnode[i] = __ldg(plan + node_base + i);
+        for (int i = tid; i <= (int)nlev; i += blockDim.x) s_plev[i] = __ldg(plan + lev_base + i);
+        for (int i = tid; i < tn; i += blockDim.x) s_pstep[i] = __ldg(plan + steps_base + t0 + i);
+        for (int i = tid; i < (int)stk_cnt; i += blockDim.x) s_pstk[i] = __ldg(plan + stk_base + i);
+      }
       const int ntask = nn * N * nch;
       for (int task = tid; task < ntask; task += blockDim.x) {
         const int c = task % nch, rem = task / nch, f = rem % N, j = rem / N;
@@ -199,31 +215,66 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
         }
       }
       __syncthreads();
-      // ---- B: streamed bridge, one chain per (path, factor)
-      for (int c = tid; c < PbN; c += blockDim.x) {
-        const int p = c % Pb, f = c / Pb;
-        if (tile0 + p >= npaths) continue;
-        const int pc = p / GEN_CH, pq = p % GEN_CH;
-        float wc = wcur[c];
-        int lsp = sp;
-        for (int tt = 0; tt < tn; ++tt) {
-          const int e0 = s_noff[tt], e1 = s_noff[tt + 1];
-          for (int nd = e0; nd < e1; ++nd) {
-            const int j = nd - n0;
-            const float z = Z[(size_t)(j * N + f) * (Pb + 4) + pq * nch + pc];
-            const float cf = s_ncf[j];
-            const float w = nd == 0 ? z * cf : fmaf(z, cf, 0.5f * (wc + stack[(lsp - 1) * PbN + c]));
-            stack[lsp * PbN + c] = w;
-            ++lsp;
-          }
-          --lsp;
-          const float wn = stack[lsp * PbN + c];
-          dW[(tt * N + f) * Pb + p] = wn - wc;
-          wc = wn;
+      // ---- B: the tile's bridge nodes in the plan's dependency levels, then the increments.  Warp
+      // w owns chains [w·cpw, w·cpw + nc) (chain c = path c % Pb, factor c / Pb): its lanes
+      // evaluate one level's nodes of those chains at once, W = z·c + (W_left + W_right) / 2 —
+      // the streamed bridge's arithmetic on the same anchors, so the values are identical — each
+      // written over its normal in Z; then dW of every step, and the state carried to the next
+      // tile (the value at the tile end, the stack entries pushed in the tile).  Every anchor is
+      // a row of Z, so an evaluation is four loads and one FMA.
+      {
+        const int zs = N * (Pb + 4);
+        const int nwarp = (int)(blockDim.x >> 5);
+        const int cpw = (PbN + nwarp - 1) / nwarp;  // at most 64 (host-checked)
+        const int c_lo = (tid >> 5) * cpw;
+        const int nc = max(0, min(cpw, PbN - c_lo));
+        const int nc1 = nc < 32 ? max(nc, 1) : 32;
+        const int G = 32 / nc1, q0 = lane / nc1;  // G node slots at once; this lane's first
+        const bool lane_on = nc > 0 && lane < G * nc1;
+        const int cA = c_lo + lane % nc1, cB = cA + 32;  // this lane's chains (B when nc > 32)
+        const bool hasB = lane_on && cB < c_lo + nc;
+        auto zoff_of = [&](int c) {
+          const int p = c & (Pb - 1);
+          return (c >> lg_pb) * (Pb + 4) + (p & (GEN_CH - 1)) * nch + (p >> 3);
+        };
+        const int zA = zoff_of(cA), zB = zoff_of(cB);
+        auto eval = [&](uint32_t e, float cf, int zo) {
+          float* zp = Z + (int)(e & 511u) * zs + zo;
+          const float z = *zp;
+          const float l = Z[(int)((e >> 9) & 511u) * zs + zo], r = Z[(int)((e >> 18) & 511u) * zs + zo];
+          *zp = (e >> 27) ? z * cf : fmaf(z, cf, 0.5f * (l + r));
+        };
+        for (uint32_t L = 0; L < nlev; ++L) {
+          const int a = (int)s_plev[L], b = (int)s_plev[L + 1];
+          if (lane_on)
+            for (int q = a + q0; q < b; q += G) {
+              const uint32_t e = s_pnode[q];
+              const float cf = s_ncf[e & 511u];
+              eval(e, cf, zA);
+              if (hasB) eval(e, cf, zB);
+            }
+          __syncwarp();
         }
-        wcur[c] = wc;
+        if (lane_on)
+          for (int tt = q0; tt < tn; tt += G) {
+            const int hi = (int)s_pstep[tt] * zs;
+            const int lo = tt == 0 ? NNmax * zs : (int)s_pstep[tt - 1] * zs;
+            dW[tt * PbN + cA] = Z[hi + zA] - Z[lo + zA];
+            if (hasB) dW[tt * PbN + cB] = Z[hi + zB] - Z[lo + zB];
+          }
+        __syncwarp();
+        if (lane_on && q0 == 0) {
+          const int wrow = (int)s_pstep[tn - 1] * zs;
+          const float wnA = Z[wrow + zA], wnB = hasB ? Z[wrow + zB] : 0.0f;
+          for (uint32_t k = 0; k < stk_cnt; ++k) {
+            const uint32_t e = s_pstk[k];  // (destination row, tile node)
+            Z[(int)(e >> 9) * zs + zA] = Z[(int)(e & 511u) * zs + zA];
+            if (hasB) Z[(int)(e >> 9) * zs + zB] = Z[(int)(e & 511u) * zs + zB];
+          }
+          Z[NNmax * zs + zA] = wnA;
+          if (hasB) Z[NNmax * zs + zB] = wnB;
+        }
       }
-      sp += nn - tn;
       __syncthreads();
       // ---- S: scenario stepping
       if (ok) {
@@ -312,21 +363,11 @@ static const void* select_kernel(int n, bool lv, bool rec) {
   }
 }
 
-Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
-  Fp32Shape sh{};
-  if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
-  if (p32_direct(P, npaths)) {
-    // nothing for the scenarios to share: the per-thread kernel without shared-memory tiles
-    sh.direct = 1;
-    sh.Sb = P.n_scen;
-    sh.threads = 256;
-    sh.grid = phoenix32d_grid(P, npaths, sm_count);
-    sh.smem = P.stack_max * P.n * 256 * (int)sizeof(float);  // the bridge stacks (dynamic)
-    return sh;
-  }
-  // scenario slots: S rounded up to a power of two, at least 4 (two scenarios run padded: a CTA
-  // of 1024 threads on half the slots beats both the direct kernel and a smaller CTA); the
-  // largest block of 1024, 512 or 256 threads whose shared-memory layout fits
+// The tiled kernel's block and formula tile depth.  Scenario slots: S rounded up to a power of
+// two, at least 4 (two scenarios run padded: a CTA of 1024 threads on half the slots beats both
+// the direct kernel and a smaller CTA); the largest block of 1024, 512 or 256 threads whose
+// shared-memory layout fits.
+static void tiled_shape(const Prepared& P, Fp32Shape& sh) {
   int sb = 4;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
@@ -341,6 +382,141 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
     sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, threads).total;
     if (sh.smem <= 227 * 1024 || threads == 256) break;
   }
+}
+
+// Tile depths the autotuner times besides the formula depth.
+static const int kTileCandidates[] = {24, 32, 48, 64, 80, 96, 128};
+
+// ----------------------------------------------------------------------- bridge plans --------
+// The plan of one tile depth TT, word offsets relative to its start:
+//   [0] tiles; then per tile 6 words (node list, level offsets, level count, stack entries,
+//   stack entry count, step codes); the step codes of all T steps; per tile its nodes in level
+//   order, its level offsets and its stack entries.
+// Values are named by their row in the kernel's Z array: tile node j is row j, the value at the
+// tile start row NNmax = TT + stack_max, stack slot d (as the tile found it) row NNmax + 1 + d.
+// A node word packs (tile node j, left anchor row, right anchor row) in 9-bit fields, and bit 27
+// for the bridge's first node (no anchors: W = z·c; its anchor fields name row NNmax).  A step
+// code is the row of W at the step's end.  A stack entry packs (destination row NNmax + 1 + d,
+// tile node) for each entry pushed in the tile and still on the stack at its end.
+// The plan comes from running the streamed bridge (qmc.rs:158-191 in the order of
+// bridge_schedule_into) on node ids: a node pushed at step t has the value at t as its left anchor
+// and the stack's top as its right one; its level is one more than the deepest in-tile anchor.
+static void build_bridge_plan(const std::vector<int32_t>& node_off, int64_t T, int TT, int stack_max,
+                              std::vector<uint32_t>& w) {
+  const uint32_t NNmax = (uint32_t)(TT + stack_max);
+  if (NNmax + 1 + (uint32_t)stack_max > 511u) raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: tile too deep");
+  const size_t base = w.size();
+  const int64_t ntiles = (T + TT - 1) / TT;
+  w.push_back((uint32_t)ntiles);
+  const size_t hdr = w.size();
+  w.resize(hdr + (size_t)ntiles * 6);
+  const size_t steps_at = w.size();
+  w.resize(steps_at + (size_t)T);
+  std::vector<int32_t> stk;  // node ids on the stack
+  int32_t wc = -1;           // node id of the value at the current time (-1: W(0) = 0)
+  std::vector<int> level((size_t)node_off[T], 0);
+  std::vector<std::pair<int, uint32_t>> recs;
+  for (int64_t k = 0; k < ntiles; ++k) {
+    const int64_t t0 = k * TT, tn = std::min<int64_t>(TT, T - t0);
+    const int32_t n0 = node_off[t0], n1 = node_off[t0 + tn];
+    if ((uint32_t)(n1 - n0) > NNmax) raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: tile too deep");
+    const std::vector<int32_t> stk0 = stk;
+    const int32_t wc0 = wc;
+    auto code = [&](int32_t id) -> uint32_t {
+      if (id >= n0 && id < n1) return (uint32_t)(id - n0);
+      if (id == wc0) return NNmax;
+      for (size_t d = 0; d < stk0.size(); ++d)
+        if (stk0[d] == id) return NNmax + 1u + (uint32_t)d;
+      raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: an anchor is outside the tile's state");
+    };
+    recs.clear();
+    for (int64_t tt = 0; tt < tn; ++tt) {
+      for (int32_t nd = node_off[t0 + tt]; nd < node_off[t0 + tt + 1]; ++nd) {
+        uint32_t lc = NNmax, rc = NNmax, first = 1u;
+        int lev = 0;
+        if (nd != 0) {
+          first = 0u;
+          if (stk.empty()) raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: empty stack");
+          const int32_t top = stk.back();
+          lc = code(wc);
+          rc = code(top);
+          if (lc < NNmax) lev = std::max(lev, level[wc] + 1);
+          if (rc < NNmax) lev = std::max(lev, level[top] + 1);
+        }
+        level[nd] = lev;
+        recs.push_back({lev, (uint32_t)(nd - n0) | (lc << 9) | (rc << 18) | (first << 27)});
+        stk.push_back(nd);
+        if ((int)stk.size() > stack_max) raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: stack overflow");
+      }
+      if (stk.empty()) raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: empty stack");
+      wc = stk.back();
+      stk.pop_back();
+      w[steps_at + t0 + tt] = code(wc);
+    }
+    // nodes in level order (stable), and the level offsets
+    int nlev = 0;
+    for (const auto& r : recs) nlev = std::max(nlev, r.first + 1);
+    std::stable_sort(recs.begin(), recs.end(),
+                     [](const std::pair<int, uint32_t>& a, const std::pair<int, uint32_t>& b) { return a.first < b.first; });
+    const size_t node_at = w.size();
+    for (const auto& r : recs) w.push_back(r.second);
+    const size_t lev_at = w.size();
+    {
+      size_t i = 0;
+      for (int L = 0; L <= nlev; ++L) {
+        while (i < recs.size() && recs[i].first < L) ++i;
+        w.push_back((uint32_t)i);
+      }
+    }
+    // entries pushed in this tile and still on the stack; the rest kept their slots
+    const size_t stk_at = w.size();
+    for (size_t d = 0; d < stk.size(); ++d) {
+      if (stk[d] >= n0 && stk[d] < n1) {
+        w.push_back(((NNmax + 1u + (uint32_t)d) << 9) | (uint32_t)(stk[d] - n0));
+      } else if (d >= stk0.size() || stk0[d] != stk[d]) {
+        raise(RG_ERR_INVALID_SCHEDULE, "bridge plan: a carried stack entry moved");
+      }
+    }
+    uint32_t* h = w.data() + hdr + (size_t)k * 6;
+    h[0] = (uint32_t)(node_at - base);
+    h[1] = (uint32_t)(lev_at - base);
+    h[2] = (uint32_t)nlev;
+    h[3] = (uint32_t)(stk_at - base);
+    h[4] = (uint32_t)(w.size() - stk_at);
+    h[5] = (uint32_t)(steps_at - base);
+  }
+}
+
+void p32_bridge_plans(const Prepared& P, BridgePlans& out) {
+  out.words.clear();
+  out.n = 0;
+  Fp32Shape sh{};
+  tiled_shape(P, sh);
+  std::vector<int> tts{sh.TT};
+  for (int tt : kTileCandidates)
+    if (std::find(tts.begin(), tts.end(), tt) == tts.end()) tts.push_back(tt);
+  for (int tt : tts) {
+    if (out.n == RG_BPLAN_MAX) break;
+    out.tt[out.n] = tt;
+    out.at[out.n] = (int32_t)out.words.size();
+    build_bridge_plan(P.node_off, P.T, tt, P.stack_max, out.words);
+    ++out.n;
+  }
+}
+
+Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
+  Fp32Shape sh{};
+  if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
+  if (p32_direct(P, npaths)) {
+    // nothing for the scenarios to share: the per-thread kernel without shared-memory tiles
+    sh.direct = 1;
+    sh.Sb = P.n_scen;
+    sh.threads = 256;
+    sh.grid = phoenix32d_grid(P, npaths, sm_count);
+    sh.smem = P.stack_max * P.n * 256 * (int)sizeof(float);  // the bridge stacks (dynamic)
+    return sh;
+  }
+  tiled_shape(P, sh);
   // Function attributes are process-wide: raise every instantiation's dynamic shared-memory limit
   // to the device maximum once, so engines pricing concurrently never lower it under each other.
   {
@@ -424,7 +600,9 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   const uint64_t prefix = (uint64_t)sh.grid * (uint64_t)sh.Pb * 2;
   if (!may_tune || npaths < prefix * 4) return sh;
   std::vector<int> cand;
-  for (int tt : {sh.TT, 24, 32, 48, 64, 80, 96, 128}) {
+  std::vector<int> tts{sh.TT};
+  tts.insert(tts.end(), std::begin(kTileCandidates), std::end(kTileCandidates));
+  for (int tt : tts) {
     Fp32Shape c = sh;
     if (std::find(cand.begin(), cand.end(), tt) == cand.end() && p32_with_tt(P, c, tt)) cand.push_back(tt);
   }
@@ -467,12 +645,19 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
   }
   const float ln_ko = (float)P.ln_ko, ln_cb = (float)P.ln_cb, ln_ki = (float)P.ln_ki;
   const int NNmax = sh.TT + P.stack_max;
+  const uint32_t* plan = nullptr;
+  for (int i = 0; i < tb.n_bplan; ++i)
+    if (tb.bplan_tt[i] == sh.TT) plan = tb.bplan + tb.bplan_at[i];
+  if (!plan) raise(RG_ERR_GPU_ERROR, "phoenix32: no bridge plan staged for the tile depth");
+  // the bridge phase gives each warp at most 64 chains (two per lane)
+  if ((sh.Pb * P.n + sh.threads / 32 - 1) / (sh.threads / 32) > 64)
+    raise(RG_ERR_GPU_ERROR, "phoenix32: too many bridge chains per warp");
 #define RG_LAUNCH(NN, LVV)                                                                        \
   if (out.records) RG_LAUNCH_R(NN, LVV, true) else RG_LAUNCH_R(NN, LVV, false)
 #define RG_LAUNCH_R(NN, LVV, REC)                                                                 \
   phoenix32_kernel<NN, LVV, REC><<<sh.grid, sh.threads, sh.smem, st>>>(                           \
       P.trade, tb, scen, scen32, P.n_scen, sh.Pb, sh.TT, NNmax, P.stack_max, ln_ko, ln_cb, ln_ki, \
-      path0, npaths, out.partial, out.ko_steps, out.records);
+      path0, npaths, plan, out.partial, out.ko_steps, out.records);
   const bool lv = P.trade.has_lv != 0;
   switch (P.n) {
     case 1: if (lv) { RG_LAUNCH(1, true) } else { RG_LAUNCH(1, false) } break;

@@ -16,6 +16,7 @@
 #define RG_ACC 16          // FP64 accumulators per (block, scenario)
 #define RG_STACK_MAX 24    // Brownian-bridge anchor stack depth (T <= 2^22)
 #define RG_MAX_SCEN 64     // scenarios in one fused CRN launch
+#define RG_BPLAN_MAX 8     // tile depths with a bridge plan: the formula depth and the tuner's candidates
 
 // Accumulator slots (per scenario).  Second moments are of shifted values so that the FP64
 // sums keep their precision: pv and KO funding are shifted by 1.
@@ -84,6 +85,10 @@ struct DevTables {
   const float* df_f;
   const float* df_mat_f;
   int32_t lv_nt;
+  // level-ordered bridge plans of the FP32 tiled kernel (phoenix32.cu), one per tile depth
+  const uint32_t* bplan;
+  int32_t bplan_tt[RG_BPLAN_MAX], bplan_at[RG_BPLAN_MAX];
+  int32_t n_bplan;
 };
 
 // ------------------------------------------------------------------ integer QMC primitives ----

@@ -245,6 +245,15 @@ int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                        uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count);
+// The level-ordered evaluation plans of the streamed Brownian bridge for every tile depth the tiled
+// FP32 kernel may launch with (its formula depth and the autotuner's candidates): packed words,
+// and per depth its value and word offset.
+struct BridgePlans {
+  std::vector<uint32_t> words;
+  int32_t tt[RG_BPLAN_MAX], at[RG_BPLAN_MAX];
+  int n = 0;
+};
+void p32_bridge_plans(const Prepared& P, BridgePlans& out);
 // The tiled kernel's step tiling from the autotuner: a cached choice for the launch's shape, or —
 // when `may_tune` and the launch is large enough to amortise it — one tuning pass that times the
 // candidate tile depths on a prefix of the paths (their results are discarded; the tile depth
