@@ -42,6 +42,9 @@ struct P32Layout {
   uint32_t acc, lv, flags, per, noff, ncf, plan, z, dw, total;
 };
 
+// Floats per row of the Z array: N·(Pb + 4) and one more, so that rows start in different banks.
+__host__ __device__ inline int p32_zrow(int N, int Pb) { return N * (Pb + 4) + 1; }
+
 __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, int NNmax, int stack_max,
                                                 int threads) {
   P32Layout L;
@@ -52,11 +55,12 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
   };
   const uint32_t PbN = (uint32_t)(Pb * N);
   const int g = Pb < 32 ? Pb : 32;
-  // rows of N·(Pb + 4) floats, one float per (factor, path): the normals of the tile's bridge nodes
-  // (rows 0 .. NNmax-1, overwritten by their bridge values), then the bridge state carried between
-  // tiles: the value at the tile start (row NNmax) and the stack (rows NNmax + 1 + slot).  The
-  // padding spreads a generation pass's stores (lanes stride GEN_CH·nch apart) over distinct banks
-  const uint32_t zb = (uint32_t)(NNmax + 1 + stack_max) * (uint32_t)N * (uint32_t)(Pb + 4) * 4u;
+  // rows of p32_zrow(N, Pb) floats, N·(Pb + 4) of them one per (factor, path): the normals of the
+  // tile's bridge nodes (rows 0 .. NNmax-1, overwritten by their bridge values), then the bridge
+  // state carried between tiles: the value at the tile start (row NNmax) and the stack (rows
+  // NNmax + 1 + slot).  The padding spreads a generation pass's stores (lanes stride GEN_CH·nch
+  // apart) over distinct banks, and the odd row length the bridge phase's loads of several rows
+  const uint32_t zb = (uint32_t)(NNmax + 1 + stack_max) * (uint32_t)p32_zrow(N, Pb) * 4u;
   const uint32_t rb = (uint32_t)(threads / g) * RG_ACC * 8u;  // per-tile reduction, aliases Z
   put(L.acc, (uint32_t)S * RG_ACC * 8u);
   put(L.lv, (uint32_t)(S * N) * 16u);
@@ -67,7 +71,7 @@ __host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, in
   // the tile's bridge plan: node words, level offsets, step codes, stack entries
   put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + TT + stack_max) * 4u);
   put(L.z, zb > rb ? zb : rb);
-  put(L.dw, (uint32_t)TT * PbN * 4u);
+  put(L.dw, (uint32_t)TT * (PbN + 1) * 4u);  // dW[step][factor][path], odd step stride
   L.total = o;
   return L;
 }
@@ -83,6 +87,8 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
   const int PbN = Pb * N;
   const int nch = Pb / GEN_CH;
   const int lg_pb = __ffs(Pb) - 1;  // Pb is a power of two
+  const int zs = p32_zrow(N, Pb);    // floats per Z row
+  const int dws = PbN + 1;           // floats per dW step
   const int T = (int)tr.steps;
   // ---- shared-memory carve-up (the host sizes the launch from the same layout)
   const P32Layout L = p32_layout(S, N, Pb, TT, NNmax, stack_max, (int)blockDim.x);
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t tile0 = tile * Pb;
-    for (int i = tid; i < N * (Pb + 4); i += blockDim.x) Z[(size_t)NNmax * N * (Pb + 4) + i] = 0.0f;  // W(0)
+    for (int i = tid; i < zs; i += blockDim.x) Z[(size_t)NNmax * zs + i] = 0.0f;  // W(0)
     const uint64_t gi = tile0 + pl;
     const bool ok = lane_ok && gi < npaths;
     float x[N];
@@ -184,7 +190,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
         const int nd = n0 + j;
         const uint64_t g0 = tile0 + (uint64_t)c * GEN_CH;
         if (g0 >= npaths) continue;  // these paths are never read
-        float* zo = Z + (size_t)(j * N + f) * (Pb + 4) + c;
+        float* zo = Z + (size_t)j * zs + f * (Pb + 4) + c;
         if (tr.vr == RG_VR_SOBOL) {
           const uint32_t* row = tb.sobol + 32 * (size_t)__ldg(tb.nf_row + nd * N + f);
           uint64_t n = path0 + g0 + 1;
@@ -223,7 +229,6 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
       // tile (the value at the tile end, the stack entries pushed in the tile).  Every anchor is
       // a row of Z, so an evaluation is four loads and one FMA.
       {
-        const int zs = N * (Pb + 4);
         const int nwarp = (int)(blockDim.x >> 5);
         const int cpw = (PbN + nwarp - 1) / nwarp;  // at most 64 (host-checked)
         const int c_lo = (tid >> 5) * cpw;
@@ -259,8 +264,8 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
           for (int tt = q0; tt < tn; tt += G) {
             const int hi = (int)s_pstep[tt] * zs;
             const int lo = tt == 0 ? NNmax * zs : (int)s_pstep[tt - 1] * zs;
-            dW[tt * PbN + cA] = Z[hi + zA] - Z[lo + zA];
-            if (hasB) dW[tt * PbN + cB] = Z[hi + zB] - Z[lo + zB];
+            dW[tt * dws + cA] = Z[hi + zA] - Z[lo + zA];
+            if (hasB) dW[tt * dws + cB] = Z[hi + zB] - Z[lo + zB];
           }
         __syncwarp();
         if (lane_on && q0 == 0) {
@@ -282,7 +287,7 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
           const int tg = (t0 + tt) * gx;
           float d[N], y[N];
 #pragma unroll
-          for (int f = 0; f < N; ++f) d[f] = dW[(tt * N + f) * Pb + pl];
+          for (int f = 0; f < N; ++f) d[f] = dW[tt * dws + f * Pb + pl];
           int q = 0;
 #pragma unroll
           for (int a = 0; a < N; ++a) {
