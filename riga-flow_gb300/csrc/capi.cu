@@ -299,11 +299,11 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   size_t o_df = pk.add(P.df), o_dfm = pk.add(P.df_mat);
   size_t o_acf = pk.add(P.accr_f), o_dff = pk.add(P.df_f), o_dfmf = pk.add(P.df_mat_f);
   // the FP32 tiled kernel's bridge plans, one per tile depth it may launch with
-  BridgePlans bp;
+  std::shared_ptr<const BridgePlans> bp;
   size_t o_bplan = 0;
   if (req->config.precision == RG_PRECISION_FP32) {
-    p32_bridge_plans(P, bp);
-    o_bplan = pk.add(bp.words);
+    bp = p32_bridge_plans(P);
+    o_bplan = pk.add(bp->words);
   }
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
   // local-vol surfaces: inputs (grids) and outputs
@@ -406,10 +406,10 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   tb.df_f = reinterpret_cast<const float*>(base + o_dff);
   tb.df_mat_f = reinterpret_cast<const float*>(base + o_dfmf);
   tb.bplan = reinterpret_cast<const uint32_t*>(base + o_bplan);
-  tb.n_bplan = bp.n;
+  tb.n_bplan = bp ? bp->n : 0;
   for (int i = 0; i < RG_BPLAN_MAX; ++i) {
-    tb.bplan_tt[i] = i < bp.n ? bp.tt[i] : 0;
-    tb.bplan_at[i] = i < bp.n ? bp.at[i] : 0;
+    tb.bplan_tt[i] = i < tb.n_bplan ? bp->tt[i] : 0;
+    tb.bplan_at[i] = i < tb.n_bplan ? bp->at[i] : 0;
   }
   tb.lv_nt = P.lv_nt_max;
   S.scen = reinterpret_cast<DevScenario*>(base + o_scen);

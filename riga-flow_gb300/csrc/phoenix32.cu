@@ -492,21 +492,32 @@ static void build_bridge_plan(const std::vector<int32_t>& node_off, int64_t T, i
   }
 }
 
-void p32_bridge_plans(const Prepared& P, BridgePlans& out) {
-  out.words.clear();
-  out.n = 0;
+std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P) {
   Fp32Shape sh{};
   tiled_shape(P, sh);
+  static std::mutex mu;
+  static std::map<std::pair<int64_t, int>, std::shared_ptr<const BridgePlans>> cache;
+  const std::pair<int64_t, int> key{P.T, sh.TT};
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  auto out = std::make_shared<BridgePlans>();
   std::vector<int> tts{sh.TT};
   for (int tt : kTileCandidates)
     if (std::find(tts.begin(), tts.end(), tt) == tts.end()) tts.push_back(tt);
   for (int tt : tts) {
-    if (out.n == RG_BPLAN_MAX) break;
-    out.tt[out.n] = tt;
-    out.at[out.n] = (int32_t)out.words.size();
-    build_bridge_plan(P.node_off, P.T, tt, P.stack_max, out.words);
-    ++out.n;
+    if (out->n == RG_BPLAN_MAX) break;
+    out->tt[out->n] = tt;
+    out->at[out->n] = (int32_t)out->words.size();
+    build_bridge_plan(P.node_off, P.T, tt, P.stack_max, out->words);
+    ++out->n;
   }
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() >= 256) cache.clear();  // bounded: one entry per step count in use
+  cache[key] = out;
+  return out;
 }
 
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {

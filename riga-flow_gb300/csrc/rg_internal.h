@@ -10,6 +10,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "rg_common.cuh"
@@ -253,7 +254,9 @@ struct BridgePlans {
   int32_t tt[RG_BPLAN_MAX], at[RG_BPLAN_MAX];
   int n = 0;
 };
-void p32_bridge_plans(const Prepared& P, BridgePlans& out);
+// A plan depends only on the step count (the node schedule and stack depth) and the tile depths,
+// so the plans are built once per (steps, formula depth) and shared process-wide.
+std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P);
 // The tiled kernel's step tiling from the autotuner: a cached choice for the launch's shape, or —
 // when `may_tune` and the launch is large enough to amortise it — one tuning pass that times the
 // candidate tile depths on a prefix of the paths (their results are discarded; the tile depth

@@ -16,8 +16,8 @@ static int check(int64_t T) {
   P.n = 3;
   P.n_scen = 16;
   bridge_schedule_into(T, 1.0 / 252, P);
-  BridgePlans bp;
-  p32_bridge_plans(P, bp);
+  const std::shared_ptr<const BridgePlans> bpp = p32_bridge_plans(P);
+  const BridgePlans& bp = *bpp;
   std::mt19937 rng(1234 + (unsigned)T);
   std::normal_distribution<float> nd(0.f, 1.f);
   const int64_t NN = P.node_off[T];
