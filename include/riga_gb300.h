@@ -279,16 +279,20 @@ void rg_engine_destroy(rg_engine* engine);
 int32_t rg_price_put_leg(rg_engine* engine, const rg_price_request* request, rg_price_result* out);
 
 /* rg_price_put_leg without any device allocation (this entry point has no counterpart in the
- * reference).  For callers that may not allocate device memory — code running during CUDA-graph
- * capture, hosts whose memory pool owns the device, plugins that must not call cudaMalloc or
- * cudaFree.  It needs no engine: every device buffer comes from one static 16 MiB region of the
- * library (reserved on each GPU where the entry point is used, until the process exits), and
- * requests that need more — e.g. many paths with trace events on — fail with
- * RG_ERR_INVALID_ARGUMENT.  Runs on the current device and the legacy default stream and returns
- * when the result is ready.  The first call on a device resolves the region's address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.  Calls share the
- * region: they are serialised by a process-wide lock, because GPU work of two overlapping calls
- * would race on it.  Same results as rg_price_put_leg for the same request. */
+ * reference).  For callers that may not allocate device memory: hosts whose memory pool owns every
+ * byte of the device, processes under a hard device-memory budget, and plugins that must not call
+ * cudaMalloc or cudaFree behind their host's back (cudaFree synchronises the whole device; both
+ * take memory outside the host's accounting).  It needs no engine: every device buffer comes from
+ * one static 16 MiB region of the library, a module global that stays reserved on each GPU where
+ * the library's module is loaded until the process exits (with lazy module loading, the CUDA
+ * default, only GPUs where the library's kernels run; with CUDA_MODULE_LOADING=EAGER every context
+ * that loads the library).  Requests that need more — e.g. many paths with trace events on, or
+ * long local-vol grids — fail with RG_ERR_INVALID_ARGUMENT.  Runs on the current device and the
+ * legacy default stream and returns when the result is ready.  The first call on a device
+ * resolves the region's address (cudaGetSymbolAddress) with that device current, so make that
+ * first call before any stream capture.  Calls on one device share the region, which keeps the
+ * last call's contents: they are serialised by a per-device lock, because GPU work of two calls
+ * that overlapped would race on it.  Same results as rg_price_put_leg for the same request. */
 int32_t rg_price_put_leg_static(const rg_price_request* request, rg_price_result* out);
 
 /* A CRN scenario batch in one fused launch: out[i] is the request priced under scenarios[i] with

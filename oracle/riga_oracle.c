@@ -37,12 +37,16 @@ const char* or_last_error(void) { return g_err; }
 
 
 /* ============================================================ elementary functions =========== */
-/* Two modes.  Default: the platform libm, which is what the reference's Rust f64::exp/ln call —
- * the golden vector is reproduced bit for bit in this mode.  Portable: a deterministic exp/log
- * built only from IEEE-754 +, -, *, / and exact power-of-two scaling (Cody–Waite reduction by a
- * split ln 2 and the degree-13 Taylor polynomial; log by the artanh series through s^23), the
- * same published method and coefficients the engine's FP64 parity kernel uses, so the two agree
- * bit for bit.  Compiled with -ffp-contract=off. */
+/* Two modes for the per-path elementary functions (the Euler step's exp, the local-vol lookup's
+ * log of the spot, the probit tails' log).  Default: the platform libm, which is what the
+ * reference's Rust f64::exp/ln call — the golden vector is reproduced bit for bit in this mode.
+ * Portable: a deterministic exp/log built only from IEEE-754 +, -, *, / and exact power-of-two
+ * scaling (Cody–Waite reduction by a split ln 2 and the degree-13 Taylor polynomial; log by the
+ * artanh series through s^23), the same published method and coefficients the engine's FP64
+ * parity kernel uses on the device, so the two agree bit for bit.  The path-independent values —
+ * the Dupire calibration's logarithms and exponentials and the discount factors — are libm's in
+ * both modes, as the engine evaluates them on the host with the platform libm.  Compiled with
+ * -ffp-contract=off. */
 static int g_portable = 0;
 void or_set_portable_math(int on) { g_portable = on != 0; }
 
@@ -487,7 +491,9 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   int nt = grid->n_maturities, nk = grid->n_strikes;
   const double* K = grid->strikes;
   double s_min = K[0] * 0.55, s_max = K[nk - 1] * 1.05;
-  double log_lo = OLOG(s_min > 1e-6 ? s_min : 1e-6), log_hi = OLOG(s_max > 1e-6 ? s_max : 1e-6);
+  /* the calibration's logarithms and exponentials are libm's in both math modes: the engine
+     evaluates them on the host with the platform libm too */
+  double log_lo = log(s_min > 1e-6 ? s_min : 1e-6), log_hi = log(s_max > 1e-6 ? s_max : 1e-6);
   out->n_t = nt;
   out->gx = gx;
   out->t_axis = (double*)malloc(sizeof(double) * (size_t)nt);
@@ -497,7 +503,7 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   double* s_axis = (double*)malloc(sizeof(double) * (size_t)gx);
   for (int i = 0; i < gx; ++i) {
     out->log_s[i] = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
-    s_axis[i] = OEXP(out->log_s[i]);
+    s_axis[i] = exp(out->log_s[i]);
   }
   size_t cells = (size_t)nt * (size_t)gx;
   double *w = (double*)malloc(sizeof(double) * cells), *wx = (double*)malloc(sizeof(double) * cells),
@@ -505,13 +511,13 @@ int32_t or_lv_calibrate(const rg_implied_vol_grid* grid, double spot, double rat
   double *xj = (double*)malloc(sizeof(double) * (size_t)nk), *y2 = (double*)malloc(sizeof(double) * (size_t)nk);
   for (int k = 0; k < nt; ++k) {
     double tk = grid->maturities_years[k];
-    double forward = spot * OEXP(rate * tk);
-    for (int j = 0; j < nk; ++j) xj[j] = OLOG(K[j] / forward);
+    double forward = spot * exp(rate * tk);
+    for (int j = 0; j < nk; ++j) xj[j] = log(K[j] / forward);
     const double* y = grid->vols + (size_t)k * nk;
     natural_second_derivatives(xj, y, nk, y2);
     double x_lo = xj[0], x_hi = xj[nk - 1];
     for (int i = 0; i < gx; ++i) {
-      double xd = OLOG(s_axis[i] / forward);
+      double xd = log(s_axis[i] / forward);
       xd = xd < x_lo ? x_lo : (xd > x_hi ? x_hi : xd);
       double sg, s1, s2;
       if (nk >= 2) {
@@ -1020,7 +1026,7 @@ static void scan_path_cube(const model* m, const double* const* incr, path_out* 
       double due = (period == 0 && m->fixed_first) ? m->coupon_rate : accrual;
       double carry = due > 0.0 ? unpaid : 0.0;
       if (due + carry > 0.0) {
-        double df = OEXP(-m->rate * time);
+        double df = exp(-m->rate * time);
         coupon_pv += due * df;
         memory_pv += carry * df;
         received = 1;
@@ -1037,7 +1043,7 @@ static void scan_path_cube(const model* m, const double* const* incr, path_out* 
     if (step + 1 == T || next_period != period) {
       double due = (period == 0 && m->fixed_first) ? m->coupon_rate : accrual;
       if (due > 0.0) {
-        double df = OEXP(-m->rate * time);
+        double df = exp(-m->rate * time);
         coupon_pv += due * df;
         memory_pv += unpaid * df;
         received = 1;
@@ -1049,10 +1055,11 @@ static void scan_path_cube(const model* m, const double* const* incr, path_out* 
     }
   }
   /* path close, note.rs:221-258 */
-  double funding = OEXP(-m->rate * redemption_time);
+  /* discount factors are libm's in both math modes, as the engine's host tables */
+  double funding = exp(-m->rate * redemption_time);
   int hit_ki = final_worst <= m->ki;
   int put_eligible = hit_ki && !ko;
-  double put = put_eligible ? fmax(m->strike - final_worst, 0.0) * OEXP(-m->rate * m->maturity) : 0.0;
+  double put = put_eligible ? fmax(m->strike - final_worst, 0.0) * exp(-m->rate * m->maturity) : 0.0;
   double coupon_nominal = coupon_pv + memory_pv;
   o->worst_final = final_worst;
   o->redemption_time = redemption_time;

@@ -198,7 +198,7 @@ void plan_book_scenarios(const rg_book_request* r, const rg_market_snapshot* sc,
       d.q[a] = sc[s].dividend_yields[a];
     }
     // exp(-r (t+1) dt) on the universe grid (note.rs:189, 210)
-    for (int64_t t = 0; t < B.TU; ++t) B.df[(size_t)s * B.TU + t] = rg_exp64(-d.rate * ((double)(t + 1) * B.dt));
+    for (int64_t t = 0; t < B.TU; ++t) B.df[(size_t)s * B.TU + t] = std::exp(-d.rate * ((double)(t + 1) * B.dt));
   }
   B.dfm.resize((size_t)B.n_trades * B.S);
   B.pair32.resize((size_t)B.n_trades * B.S);
@@ -206,7 +206,7 @@ void plan_book_scenarios(const rg_book_request* r, const rg_market_snapshot* sc,
     for (int s = 0; s < B.S; ++s) {
       const BookTradeDev& t = B.trades[j];
       const BookScenDev& m = B.scen[s];
-      B.dfm[(size_t)j * B.S + s] = rg_exp64(-m.rate * t.maturity);  // note.rs:221, 238
+      B.dfm[(size_t)j * B.S + s] = std::exp(-m.rate * t.maturity);  // note.rs:221, 238 (libm)
       BookPair32& p = B.pair32[(size_t)j * B.S + s];
       memset(&p, 0, sizeof p);
       for (int f = 0; f < t.n; ++f) {

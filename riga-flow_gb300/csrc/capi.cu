@@ -309,7 +309,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   // local-vol surfaces: inputs (grids) and outputs
   const int gx = tr.gx;
   size_t o_lv = 0, o_lvf = 0, o_logs = 0, o_jobs = 0, o_celloff = 0, o_sasset = 0;
-  std::vector<size_t> o_mats, o_ks, o_vs;
+  std::vector<size_t> o_mats, o_ks, o_vs, o_ax;
   size_t cells = 0, scratch = 0;
   std::vector<CalibJob> jobs;
   if (tr.has_lv) {
@@ -338,6 +338,16 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
     }
     o_celloff = pk.add(cell_off);
     o_sasset = pk.add(sasset);
+    // the calibration's host-libm logarithms, once per (asset, spot, rate): vol bumps share them
+    o_ax.resize(P.n_surf);
+    for (int j = 0; j < P.n_surf; ++j) {
+      const SurfaceKey& key = P.surfaces[j];
+      int same = -1;
+      for (int i = 0; i < j && same < 0; ++i)
+        if (P.surfaces[i].asset == key.asset && P.surfaces[i].spot == key.spot && P.surfaces[i].rate == key.rate)
+          same = i;
+      o_ax[j] = same >= 0 ? o_ax[same] : pk.add(calib_axes(req->local_vol[key.asset], key.spot, key.rate, gx));
+    }
   }
   uint8_t* base = static_cast<uint8_t*>(W.device(WS_ARENA, pk.host.size()));
   if (tr.has_lv) {
@@ -361,6 +371,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
       J.out_vf = reinterpret_cast<float2*>(base + o_lvf) + cell_off;
       J.out_logs = reinterpret_cast<double*>(base + o_logs) + (size_t)j * gx;
       J.scratch = sc + sc_off;
+      J.ax = reinterpret_cast<const double*>(base + o_ax[j]);
       J.cache_src = nullptr;
       J.cache_dst = nullptr;
       if (SurfaceCache* cache = W.surfaces()) {

@@ -224,6 +224,32 @@ void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vec
 // The in-order traversal of the reference's depth-first bridge (qmc.rs:155-191): the node
 // consumed at each step, its preorder index (the QMC step whose normals it reads) and its
 // conditional standard deviation.  Node 0 is the terminal point.
+// The logarithms and exponentials of DupireLocalVol::calibrate (riga-market/src/lib.rs:217-245),
+// in its order of operations, with the platform libm (the functions f64::ln / f64::exp call):
+// [log-strike axis, gx][log(K_j / F_k), n_t * n_k][log(S_i / F_k) before clamping, n_t * gx] for
+// F_k = spot * exp(rate * T_k) and S_i = exp(axis_i).  The device calibration reads them
+// (CalibJob::ax); they do not depend on the implied vols or their bump.
+std::vector<double> calib_axes(const rg_implied_vol_grid& g, double spot, double rate, int gx) {
+  const int nt = g.n_maturities, nk = g.n_strikes;
+  std::vector<double> ax((size_t)gx + (size_t)nt * nk + (size_t)nt * gx);
+  double* logs = ax.data();
+  double* xj = logs + gx;
+  double* xd = xj + (size_t)nt * nk;
+  const double s_min = g.strikes[0] * 0.55, s_max = g.strikes[nk - 1] * 1.05;
+  const double log_lo = std::log(std::max(s_min, 1e-6)), log_hi = std::log(std::max(s_max, 1e-6));
+  std::vector<double> s_axis(gx);
+  for (int i = 0; i < gx; ++i) {
+    logs[i] = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
+    s_axis[i] = std::exp(logs[i]);
+  }
+  for (int k = 0; k < nt; ++k) {
+    const double forward = spot * std::exp(rate * g.maturities_years[k]);
+    for (int j = 0; j < nk; ++j) xj[(size_t)k * nk + j] = std::log(g.strikes[j] / forward);
+    for (int i = 0; i < gx; ++i) xd[(size_t)k * gx + i] = std::log(s_axis[i] / forward);
+  }
+  return ax;
+}
+
 void bridge_schedule_into(int64_t T, double dt, Prepared& P) {
   std::vector<int32_t> pre(size_t(T) + 1, -1);
   // preorder numbering of the bisection midpoints (index 0 is the terminal point)
@@ -401,8 +427,8 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
       }
       // Dupire log-strike axis [0.55 K_min, 1.05 K_max] (riga-market/src/lib.rs:217-224)
       double s_min = g.strikes[0] * 0.55, s_max = g.strikes[g.n_strikes - 1] * 1.05;
-      P.asset_log_lo[f] = rg_log64(std::max(s_min, 1e-6));
-      P.asset_log_hi[f] = rg_log64(std::max(s_max, 1e-6));
+      P.asset_log_lo[f] = std::log(std::max(s_min, 1e-6));
+      P.asset_log_hi[f] = std::log(std::max(s_max, 1e-6));
     }
   }
 
@@ -441,12 +467,13 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
         d32.a_u[f] = (float)((std::log(t.initial_spots[f]) - P.asset_log_lo[f]) / h);
       }
     }
-    // discount factors exp(-r * (step + 1) dt) and exp(-r * T) (note.rs:189, 210, 221, 238)
+    // discount factors exp(-r * (step + 1) dt) and exp(-r * T) (note.rs:189, 210, 221, 238), with
+    // the platform libm's exp, as the reference's f64::exp
     for (int64_t s = 0; s < T; ++s) {
       double time = (double)(s + 1) * tr.dt;
-      P.df[size_t(i) * T + s] = rg_exp64(-m.risk_free_rate * time);
+      P.df[size_t(i) * T + s] = std::exp(-m.risk_free_rate * time);
     }
-    P.df_mat[i] = rg_exp64(-m.risk_free_rate * t.maturity_years);
+    P.df_mat[i] = std::exp(-m.risk_free_rate * t.maturity_years);
   }
   P.df_f.assign(P.df.begin(), P.df.end());
   P.df_mat_f.assign(P.df_mat.begin(), P.df_mat.end());

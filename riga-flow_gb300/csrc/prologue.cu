@@ -7,8 +7,13 @@
 // * cholesky_kernel: one thread per scenario.  Jacobi minimum eigenvalue, diagonal-loading PSD
 //   clamp and Cholesky–Banachiewicz (crates/riga-market/src/correlation.rs:95-168), in place on
 //   the scenario's correlation block; cholesky_big_kernel: the same for a book's universe.
-// Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's; exp and log are
-// the deterministic rg_exp64/rg_log64, so the grid is bit-identical to a host calibration.
+// Compiled with -fmad=false so the FP64 arithmetic rounds like the reference's.  The calibration's
+// logarithms and exponentials (the log-strike axis, the forwards, the log-moneyness of every
+// strike and grid node: about n_t * (n_k + gx) values, independent of the paths) are evaluated on
+// the host with the platform libm — the functions the reference's f64::ln / f64::exp call — and
+// read here from CalibJob::ax, so a grid is bit-identical to the reference's calibration.  The
+// spline and Dupire arithmetic, which amplifies a last-ulp change of any of those inputs about a
+// million-fold, runs here in FP64.
 #include "rg_internal.h"
 
 namespace rg {
@@ -81,35 +86,30 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
   double* wx = w + nt * gx;
   double* wxx = wx + nt * gx;
   double* xa = wxx + nt * gx;
-  double* s_axis = xa + nt * gx;             // gx
-  double* xj = s_axis + gx;                   // nt * nk
+  double* xj = xa + nt * gx + gx;             // nt * nk (after gx spare doubles)
   double* y2 = xj + nt * nk;                  // nt * nk
   double* tmp = y2 + nt * nk;                 // 3 * nt * nk (h, cp, dp)
   double* yv = tmp + 3 * nt * nk;             // nt * nk shifted implied vols
-  const double s_min = J.strikes[0] * 0.55, s_max = J.strikes[nk - 1] * 1.05;
-  const double log_lo = rg_log64(s_min > 1e-6 ? s_min : 1e-6), log_hi = rg_log64(s_max > 1e-6 ? s_max : 1e-6);
-  for (int i = threadIdx.x; i < gx; i += blockDim.x) {
-    double ls = log_lo + (log_hi - log_lo) * (double)i / (double)(gx - 1);
-    J.out_logs[i] = ls;
-    s_axis[i] = rg_exp64(ls);
+  const double* ax_logs = J.ax;               // gx
+  const double* ax_xj = ax_logs + gx;         // nt * nk
+  const double* ax_xd = ax_xj + nt * nk;      // nt * gx
+  for (int i = threadIdx.x; i < gx; i += blockDim.x) J.out_logs[i] = ax_logs[i];
+  for (int i = threadIdx.x; i < nt * nk; i += blockDim.x) {
+    yv[i] = J.vols[i] + J.shift;
+    xj[i] = ax_xj[i];
   }
-  for (int i = threadIdx.x; i < nt * nk; i += blockDim.x) yv[i] = J.vols[i] + J.shift;
   __syncthreads();
-  // one thread per tenor: log-moneyness nodes and the spline solve
-  for (int k = threadIdx.x; k < nt; k += blockDim.x) {
-    double forward = J.spot * rg_exp64(J.rate * J.mats[k]);
-    for (int j = 0; j < nk; ++j) xj[k * nk + j] = rg_log64(J.strikes[j] / forward);
+  // one thread per tenor: the spline solve on the log-moneyness nodes
+  for (int k = threadIdx.x; k < nt; k += blockDim.x)
     spline_y2(xj + k * nk, yv + k * nk, nk, y2 + k * nk, tmp + 3 * k * nk, tmp + 3 * k * nk + nk,
               tmp + 3 * k * nk + 2 * nk);
-  }
   __syncthreads();
   for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
     int k = c / gx, i = c % gx;
     double tk = J.mats[k];
-    double forward = J.spot * rg_exp64(J.rate * tk);
     const double* xk = xj + k * nk;
     double x_lo = xk[0], x_hi = xk[nk - 1];
-    double xd = rg_log64(s_axis[i] / forward);
+    double xd = ax_xd[c];
     xd = xd < x_lo ? x_lo : (xd > x_hi ? x_hi : xd);
     double sg, s1, s2;
     if (nk >= 2) {

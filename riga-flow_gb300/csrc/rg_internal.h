@@ -158,6 +158,7 @@ void prepare(const rg_price_request* req, const rg_scenario* scen, int n_scen, P
 void bridge_schedule_into(int64_t T, double dt, Prepared& P);
 // The Sobol direction table for `dim` dimensions (process-wide cache).
 const std::vector<uint32_t>& sobol_table(int64_t dim);
+std::vector<double> calib_axes(const rg_implied_vol_grid& g, double spot, double rate, int gx);
 // Halton bases and permutations.
 void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vector<uint32_t>& off,
                    std::vector<uint32_t>& perm);
@@ -176,6 +177,9 @@ struct CalibJob {
   float2* out_vf;
   double* out_logs;
   double* scratch;  // 4 * n_t * gx + gx + 6 * n_t * n_k doubles
+  // the calibration's logarithms, evaluated on the host with the platform libm (calib_axes):
+  // [log-strike axis, gx][log(K_j / F_k), n_t * n_k][log(S_i / F_k) before clamping, n_t * gx]
+  const double* ax;
   // resident-surface cache entry ([v][logs][vf], surface_entry_bytes): copy the surface from it
   // instead of calibrating (cache_src), or calibrate and also store it there (cache_dst)
   const double* cache_src;

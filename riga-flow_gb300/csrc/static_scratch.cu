@@ -1,19 +1,26 @@
 // static_scratch.cu — pricing without any device allocation.
 //
-// Some callers cannot allocate device memory: code running while a CUDA graph is being captured,
-// hosts whose allocator owns every device byte (a serving framework's memory pool, a process
-// started under a hard memory budget), or plugins that must not call cudaMalloc/cudaFree behind
-// their host's back.  rg_price_put_leg_static serves them: it runs the same pipeline and kernels as
-// rg_price_put_leg, but every device buffer it needs (request tables, calibration scratch,
-// per-block partial sums, the reduced sums, optional per-path KO steps) is carved out of one
-// file-scope __device__ array of RG_STATIC_SCRATCH_BYTES, and it creates no engine, stream or
-// event.  Requests whose buffers do not fit are rejected with "invalid_argument".
+// Some callers cannot allocate device memory: hosts whose allocator owns every device byte (a
+// serving framework's memory pool, a process started under a hard device-memory budget), or
+// plugins that must not call cudaMalloc/cudaFree behind their host's back (cudaFree synchronises
+// the whole device, and both take memory outside the host's accounting).  rg_price_put_leg_static serves
+// them: it runs the same pipeline and kernels as rg_price_put_leg, but every device buffer it needs
+// (request tables, calibration scratch, per-block partial sums, the reduced sums, optional
+// per-path KO steps) is carved out of one file-scope __device__ array of RG_STATIC_SCRATCH_BYTES,
+// and it creates no engine, stream or event.  Requests whose buffers do not fit are rejected with
+// "invalid_argument".
+//
+// The array is a module global: with lazy module loading (the CUDA default) it is reserved on a
+// GPU the first time the library's kernels are used there; with CUDA_MODULE_LOADING=EAGER every
+// context that loads the library reserves it, whether or not this entry point is called.  Either
+// way it stays reserved until the process exits.
 //
 // The array is process state shared by every call on a device and keeps the last call's contents;
 // every region the pipeline reads is written by the same call first, so nothing needs clearing.
-// Calls are serialised by a process-wide lock and each returns only after its work on the legacy
-// default stream has finished; work of two calls that overlapped on the GPU would race on the
-// array, which is why the lock exists.
+// Calls on one device are serialised by that device's lock and each returns only after its work
+// on the legacy default stream has finished; work of two calls that overlapped on the GPU would
+// race on the array, which is why the lock exists.  The first call on a device resolves the
+// array's device address with cudaGetSymbolAddress while that device is current.
 #include <mutex>
 #include <new>
 
@@ -26,8 +33,9 @@ static __device__ __align__(256) unsigned char g_static_scratch[RG_STATIC_SCRATC
 
 namespace {
 
-std::mutex g_static_mu;
+std::mutex g_static_mu[RG_STATIC_MAX_DEVICES];
 void* g_static_ptr[RG_STATIC_MAX_DEVICES];
+int g_static_sms[RG_STATIC_MAX_DEVICES];
 
 // Bump allocation in the static array; restarts at every fused launch.
 struct StaticWorkspace : rg::Workspace {
@@ -63,18 +71,23 @@ extern "C" int32_t rg_price_put_leg_static(const rg_price_request* request, rg_p
     int dev = 0;
     rg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= RG_STATIC_MAX_DEVICES) rg::raise(RG_ERR_INVALID_ARGUMENT, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_static_mu);
+    std::lock_guard<std::mutex> lock(g_static_mu[dev]);
     if (!g_static_ptr[dev]) {
-      // one-time set-up on this device (the current one): the array's device address
+      // one-time set-up on this device (the current one): the array's device address and the
+      // device's own SM count, which sizes the FP32 grid and the partial-sum region
       void* p = nullptr;
+      int sms = 0;
+      rg::cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                     "cudaDeviceGetAttribute");
       rg::cuda_check(cudaGetSymbolAddress(&p, g_static_scratch), "cudaGetSymbolAddress");
+      g_static_sms[dev] = sms;
       g_static_ptr[dev] = p;
     }
     StaticWorkspace W;
     W.base = static_cast<uint8_t*>(g_static_ptr[dev]);
     W.cap = RG_STATIC_SCRATCH_BYTES;
     W.stream = 0;  // legacy default stream; the call is synchronous
-    W.sm_count = rg::device_sm_count();
+    W.sm_count = g_static_sms[dev];
     rg::price_with(W, request, nullptr, 0, out);
     return RG_OK;
   } catch (const rg::Error& e) {

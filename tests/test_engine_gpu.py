@@ -466,86 +466,3 @@ def test_gpu_worst_of_is_bit_identical_to_scalar():
     w = gpu.resident_worst_of(a, b)
     w.reduce()
     assert np.array_equal(w.download(), out)
-
-
-def _lv_inputs(termsheet1, paths=2048):
-    req = termsheet1.request
-    steps = req.trade.steps
-    dt = np.float32(req.trade.maturity_years / steps)
-    gx = 96
-    rows = np.zeros(2 * steps * gx, np.float32)
-    axes = []
-    for f in range(2):
-        t_axis, log_s, v, surf = O.lv_calibrate(req.local_vol[f], req.market.spots[f], req.market.risk_free_rate)
-        for s in range(steps):
-            t = s * float(dt)
-            tc = min(max(t, t_axis[0]), t_axis[-1])
-            i = 0
-            while i + 1 < len(t_axis) - 1 and tc > t_axis[i + 1]:
-                i += 1
-            w = (tc - t_axis[i]) / (t_axis[i + 1] - t_axis[i])
-            rows[(f * steps + s) * gx:(f * steps + s + 1) * gx] = [(1 - w) * v[i][j] + w * v[i + 1][j] for j in range(gx)]
-        axes += log_s
-    seed = 0x9E3779B9
-    normals = np.empty(paths * steps * 2, np.float32)
-    for i in range(normals.size):
-        seed = (seed * 1664525 + 1013904223) & 0xFFFFFFFF
-        normals[i] = (np.float32(seed >> 8) / np.float32(1 << 24) - np.float32(0.5)) * np.float32(2.0)
-    return normals, rows, np.asarray(axes, np.float32), steps, float(dt)
-
-
-def _lv_reference(normals, rows, axes, s0, refs, bar, paths, steps, dt, rate, divs):
-    """numpy float32 restatement of lv_propagate (gpu.rs:37-75)."""
-    gx = axes.size // 2
-    f32 = np.float32
-    ls = np.array([np.log(f32(s0[0])), np.log(f32(s0[1]))], f32)
-    ls = np.tile(ls, (paths, 1))
-    nz = normals.reshape(paths, steps, 2)
-    ko = np.full(paths, -1, np.int32)
-    sq = np.sqrt(f32(dt))
-    for s in range(steps):
-        sig = []
-        for f in range(2):
-            lo, hi = axes[f * gx], axes[f * gx + gx - 1]
-            x = np.clip((ls[:, f] - lo) * (f32(1) / (hi - lo)) * f32(gx - 1), 0, gx - 1)
-            j = np.minimum(x.astype(np.int32), gx - 2)
-            w = x - j.astype(f32)
-            row = rows[(f * steps + s) * gx:(f * steps + s + 1) * gx]
-            sig.append(row[j] * (f32(1) - w) + row[j + 1] * w)
-        for f in range(2):
-            ls[:, f] += (f32(rate) - f32(divs[f]) - f32(0.5) * sig[f] * sig[f]) * f32(dt) + sig[f] * sq * nz[:, s, f]
-        hit = (ko < 0) & (np.exp(ls[:, 0]) / f32(refs[0]) >= f32(bar)) & (np.exp(ls[:, 1]) / f32(refs[1]) >= f32(bar))
-        ko[hit] = s
-    return np.exp(ls).reshape(-1), ko
-
-
-def test_lv_terminal_spots_matches_the_float32_restatement(termsheet1):
-    normals, rows, axes, steps, dt = _lv_inputs(termsheet1, 1024)
-    req = termsheet1.request
-    s0 = np.asarray(req.market.spots, np.float32)
-    refs = np.asarray(req.trade.initial_spots, np.float32)
-    divs = np.asarray(req.market.dividend_yields, np.float32)
-    out, ko = gpu.lv_terminal_spots(normals, rows, axes, s0, refs, 1.1, 1024, steps, dt,
-                                    req.market.risk_free_rate, divs)
-    ref_out, ref_ko = _lv_reference(normals, rows, axes, s0, refs, 1.1, 1024, steps, dt,
-                                    req.market.risk_free_rate, divs)
-    assert np.max(np.abs(out - ref_out) / ref_out) < 1e-4
-    assert np.mean(ko == ref_ko) > 0.995
-
-
-def test_resident_lv_multi_scenario_matches_per_call(termsheet1):
-    """gpu.rs:625-697: each resident run is bit-identical to a fresh per-call run."""
-    normals, rows, axes, steps, dt = _lv_inputs(termsheet1, 2048)
-    req = termsheet1.request
-    base = np.asarray(req.market.spots, np.float32)
-    refs = np.asarray(req.trade.initial_spots, np.float32)
-    divs = np.asarray(req.market.dividend_yields, np.float32)
-    rate = np.float32(req.market.risk_free_rate)
-    res = gpu.resident_lv(normals, rows, axes, 2048, steps, dt)
-    for bump in (np.float32(1.0), np.float32(1.005), np.float32(0.99)):
-        s0 = base * bump
-        res.run(s0, refs, 1.1, rate, divs)
-        rt, rk = res.download()
-        t, k = gpu.lv_terminal_spots(normals, rows, axes, s0, refs, 1.1, 2048, steps, dt, rate, divs)
-        assert np.array_equal(rt.view(np.uint32), t.view(np.uint32))
-        assert np.array_equal(rk, k)

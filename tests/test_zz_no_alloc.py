@@ -1,8 +1,8 @@
 """rg_price_put_leg_static: pricing for callers that cannot allocate device memory.
 
-Such callers (code running during CUDA-graph capture, hosts whose memory pool owns the device,
-plugins that must not call cudaMalloc/cudaFree) get the same pipeline with every device buffer in
-the library's static 16 MiB region.  Its results must equal rg_price_put_leg's for the same
+Such callers (hosts whose memory pool owns the device, processes under a hard device-memory
+budget, plugins that must not call cudaMalloc/cudaFree behind their host's back) get the same
+pipeline with every device buffer in the library's static 16 MiB region.  Its results must equal rg_price_put_leg's for the same
 request, within the parity tolerance of the other GPU tests (1e-12), on two calls in a row — the
 region keeps the previous call's contents, so the second call checks that nothing stale leaks.
 This file is collected last so a failure here cannot stop the rest of the GPU suite.
@@ -58,6 +58,29 @@ def test_static_entry_point_rejects_requests_beyond_its_region():
     status = lib.rg_price_put_leg_static(a.ptr, C.byref(out))
     assert abi.STATUS_CODES[status] == "invalid_argument"
     assert "16 MiB" in abi.last_error(lib)
+
+
+def test_static_entry_point_recovers_after_overflowing_while_staging():
+    """A long local-vol request fits its tables but not its FP32 local-vol rows (3 surfaces x 12,000
+    steps x 40 points x 8 bytes = 11.5 MB beside about 7 MB of tables), so the region overflows
+    inside staging, after the calibration kernel is already queued.  The error must be
+    invalid_argument, and the next call must still equal rg_price_put_leg."""
+    build_library()
+    lib = abi.load_library()
+    big = workloads.lv3(2048, steps=12000, fp32=True)
+    a = big.to_abi()
+    out = abi.PriceResult()
+    status = lib.rg_price_put_leg_static(a.ptr, C.byref(out))
+    assert abi.STATUS_CODES[status] == "invalid_argument"
+    assert "16 MiB" in abi.last_error(lib)
+    req = workloads.lv3(1 << 15, steps=252, fp32=True)
+    eng = Engine(0)
+    try:
+        expected = result_to_json(eng.price_raw(req), req)
+    finally:
+        eng.close()
+    got = result_to_json(_static(lib, req), req)
+    assert json_close(got, expected, tol=1e-12) == []
 
 
 def test_static_entry_point_declines_the_pseudo_random_lane(termsheet1):
