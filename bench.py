@@ -438,7 +438,8 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(tm.d2h_bytes)},
         "gpu_launches": int(tm.kernel_launches) * args.steps,
         "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes,
-                   "tile_steps": tm.tile_steps, "tile_steps_from": "autotuner (rg_set_autotune), tuned during warm-up"},
+                   "tile_steps": tm.tile_steps, "paths_per_thread": tm.paths_per_thread,
+                   "tuned_by": "autotuner (rg_set_autotune): paths per thread and tile depth, timed during warm-up"},
         "clocks": clocks,
     }
     if merged_pv is not None:

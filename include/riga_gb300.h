@@ -331,16 +331,30 @@ typedef struct rg_timing {
   int32_t kernel_launches; /* kernels this call launched (prologue + fused + reduce) */
   int32_t grid, block, smem_bytes; /* launch shape of the fused kernel */
   int32_t tile_steps; /* steps per time tile of the tiled FP32 kernel (0 for the other kernels) */
+  int32_t paths_per_thread; /* paths each thread of the tiled FP32 kernel steps (1 or 2) */
 } rg_timing;
 int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
 
-/* The FP32 kernel's step-tiling autotuner (on by default, process-wide).  The first pricing call
- * of a launch shape (asset count, local vol, scenario slots, steps, QMC lane, grid width) with at
- * least eight waves of path tiles times the candidate tile depths on a prefix of its paths and
- * keeps the fastest for that shape; later calls reuse it.  The tile depth changes the schedule,
- * not the arithmetic, so prices are the same with the autotuner on or off.  Calls through
- * rg_price_put_leg_static never tune.  Disabling also clears the tuned depths. */
+/* The tiled FP32 kernel's autotuner (on by default, process-wide).  The first pricing call of a
+ * launch shape (asset count, local vol, scenario slots, steps, QMC lane, grid width) with at least
+ * eight waves of path tiles times every candidate schedule — one or two paths per thread (two:
+ * packed FP32x2 stepping on 512 threads) and the time-tile depths — on a prefix of its paths and
+ * keeps the fastest for that shape; later calls reuse it.  Neither knob changes a path's arithmetic
+ * or the 32-path chunks of the sums, so prices are the same with the autotuner on or off.  Calls
+ * through rg_price_put_leg_static never tune.  Disabling also clears the tuned shapes.  No
+ * counterpart in the reference. */
 int32_t rg_set_autotune(int32_t enabled);
+/* Forces every tiled FP32 launch of the process onto one schedule: paths per thread 1 or 2 and a
+ * tile depth among the autotuner's candidates (24, 32, 48, 64, 80, 96, 128); (0, 0) returns to the
+ * formula shape or the autotuner.  A forced tile that does not fit in shared memory fails the
+ * pricing call with RG_ERR_INVALID_ARGUMENT.  For callers that need a fixed schedule, and for
+ * checking that schedules do not change prices.  No counterpart in the reference. */
+int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps);
+/* Clock cycles the tiled FP32 kernel's CTAs spent in generation, bridge, stepping and path close
+ * (out[0..3], summed over CTAs since the last reset), for profiling.  Only a library built with
+ * RG_PHASE_CLOCKS=1 records them; others return RG_ERR_UNSUPPORTED.  No counterpart in the
+ * reference. */
+int32_t rg_phase_clocks(uint64_t out[4], int32_t reset);
 
 /* explain::run_paths restricted to [first_path, first_path + count),
  * crates/riga-engine/src/explain.rs:90-316 (reconstruct_path :319-333 is count == 1). */

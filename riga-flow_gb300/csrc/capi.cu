@@ -560,16 +560,19 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     Staged S = stage(W, req, P);
     LaunchOut lo{};
     lo.mcz = mcz;
-    int grid;
+    // rows of partial sums: one per block of the FP64 kernel, one per 32-path chunk of the FP32 kernels
+    uint64_t rows;
     Fp32Shape sh{};
     if (fp32) {
       sh = phoenix32_shape(P, paths, W.sm_count);
-      grid = sh.grid;
+      rows = p32_chunks(paths);
     } else {
-      grid = phoenix64_grid(P, paths);
+      rows = (uint64_t)phoenix64_grid(P, paths);
     }
+    if (rows > (uint64_t)INT32_MAX) raise(RG_ERR_INVALID_PATHS, "too many paths for one launch");
+    const int grid = (int)rows;
     const size_t sums_bytes = (size_t)P.n_scen * RG_ACC * sizeof(double);
-    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)grid * P.n_scen * RG_ACC * sizeof(double)));
+    lo.partial = static_cast<double*>(W.device(WS_PARTIAL, rows * P.n_scen * RG_ACC * sizeof(double)));
     double* dsums = static_cast<double*>(W.device(WS_SUMS, sums_bytes));
     lo.grid = grid;
     if (trace) {
@@ -587,7 +590,8 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
       W.timing->block = fp32 ? sh.threads : 128;
       W.timing->smem_bytes = fp32 ? sh.smem : 0;
       W.timing->tile_steps = fp32 && !sh.direct ? sh.TT : 0;
-      W.timing->grid = grid;
+      W.timing->paths_per_thread = fp32 && !sh.direct ? sh.ppt : 1;
+      W.timing->grid = fp32 ? sh.grid : grid;
       W.timing->kernel_launches += 2;
       W.timing->d2h_bytes += sums_bytes;
     }
@@ -907,7 +911,8 @@ static void run_path_range(rg_engine* e, const rg_price_request* req, uint64_t f
     LaunchOut lo{};
     lo.mcz = mcz;
     Fp32Shape sh{};
-    lo.grid = fp32 ? (sh = phoenix32_shape(P, m, device_info().sm_count)).grid : phoenix64_grid(P, m);
+    if (fp32) sh = phoenix32_shape(P, m, device_info().sm_count);
+    lo.grid = fp32 ? (int)p32_chunks(m) : phoenix64_grid(P, m);
     lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));
     if (out) lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, m * sizeof(rg_path_record)));
     if (cube) lo.cube = static_cast<float*>(W.device(WS_CUBE, m * cube_row * sizeof(float)));
@@ -950,6 +955,20 @@ extern "C" int32_t rg_materialize_paths(rg_engine* e, const rg_price_request* re
 
 extern "C" int32_t rg_set_autotune(int32_t enabled) {
   RG_TRY({ p32_set_autotune(enabled != 0); })
+}
+
+extern "C" int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps) {
+  RG_TRY({ p32_force_shape(paths_per_thread, tile_steps); })
+}
+
+extern "C" int32_t rg_phase_clocks(uint64_t out[4], int32_t reset) {
+  RG_TRY({
+    if (!out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    unsigned long long v[4];
+    if (!p32_phase_clocks(v, reset != 0))
+      raise(RG_ERR_UNSUPPORTED, "this build has no phase clocks (build with RG_PHASE_CLOCKS=1)");
+    for (int k = 0; k < 4; ++k) out[k] = v[k];
+  })
 }
 
 extern "C" int32_t rg_sobol_directions(int64_t dim, uint32_t* out) {

@@ -2,28 +2,29 @@
 // scenarios of one trade.
 //
 // A CTA owns Pb consecutive paths × Sb scenario slots (Sb = S rounded up to a power of two, at least
-// 4; a single scenario runs on the direct kernel of phoenix32d.cu); thread
-// t serves scenario t / Pb and path t % Pb, so a warp is 32 paths of one scenario and its
-// local-vol lookups all read one surface.  Time is walked in tiles of TT steps, each in three
-// phases separated by CTA barriers:
-//   G. generation — every thread takes (bridge node, factor, 8-path run) tasks: the Sobol integer
-//      of the run's first point from its Gray code, the next seven by the Gray recurrence
-//      x(n) = x(n-1) ^ v[ctz(n)] (one load each), the digital shift (or Owen scramble) and the
-//      FP32 inverse normal; the standard normals of every node the tile consumes land in shared
-//      memory.  The step schedule of the tile is staged next to them.
-//   B. bridge — the tile's bridge nodes of every (path, factor) chain, evaluated level by level
-//      from a host plan of the streamed Brownian bridge's dependencies (each warp owns a slice of
-//      the chains, its lanes take one level's nodes at once), then the uncorrelated increments
-//      dW[step][factor][path] and the state carried to the next tile.
-//   S. scenario stepping — every (path, scenario) thread correlates dW with its own Cholesky
+// 4; Pb = 1024 / Sb; a single scenario runs on the direct kernel of phoenix32d.cu).  In the
+// stepping phase a thread serves one scenario and PPT paths: PPT = 2 (512 threads) steps a pair of
+// paths in packed FP32x2 arithmetic (fma/add .f32x2, one instruction for both paths), PPT = 1
+// (1024 threads) one path; a warp is 32·PPT paths of one scenario, so its local-vol lookups all
+// read one surface.  Time is walked in tiles of TT steps, each in three phases separated by CTA
+// barriers:
+//   G. generation — warp-wide items (bridge node, 32-path group): the Sobol integers of the group's
+//      32 consecutive points by a warp cooperation (rg_warp_sobol: shuffle reduction of the first
+//      point's Gray code, XOR scan of the Gray recurrence), the digital shift (or Owen scramble) and
+//      the FP32 inverse normal, for every factor; the standard normals of every node the tile
+//      consumes land in shared memory, 32 consecutive floats per store.  The tile's step schedule
+//      is staged beside them.
+//   B. bridge — the tile's bridge nodes level by level from a host plan of the streamed Brownian
+//      bridge's dependencies, each level's (node, factor, 32-path group) items spread over all
+//      warps; then the uncorrelated increments dW[step][factor][path] and the state carried to
+//      the next tile.
+//   S. scenario stepping — every (path, scenario) correlates dW with its scenario's Cholesky
 //      factor (the bridge is linear, so L·bridge(z) = bridge(L·z)), steps ln(S/S0) under flat vol
 //      or its scenario's Dupire surface and runs the Phoenix state machine.
 // Generation is paid once per path, not once per scenario.  Path state and a path's payoff values
-// are FP32; the 32 paths of a warp are summed in FP32 by a fixed shuffle butterfly, and every
-// sum above that (warps in index order, tiles, blocks in the final reduce kernel) is FP64, so a
-// launch of a given shape is bit-reproducible.  With 16 scenarios a CTA is 1024 threads (64 paths
-// × 16 scenarios, one CTA per SM): each scenario has two warps on the same paths, which share
-// its local-vol rows in L1.
+// are FP32; each 32-path chunk is summed in FP32 by a fixed shuffle butterfly and written as FP64
+// to partial[chunk][scenario], and the chunks are reduced in chunk order, so the sums — and the
+// prices — are the same for every launch shape (paths per thread, tile depth, block).
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -34,146 +35,228 @@
 
 namespace rg {
 
-#define GEN_CH 8  // consecutive paths per generation task (one Gray-code run)
-
 // Byte offsets of the kernel's dynamic shared-memory regions, 16-byte aligned, and their total.
 // Computed by the same function on the host (to size the launch) and in the kernel (to carve).
 struct P32Layout {
-  uint32_t acc, lv, flags, per, noff, ncf, plan, z, dw, total;
+  uint32_t flags, per, thr, noff, ncf, qmc, plan, z, dw, total;
 };
 
 // Floats per row of the Z array: N·(Pb + 4) and one more, so that rows start in different banks.
 __host__ __device__ inline int p32_zrow(int N, int Pb) { return N * (Pb + 4) + 1; }
+// Floats per step of the dW array: odd for one path per thread, even for two, whose (path,
+// path + 1) pairs are read as one aligned 8-byte load.
+__host__ __device__ inline int p32_dwstep(int N, int Pb, int ppt) { return Pb * N + (ppt == 2 ? 2 : 1); }
 
-__host__ __device__ inline P32Layout p32_layout(int S, int N, int Pb, int TT, int NNmax, int stack_max,
-                                                int threads) {
+__host__ __device__ inline P32Layout p32_layout(int N, int Pb, int TT, int NNmax, int stack_max, int ppt) {
   P32Layout L;
   uint32_t o = 0;
   auto put = [&o](uint32_t& field, uint32_t bytes) {
     field = o;
     o += (bytes + 15u) & ~15u;
   };
-  const uint32_t PbN = (uint32_t)(Pb * N);
-  const int g = Pb < 32 ? Pb : 32;
-  // rows of p32_zrow(N, Pb) floats, N·(Pb + 4) of them one per (factor, path): the normals of the
-  // tile's bridge nodes (rows 0 .. NNmax-1, overwritten by their bridge values), then the bridge
-  // state carried between tiles: the value at the tile start (row NNmax) and the stack (rows
-  // NNmax + 1 + slot).  The padding spreads a generation pass's stores (lanes stride GEN_CH·nch
-  // apart) over distinct banks, and the odd row length the bridge phase's loads of several rows
+  // rows of p32_zrow(N, Pb) floats, factor f's paths at columns f·(Pb + 4) + path: the normals of
+  // the tile's bridge nodes (rows 0 .. NNmax-1, overwritten by their bridge values), then the
+  // bridge state carried between tiles: the value at the tile start (row NNmax) and the stack
+  // (rows NNmax + 1 + slot)
   const uint32_t zb = (uint32_t)(NNmax + 1 + stack_max) * (uint32_t)p32_zrow(N, Pb) * 4u;
-  const uint32_t rb = (uint32_t)(threads / g) * RG_ACC * 8u;  // per-tile reduction, aliases Z
-  put(L.acc, (uint32_t)S * RG_ACC * 8u);
-  put(L.lv, (uint32_t)(S * N) * 16u);
   put(L.flags, (uint32_t)TT * 4u);
   put(L.per, (uint32_t)TT * 4u);
+  put(L.thr, (uint32_t)TT * 8u);  // per step (coupon threshold, knock-out threshold) or +inf
   put(L.noff, (uint32_t)(TT + 1) * 4u);
   put(L.ncf, (uint32_t)NNmax * 4u);
+  // per (tile node, factor): Sobol row and digital-shift mask; per tile node: preorder index
+  put(L.qmc, (uint32_t)NNmax * (uint32_t)(2 * N + 1) * 4u);
   // the tile's bridge plan: node words, level offsets, step codes, stack entries
   put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + TT + stack_max) * 4u);
-  put(L.z, zb > rb ? zb : rb);
-  put(L.dw, (uint32_t)TT * (PbN + 1) * 4u);  // dW[step][factor][path], odd step stride
+  put(L.z, zb);
+  put(L.dw, (uint32_t)TT * (uint32_t)p32_dwstep(N, Pb, ppt) * 4u);  // dW[step][factor][path]
   L.total = o;
   return L;
 }
 
-template <int N, bool LV, bool REC>
-__global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
+// PPT path values of one thread: a float (one path per thread) or a float pair (two), so that the
+// stepping arithmetic of two paths issues as one packed FP32x2 instruction (__ffma2_rn etc.).
+template <int PPT> struct PVec;
+template <> struct PVec<1> {
+  float v[1];
+  __device__ __forceinline__ static PVec splat(float a) { return {{a}}; }
+  __device__ __forceinline__ static PVec fma(PVec a, PVec b, PVec c) { return {{fmaf(a.v[0], b.v[0], c.v[0])}}; }
+  __device__ __forceinline__ static PVec fma_rd(PVec a, PVec b, PVec c) { return {{__fmaf_rd(a.v[0], b.v[0], c.v[0])}}; }
+  __device__ __forceinline__ static PVec add(PVec a, PVec b) { return {{a.v[0] + b.v[0]}}; }
+};
+template <> struct PVec<2> {
+  float v[2];
+  __device__ __forceinline__ static PVec splat(float a) { return {{a, a}}; }
+  __device__ __forceinline__ static PVec from(float2 f) { return {{f.x, f.y}}; }
+  __device__ __forceinline__ float2 f2() const { return make_float2(v[0], v[1]); }
+  __device__ __forceinline__ static PVec fma(PVec a, PVec b, PVec c) { return from(__ffma2_rn(a.f2(), b.f2(), c.f2())); }
+  __device__ __forceinline__ static PVec fma_rd(PVec a, PVec b, PVec c) { return from(__ffma2_rd(a.f2(), b.f2(), c.f2())); }
+  __device__ __forceinline__ static PVec add(PVec a, PVec b) { return from(__fadd2_rn(a.f2(), b.f2())); }
+};
+
+// The knock-out branch of the Phoenix state machine (p32_phoenix_step) for one live path.
+template <bool REC>
+__device__ __forceinline__ void p32_knock_out(P32Phoenix& st, uint32_t fl, int t, const DevTrade& tr,
+                                              const DevTables& tb, const float* __restrict__ df, int period) {
+  st.alive = false;
+  st.ko_step = t;
+  const float due = (fl & STEP_FIXED_DUE) ? tr.coupon_f : (float)st.qual * __ldg(tb.accr_f + period);
+  const float carry = due > 0.0f ? (float)st.unpaid * tr.coupon_f : 0.0f;
+  if (due + carry > 0.0f) {
+    const float d = __ldg(df + t);
+    st.cpv = fmaf(due, d, st.cpv);
+    st.mpv = fmaf(carry, d, st.mpv);
+    st.received = true;
+    if (REC) ++st.paid;
+  }
+}
+
+// Phase clocks, a build option (RG_PHASE_CLOCKS, see riga_gb300/build.py): thread 0 of every CTA
+// reads clock64 at each phase boundary — the CTA's wall time in generation (0), bridge (1),
+// stepping (2) and path close (3) — and adds its totals to g_p32_phase_clocks at exit
+// (rg_phase_clocks).  Off in the product build.
+#ifdef RG_PHASE_CLOCKS
+__device__ unsigned long long g_p32_phase_clocks[4];
+#define RG_PHASE_BEGIN()                        \
+  unsigned long long rg_pc[4] = {0, 0, 0, 0}; \
+  long long rg_pt = clock64();
+#define RG_PHASE_MARK(k)                                \
+  if (threadIdx.x == 0) {                               \
+    const long long rg_now = clock64();                 \
+    rg_pc[k] += (unsigned long long)(rg_now - rg_pt);   \
+    rg_pt = rg_now;                                     \
+  }
+#define RG_PHASE_END()         \
+  if (threadIdx.x == 0)        \
+    for (int rg_k = 0; rg_k < 4; ++rg_k) atomicAdd(&g_p32_phase_clocks[rg_k], rg_pc[rg_k]);
+#else
+#define RG_PHASE_BEGIN()
+#define RG_PHASE_MARK(k)
+#define RG_PHASE_END()
+#endif
+
+template <int N, bool LV, bool REC, int PPT>
+__global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
     const DevScen32* __restrict__ scen32, int S, int Pb, int TT, int NNmax, int stack_max,
     float ln_ko, float ln_cb, float ln_ki, uint64_t path0, uint64_t npaths, const uint32_t* __restrict__ plan,
     double* __restrict__ partial, int32_t* __restrict__ ko_steps, rg_path_record* __restrict__ records) {
+  using V = PVec<PPT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, lane = tid & 31;
-  const int PbN = Pb * N;
-  const int nch = Pb / GEN_CH;
-  const int lg_pb = __ffs(Pb) - 1;  // Pb is a power of two
+  const int lg_pb = __ffs(Pb) - 1;  // Pb is a power of two, at least 32
   const int zs = p32_zrow(N, Pb);    // floats per Z row
-  const int dws = PbN + 1;           // floats per dW step
+  const int dws = p32_dwstep(N, Pb, PPT);
   const int T = (int)tr.steps;
+  const uint64_t nchunks = (npaths + 31) / 32;
   // ---- shared-memory carve-up (the host sizes the launch from the same layout)
-  const P32Layout L = p32_layout(S, N, Pb, TT, NNmax, stack_max, (int)blockDim.x);
+  const P32Layout L = p32_layout(N, Pb, TT, NNmax, stack_max, PPT);
   uint32_t dyn_bytes;
   asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
   if (L.total > dyn_bytes) {
-    // launched with less shared memory than the layout needs: touch none of it, poison this
-    // block's sums so the host reports the launch as failed
-    for (int k = tid; k < S * RG_ACC; k += blockDim.x)
-      partial[(size_t)blockIdx.x * S * RG_ACC + k] = __longlong_as_double(0x7ff8000000000000LL);
+    // launched with less shared memory than the layout needs: touch none of it, poison the sums
+    // of this block's first chunk so the host reports the launch as failed
+    if ((uint64_t)blockIdx.x * Pb < npaths)
+      for (int k = tid; k < S * RG_ACC; k += blockDim.x)
+        partial[(size_t)((uint64_t)blockIdx.x * Pb / 32) * S * RG_ACC + k] = __longlong_as_double(0x7ff8000000000000LL);
     return;
   }
-  double* acc = reinterpret_cast<double*>(smem_raw + L.acc);
-  // per (scenario, asset): (a_u/(gx-1), inv_h/(gx-1), row offset - 0x4B000000 as bits, x0)
-  float4* s_lv = reinterpret_cast<float4*>(smem_raw + L.lv);
   uint32_t* s_flags = reinterpret_cast<uint32_t*>(smem_raw + L.flags);
   int32_t* s_per = reinterpret_cast<int32_t*>(smem_raw + L.per);
+  float2* s_thr = reinterpret_cast<float2*>(smem_raw + L.thr);
   int32_t* s_noff = reinterpret_cast<int32_t*>(smem_raw + L.noff);
   float* s_ncf = reinterpret_cast<float*>(smem_raw + L.ncf);
+  uint32_t* s_nfrow = reinterpret_cast<uint32_t*>(smem_raw + L.qmc);  // [node][factor]
+  uint32_t* s_nfsh = s_nfrow + NNmax * N;                              // [node][factor]
+  uint32_t* s_nodek = s_nfsh + NNmax * N;                              // [node]
   uint32_t* s_pnode = reinterpret_cast<uint32_t*>(smem_raw + L.plan);
   uint32_t* s_plev = s_pnode + NNmax;
   uint32_t* s_pstep = s_plev + NNmax + 1;
   uint32_t* s_pstk = s_pstep + TT;
   float* Z = reinterpret_cast<float*>(smem_raw + L.z);
   float* dW = reinterpret_cast<float*>(smem_raw + L.dw);
-  double* red = reinterpret_cast<double*>(Z);  // reduction scratch, reused after the time loop
 
-  for (int k = tid; k < S * RG_ACC; k += blockDim.x) acc[k] = 0.0;
-
-  const int s = tid / Pb, pl = tid % Pb;
+  // stepping: thread tid serves scenario s and paths pl0 .. pl0 + PPT - 1 of each tile
+  const int tps = Pb / PPT;  // threads per scenario
+  const int s = tid / tps, pl0 = (tid % tps) * PPT;
   const bool lane_ok = s < S;
-  const int gx = tr.gx;
-  const float gxm1 = (float)(gx - 1);
-  const float nhdt = (float)(-0.5 * tr.dt);
-
-  // scenario constants: the Cholesky factor and drifts in registers; the per-asset local-vol
-  // constants (warp-uniform) in shared memory
-  for (int i = tid; i < S * N; i += blockDim.x) {
-    const DevScen32& s3 = scen32[i / N];
-    const int f = i % N;
-    const float inv_gxm1 = 1.0f / (float)(tr.gx - 1);
-    s_lv[i] = make_float4(s3.a_u[f] * inv_gxm1, s3.inv_h[f] * inv_gxm1,
-                          __int_as_float((int)((uint32_t)s3.surf_off[f] - 0x4B000000u)), s3.x0[f]);
-  }
-  float Lf[N * (N + 1) / 2], mu[N], sig[N];
   const int ss = lane_ok ? s : 0;
+  // a warp whose first thread has no scenario (padded scenario slots) skips the stepping phase
+  const bool warp_on = ((tid & ~31) / tps) < S;
+  const int gx = tr.gx;
+  const V gxm1 = V::splat((float)(gx - 1));
+  const V two23 = V::splat(8388608.0f), neg1 = V::splat(-1.0f);
+  const V nhdt = V::splat((float)(-0.5 * tr.dt));
+  // generation and bridge: warp-wide items over 32-path groups of the tile
+  const int ngrp = Pb >> 5, lg_ngrp = lg_pb - 5;
+  const int ncg = N * ngrp;  // chain groups (factor, path group)
+  const int nwarp = (int)(blockDim.x >> 5), wid = tid >> 5;
+
+  // scenario constants in registers: the Cholesky factor, drifts, flat vols and the per-asset
+  // local-vol lookup constants (a_u/(gx-1), inv_h/(gx-1), row offset - 0x4B000000, x0)
+  V Lf[N * (N + 1) / 2], mu[N], sig[N];
+  float lva[N], lvb[N], x0[N];
+  uint32_t lvo[N];
   {
     const DevScenario& sc = scen[ss];
     const DevScen32& s3 = scen32[ss];
+    const float inv_gxm1 = 1.0f / (float)(gx - 1);
     int q = 0;
 #pragma unroll
     for (int a = 0; a < N; ++a)
 #pragma unroll
-      for (int b = 0; b <= a; ++b) Lf[q++] = (float)sc.L[a * N + b];
+      for (int b = 0; b <= a; ++b) Lf[q++] = V::splat((float)sc.L[a * N + b]);
 #pragma unroll
     for (int f = 0; f < N; ++f) {
-      mu[f] = s3.mu_dt[f];
-      sig[f] = s3.sig[f];
+      mu[f] = V::splat(s3.mu_dt[f]);
+      sig[f] = V::splat(s3.sig[f]);
+      lva[f] = s3.a_u[f] * inv_gxm1;
+      lvb[f] = s3.inv_h[f] * inv_gxm1;
+      lvo[f] = (uint32_t)s3.surf_off[f] - 0x4B000000u;
+      x0[f] = s3.x0[f];
     }
   }
-  const float4* lvc = s_lv + ss * N;
-  __syncthreads();
+  const float* __restrict__ dfs = tb.df_f + (size_t)ss * T;
 
+  RG_PHASE_BEGIN();
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t tile0 = tile * Pb;
     for (int i = tid; i < zs; i += blockDim.x) Z[(size_t)NNmax * zs + i] = 0.0f;  // W(0)
-    const uint64_t gi = tile0 + pl;
-    const bool ok = lane_ok && gi < npaths;
-    float x[N];
+    bool ok[PPT];
+    V x[N];
+    P32Phoenix ph[PPT];
+    float worst[PPT];
 #pragma unroll
-    for (int f = 0; f < N; ++f) x[f] = lvc[f].w;
-    P32Phoenix ph;
-    float worst = 0.0f;
+    for (int j = 0; j < PPT; ++j) {
+      ok[j] = lane_ok && tile0 + pl0 + j < npaths;
+      ph[j].alive = ok[j];
+      worst[j] = 0.0f;
+    }
+#pragma unroll
+    for (int f = 0; f < N; ++f) x[f] = V::splat(x0[f]);
     for (int t0 = 0; t0 < T; t0 += TT) {
       const int tn = min(TT, T - t0);
       const int n0 = __ldg(tb.node_off + t0), n1 = __ldg(tb.node_off + t0 + tn);
       const int nn = n1 - n0;
       // ---- G: standard normals of the tile's bridge nodes, and the tile's step schedule
       for (int i = tid; i < tn; i += blockDim.x) {
-        s_flags[i] = __ldg(tb.step_flags + t0 + i);
+        const uint32_t fl = __ldg(tb.step_flags + t0 + i);
+        s_flags[i] = fl;
         s_per[i] = __ldg(tb.step_period + t0 + i);
+        s_thr[i] = make_float2((fl & STEP_ACCRUE) ? ln_cb : INFINITY, (fl & STEP_CALL_ACTIVE) ? ln_ko : INFINITY);
       }
       for (int i = tid; i <= tn; i += blockDim.x) s_noff[i] = __ldg(tb.node_off + t0 + i);
-      for (int i = tid; i < nn; i += blockDim.x) s_ncf[i] = __ldg(tb.node_cf + n0 + i);
+      for (int i = tid; i < nn; i += blockDim.x) {
+        s_ncf[i] = __ldg(tb.node_cf + n0 + i);
+        s_nodek[i] = (uint32_t)__ldg(tb.node_k + n0 + i);
+      }
+      if (tr.vr == RG_VR_SOBOL)
+        for (int i = tid; i < nn * N; i += blockDim.x) {
+          s_nfrow[i] = (uint32_t)__ldg(tb.nf_row + n0 * N + i);
+          s_nfsh[i] = __ldg(tb.nf_shift + n0 * N + i);
+        }
+      __syncthreads();
       const uint32_t* hd = plan + 1 + (size_t)(t0 / TT) * 6;
       const uint32_t nlev = __ldg(hd + 2), stk_cnt = __ldg(hd + 4);
       {
@@ -184,209 +267,283 @@ __global__ void __launch_bounds__(1024, 1) phoenix32_kernel(
         for (int i = tid; i < tn; i += blockDim.x) s_pstep[i] = __ldg(plan + steps_base + t0 + i);
         for (int i = tid; i < (int)stk_cnt; i += blockDim.x) s_pstk[i] = __ldg(plan + stk_base + i);
       }
-      const int ntask = nn * N * nch;
-      for (int task = tid; task < ntask; task += blockDim.x) {
-        const int c = task % nch, rem = task / nch, f = rem % N, j = rem / N;
-        const int nd = n0 + j;
-        const uint64_t g0 = tile0 + (uint64_t)c * GEN_CH;
-        if (g0 >= npaths) continue;  // these paths are never read
-        float* zo = Z + (size_t)j * zs + f * (Pb + 4) + c;
-        if (tr.vr == RG_VR_SOBOL) {
-          const uint32_t* row = tb.sobol + 32 * (size_t)__ldg(tb.nf_row + nd * N + f);
-          uint64_t n = path0 + g0 + 1;
-          uint32_t xs = rg_sobol_gray(row, n);
-          if (tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT) {
-            const uint32_t shift = __ldg(tb.nf_shift + nd * N + f);
-#pragma unroll
-            for (int q = 0; q < GEN_CH; ++q) {
-              if (q) {
-                ++n;
-                xs ^= __ldg(row + (__ffsll((long long)n) - 1));
-              }
-              zo[q * nch] = rg_probit32(xs ^ shift);
-            }
-          } else {
-            const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
-            for (int q = 0; q < GEN_CH; ++q) {
-              if (q) {
-                ++n;
-                xs ^= __ldg(row + (__ffsll((long long)n) - 1));
-              }
-              zo[q * nch] = rg_probit32(rg_owen(xs, dim, tr.seed));
-            }
-          }
-        } else {
-          const uint64_t dim = (uint64_t)__ldg(tb.node_k + nd) * N + f;
-          for (int q = 0; q < GEN_CH; ++q) zo[q * nch] = rg_qmc_normal32(tr, tb, path0 + g0 + q, dim);
-        }
-      }
-      __syncthreads();
-      // ---- B: the tile's bridge nodes in the plan's dependency levels, then the increments.  Warp
-      // w owns chains [w·cpw, w·cpw + nc) (chain c = path c % Pb, factor c / Pb): its lanes
-      // evaluate one level's nodes of those chains at once, W = z·c + (W_left + W_right) / 2 —
-      // the streamed bridge's arithmetic on the same anchors, so the values are identical — each
-      // written over its normal in Z; then dW of every step, and the state carried to the next
-      // tile (the value at the tile end, the stack entries pushed in the tile).  Every anchor is
-      // a row of Z, so an evaluation is four loads and one FMA.
       {
-        const int nwarp = (int)(blockDim.x >> 5);
-        const int cpw = (PbN + nwarp - 1) / nwarp;  // at most 64 (host-checked)
-        const int c_lo = (tid >> 5) * cpw;
-        const int nc = max(0, min(cpw, PbN - c_lo));
-        const int nc1 = nc < 32 ? max(nc, 1) : 32;
-        const int G = 32 / nc1, q0 = lane / nc1;  // G node slots at once; this lane's first
-        const bool lane_on = nc > 0 && lane < G * nc1;
-        const int cA = c_lo + lane % nc1, cB = cA + 32;  // this lane's chains (B when nc > 32)
-        const bool hasB = lane_on && cB < c_lo + nc;
-        auto zoff_of = [&](int c) {
-          const int p = c & (Pb - 1);
-          return (c >> lg_pb) * (Pb + 4) + (p & (GEN_CH - 1)) * nch + (p >> 3);
-        };
-        const int zA = zoff_of(cA), zB = zoff_of(cB);
-        auto eval = [&](uint32_t e, float cf, int zo) {
-          float* zp = Z + (int)(e & 511u) * zs + zo;
-          const float z = *zp;
-          const float l = Z[(int)((e >> 9) & 511u) * zs + zo], r = Z[(int)((e >> 18) & 511u) * zs + zo];
-          *zp = (e >> 27) ? z * cf : fmaf(z, cf, 0.5f * (l + r));
-        };
-        for (uint32_t L = 0; L < nlev; ++L) {
-          const int a = (int)s_plev[L], b = (int)s_plev[L + 1];
-          if (lane_on)
-            for (int q = a + q0; q < b; q += G) {
-              const uint32_t e = s_pnode[q];
-              const float cf = s_ncf[e & 511u];
-              eval(e, cf, zA);
-              if (hasB) eval(e, cf, zB);
+        // kGB items per warp at a time in straight-line code, so that their global loads, shuffles
+        // and inverse normals overlap; a warp's surplus slots recompute its last item (the same
+        // values stored twice), and items of paths past the request compute values nobody reads
+        constexpr int kGB = 4;
+        const int nitems = nn << lg_ngrp;
+        const bool shift_lane = tr.vr == RG_VR_SOBOL && tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT;
+        for (int base = wid; base < nitems; base += kGB * nwarp) {
+          int jj[kGB], hh[kGB];
+#pragma unroll
+          for (int u = 0; u < kGB; ++u) {
+            const int it = min(base + u * nwarp, nitems - 1);
+            jj[u] = it >> lg_ngrp;
+            hh[u] = it & (ngrp - 1);
+          }
+          if (shift_lane) {
+            uint32_t xs[kGB][N];
+#pragma unroll
+            for (int u = 0; u < kGB; ++u) {
+              const uint64_t n1 = path0 + tile0 + ((uint64_t)hh[u] << 5) + 1;  // Sobol point of lane 0
+#pragma unroll
+              for (int f = 0; f < N; ++f)
+                xs[u][f] = rg_warp_sobol(tb.sobol + 32 * (size_t)s_nfrow[jj[u] * N + f], n1, lane) ^ s_nfsh[jj[u] * N + f];
             }
-          __syncwarp();
-        }
-        if (lane_on)
-          for (int tt = q0; tt < tn; tt += G) {
-            const int hi = (int)s_pstep[tt] * zs;
-            const int lo = tt == 0 ? NNmax * zs : (int)s_pstep[tt - 1] * zs;
-            dW[tt * dws + cA] = Z[hi + zA] - Z[lo + zA];
-            if (hasB) dW[tt * dws + cB] = Z[hi + zB] - Z[lo + zB];
+#pragma unroll
+            for (int u = 0; u < kGB; ++u)
+#pragma unroll
+              for (int f = 0; f < N; ++f)
+                Z[(size_t)jj[u] * zs + f * (Pb + 4) + (hh[u] << 5) + lane] = rg_probit32(xs[u][f]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < kGB; ++u) {
+              const uint64_t g0 = tile0 + ((uint64_t)hh[u] << 5);
+              float* zo = Z + (size_t)jj[u] * zs + (hh[u] << 5) + lane;
+              if (tr.vr == RG_VR_SOBOL) {
+                const uint64_t n1 = path0 + g0 + 1;
+#pragma unroll
+                for (int f = 0; f < N; ++f) {
+                  const uint32_t xs = rg_warp_sobol(tb.sobol + 32 * (size_t)s_nfrow[jj[u] * N + f], n1, lane);
+                  zo[f * (Pb + 4)] = rg_probit32(rg_owen(xs, (uint64_t)s_nodek[jj[u]] * N + f, tr.seed));
+                }
+              } else {
+#pragma unroll
+                for (int f = 0; f < N; ++f)
+                  zo[f * (Pb + 4)] = rg_qmc_normal32(tr, tb, path0 + g0 + lane, (uint64_t)s_nodek[jj[u]] * N + f);
+              }
+            }
           }
-        __syncwarp();
-        if (lane_on && q0 == 0) {
-          const int wrow = (int)s_pstep[tn - 1] * zs;
-          const float wnA = Z[wrow + zA], wnB = hasB ? Z[wrow + zB] : 0.0f;
-          for (uint32_t k = 0; k < stk_cnt; ++k) {
-            const uint32_t e = s_pstk[k];  // (destination row, tile node)
-            Z[(int)(e >> 9) * zs + zA] = Z[(int)(e & 511u) * zs + zA];
-            if (hasB) Z[(int)(e >> 9) * zs + zB] = Z[(int)(e & 511u) * zs + zB];
-          }
-          Z[NNmax * zs + zA] = wnA;
-          if (hasB) Z[NNmax * zs + zB] = wnB;
         }
       }
       __syncthreads();
-      // ---- S: scenario stepping
-      if (ok) {
-        for (int tt = 0; tt < tn; ++tt) {
-          const int tg = (t0 + tt) * gx;
-          float d[N], y[N];
+      RG_PHASE_MARK(0);
+      // ---- B: the tile's bridge nodes level by level from the plan (every node after its
+      // anchors), W = z·c + (W_left + W_right) / 2 on the streamed bridge's anchors — so the
+      // values are its values — each written over its normal in Z.  Warp w takes chain groups
+      // (factor, 32-path group) w, w + nwarp, ...; a lane owns one chain (one column of Z), so it
+      // needs no synchronisation with other lanes, and the nodes of one level, which never read
+      // each other, are loaded kB at a time before any of them is stored.  Then the chain's dW of
+      // every step, and the state it carries to the next tile (the value at the tile end, the
+      // stack entries pushed in the tile).
+      for (int cg = wid; cg < ncg; cg += nwarp) {
+        const int c = (cg >> lg_ngrp) * (Pb + 4) + ((cg & (ngrp - 1)) << 5) + lane;
+        constexpr int kB = 8;
+        for (uint32_t lv = 0; lv < nlev; ++lv) {
+          const int a = (int)s_plev[lv], b = (int)s_plev[lv + 1];
+          for (int q = a; q < b; q += kB) {
+            // straight-line batch: surplus slots recompute the level's last node (same value)
+            float val[kB];
+            int row[kB];
 #pragma unroll
-          for (int f = 0; f < N; ++f) d[f] = dW[tt * dws + f * Pb + pl];
+            for (int u = 0; u < kB; ++u) {
+              const uint32_t e = s_pnode[min(q + u, b - 1)];
+              const float cf = s_ncf[e & 511u];
+              row[u] = (int)(e & 511u) * zs + c;
+              const float z = Z[row[u]];
+              const float l = Z[(int)((e >> 9) & 511u) * zs + c], r = Z[(int)((e >> 18) & 511u) * zs + c];
+              val[u] = (e >> 27) ? z * cf : fmaf(z, cf, 0.5f * (l + r));
+            }
+#pragma unroll
+            for (int u = 0; u < kB; ++u) Z[row[u]] = val[u];
+          }
+        }
+        float* dwc = dW + (cg >> lg_ngrp) * Pb + ((cg & (ngrp - 1)) << 5) + lane;
+        for (int t1 = 0; t1 < tn; t1 += kB) {
+          float dv[kB];
+          int tt[kB];
+#pragma unroll
+          for (int u = 0; u < kB; ++u) {
+            tt[u] = min(t1 + u, tn - 1);
+            const int lo = tt[u] == 0 ? NNmax * zs : (int)s_pstep[tt[u] - 1] * zs;
+            dv[u] = Z[(int)s_pstep[tt[u]] * zs + c] - Z[lo + c];
+          }
+#pragma unroll
+          for (int u = 0; u < kB; ++u) dwc[tt[u] * dws] = dv[u];
+        }
+        const float wlo = Z[(int)s_pstep[tn - 1] * zs + c];  // the value at the tile end
+        for (uint32_t k = 0; k < stk_cnt; ++k) {
+          const uint32_t e = s_pstk[k];  // (destination row, tile node)
+          Z[(int)(e >> 9) * zs + c] = Z[(int)(e & 511u) * zs + c];
+        }
+        Z[NNmax * zs + c] = wlo;  // the value at the tile end
+      }
+      __syncthreads();
+      RG_PHASE_MARK(1);
+      // ---- S: scenario stepping.  Every thread of a warp with a scenario runs it (threads of
+      // padded slots and paths past the request with their Phoenix state dead), so the
+      // knock-out test can vote warp-wide.
+      if (warp_on) {
+        for (int tt = 0; tt < tn; ++tt) {
+          const int t = t0 + tt;
+          const int tg = t * gx;
+          V d[N], y[N];
+#pragma unroll
+          for (int f = 0; f < N; ++f) {
+            const float* dp = dW + tt * dws + f * Pb + pl0;
+            if constexpr (PPT == 2) d[f] = V::from(*reinterpret_cast<const float2*>(dp));
+            else d[f] = V::splat(*dp);
+          }
           int q = 0;
 #pragma unroll
           for (int a = 0; a < N; ++a) {
-            float acc_y = 0.0f;
+            V acc_y = V::fma(Lf[q++], d[0], V::splat(0.0f));
 #pragma unroll
-            for (int b = 0; b <= a; ++b) acc_y = fmaf(Lf[q++], d[b], acc_y);
+            for (int b = 1; b <= a; ++b) acc_y = V::fma(Lf[q++], d[b], acc_y);
             y[a] = acc_y;
           }
-          float wmin = INFINITY;
+          float wmin[PPT];
+#pragma unroll
+          for (int j = 0; j < PPT; ++j) wmin[j] = INFINITY;
 #pragma unroll
           for (int f = 0; f < N; ++f) {
-            float sg;
+            V sg;
             if (LV) {
               // sigma at the step's time row, linear in log-spot.  u01 = the grid position scaled
               // to [0, 1], clamped by the FMA's saturation (NaN -> 0); 2^23 + floor(u01·(gx-1))
               // by one round-down FMA, whose bit pattern minus 0x4B000000 is the grid index —
-              // that bias is folded into the row offset c4.z; then one (value, slope) gather
-              const float4 c4 = lvc[f];
-              const float u01 = __saturatef(fmaf(x[f], c4.y, c4.x));
-              const float fl = __fmaf_rd(u01, gxm1, 8388608.0f);
-              const float w = fmaf(u01, gxm1, 8388608.0f - fl);
-              const uint32_t idx = (uint32_t)__float_as_int(c4.z) + (uint32_t)tg + (uint32_t)__float_as_int(fl);
-              const float2 r = __ldg(tb.lv_rows + idx);
-              sg = fmaf(w, r.y, r.x);
+              // that bias is folded into the row offset lvo; then one (value, slope) gather
+              V u01;
+#pragma unroll
+              for (int j = 0; j < PPT; ++j) u01.v[j] = __saturatef(fmaf(x[f].v[j], lvb[f], lva[f]));
+              const V fl = V::fma_rd(u01, gxm1, two23);
+              const V w = V::fma(u01, gxm1, V::fma(fl, neg1, two23));
+#pragma unroll
+              for (int j = 0; j < PPT; ++j) {
+                const uint32_t idx = lvo[f] + (uint32_t)tg + (uint32_t)__float_as_int(fl.v[j]);
+                const float2 r = __ldg(tb.lv_rows + idx);
+                sg.v[j] = fmaf(w.v[j], r.y, r.x);
+              }
             } else {
               sg = sig[f];
             }
-            x[f] = fmaf(sg, fmaf(nhdt, sg, y[f]), x[f]) + mu[f];
-            wmin = fminf(wmin, x[f]);
+            x[f] = V::add(V::fma(sg, V::fma(nhdt, sg, y[f]), x[f]), mu[f]);
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) wmin[j] = fminf(wmin[j], x[f].v[j]);
           }
-          worst = wmin;
-          if (ph.alive)
-            p32_phoenix_step<REC>(ph, s_flags[tt], t0 + tt, wmin, ln_cb, ln_ko, tr, tb, tb.df_f + (size_t)ss * T,
-                                  [&] { return s_per[tt]; });
+#pragma unroll
+          for (int j = 0; j < PPT; ++j) worst[j] = wmin[j];
+          // Phoenix state machine (note.rs:150-218).  Steps that reset or close a coupon period
+          // (two in a period) take the full machine; on every other step a live path accrues and
+          // tests the knock-out branch-free against the step's thresholds (+inf where the step
+          // does not accrue or cannot call), and the knock-out branch runs when some path of the
+          // warp knocks out.
+          const uint32_t fl = s_flags[tt];
+          if (fl & (STEP_PERIOD_RESET | STEP_PERIOD_END)) {
+#pragma unroll
+            for (int j = 0; j < PPT; ++j)
+              if (ph[j].alive)
+                p32_phoenix_step<REC>(ph[j], fl, t, wmin[j], ln_cb, ln_ko, tr, tb, dfs, [&] { return s_per[tt]; });
+          } else {
+            const float2 th = s_thr[tt];
+            bool hit[PPT], any = false;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+              const bool a = ph[j].alive;
+              const bool acc = a & (wmin[j] >= th.x);
+              ph[j].qual += acc;
+              if (REC) ph[j].qualified += acc;
+              hit[j] = a & (wmin[j] >= th.y);
+              any |= hit[j];
+            }
+            if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+              for (int j = 0; j < PPT; ++j)
+                if (hit[j]) p32_knock_out<REC>(ph[j], fl, t, tr, tb, dfs, s_per[tt]);
+            }
+          }
         }
       }
       __syncthreads();
+      RG_PHASE_MARK(2);
     }
-    // ---- path close (note.rs:221-258) and the per-tile reduction
-    float out[RG_ACC];
-    p32_close_path<REC>(tr, tb, ss, T, ok, s == 0, path0, gi, ph.ko_step, worst, ln_ki, ph.cpv, ph.mpv,
-                        ph.received, ph.qualified, ph.paid, ko_steps, records, out);
-    // butterfly within each group of lanes that share a scenario (g = min(32, Pb) lanes)
-    const int g = Pb < 32 ? Pb : 32;
-    for (int off = g >> 1; off > 0; off >>= 1)
+    // ---- path close (note.rs:221-258) and the sums of each 32-path chunk: FP32 values per path,
+    // a fixed FP32 shuffle butterfly over the chunk (path offsets 16, 8, 4, 2, 1 — with two paths
+    // per thread the last offset is the thread's own pair, so the tree is the same), the chunk's
+    // 16 sums as FP64 to partial[chunk][scenario] by its first 16 lanes.  The chunk sums, and the
+    // reduction over chunks in chunk order, do not depend on the launch shape.
+    if (warp_on) {
+      float out[PPT][RG_ACC];
 #pragma unroll
-      for (int k = 0; k < RG_ACC; ++k) out[k] += __shfl_xor_sync(0xffffffffu, out[k], off);
-    if ((lane % g) == 0)
+      for (int j = 0; j < PPT; ++j)
+        p32_close_path<REC>(tr, tb, ss, T, ok[j], s == 0, path0, tile0 + pl0 + j, ph[j].ko_step, worst[j],
+                            ln_ki, ph[j].cpv, ph[j].mpv, ph[j].received, ph[j].qualified, ph[j].paid,
+                            ko_steps, records, out[j]);
+      constexpr int LG = 32 / PPT;  // lanes per chunk
+      for (int off = LG >> 1; off > 0; off >>= 1)
 #pragma unroll
-      for (int k = 0; k < RG_ACC; ++k) red[(size_t)(tid / g) * RG_ACC + k] = (double)out[k];
-    __syncthreads();
-    const int groups_per_scen = Pb / g;
-    for (int jx = tid; jx < S * RG_ACC; jx += blockDim.x) {
-      const int ss = jx / RG_ACC, k = jx % RG_ACC;
-      double v = 0.0;
-      for (int w = 0; w < groups_per_scen; ++w) v += red[(size_t)(ss * groups_per_scen + w) * RG_ACC + k];
-      acc[jx] += v;
+        for (int j = 0; j < PPT; ++j)
+#pragma unroll
+          for (int k = 0; k < RG_ACC; ++k) out[j][k] += __shfl_xor_sync(0xffffffffu, out[j][k], off);
+      float mine = 0.0f;
+      const int lk = lane & (LG - 1);
+#pragma unroll
+      for (int k = 0; k < RG_ACC; ++k) {
+        const float v = PPT == 2 ? out[0][k] + out[PPT - 1][k] : out[0][k];
+        mine = lk == k ? v : mine;
+      }
+      const uint64_t chunk = (tile0 + (uint64_t)(pl0 & ~31)) >> 5;
+      if (lane_ok && lk < RG_ACC && chunk < nchunks)
+        partial[((size_t)chunk * S + s) * RG_ACC + lk] = (double)mine;
     }
-    __syncthreads();
+    RG_PHASE_MARK(3);
   }
-  for (int jx = tid; jx < S * RG_ACC; jx += blockDim.x) partial[(size_t)blockIdx.x * S * RG_ACC + jx] = acc[jx];
+  RG_PHASE_END();
 }
 
-template <int N, bool LV>
+template <int N, bool LV, int PPT>
 static const void* kernel_ptr(bool rec) {
-  return rec ? reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, true>)
-             : reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, false>);
+  return rec ? reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, true, PPT>)
+             : reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, false, PPT>);
 }
 
-static const void* select_kernel(int n, bool lv, bool rec) {
+template <int PPT>
+static const void* select_kernel_ppt(int n, bool lv, bool rec) {
   switch (n) {
-    case 1: return lv ? kernel_ptr<1, true>(rec) : kernel_ptr<1, false>(rec);
-    case 2: return lv ? kernel_ptr<2, true>(rec) : kernel_ptr<2, false>(rec);
-    case 3: return lv ? kernel_ptr<3, true>(rec) : kernel_ptr<3, false>(rec);
-    case 4: return lv ? kernel_ptr<4, true>(rec) : kernel_ptr<4, false>(rec);
-    case 5: return lv ? kernel_ptr<5, true>(rec) : kernel_ptr<5, false>(rec);
+    case 1: return lv ? kernel_ptr<1, true, PPT>(rec) : kernel_ptr<1, false, PPT>(rec);
+    case 2: return lv ? kernel_ptr<2, true, PPT>(rec) : kernel_ptr<2, false, PPT>(rec);
+    case 3: return lv ? kernel_ptr<3, true, PPT>(rec) : kernel_ptr<3, false, PPT>(rec);
+    case 4: return lv ? kernel_ptr<4, true, PPT>(rec) : kernel_ptr<4, false, PPT>(rec);
+    case 5: return lv ? kernel_ptr<5, true, PPT>(rec) : kernel_ptr<5, false, PPT>(rec);
     default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
   }
 }
 
+static const void* select_kernel(int n, bool lv, bool rec, int ppt) {
+  return ppt == 2 ? select_kernel_ppt<2>(n, lv, rec) : select_kernel_ppt<1>(n, lv, rec);
+}
+
+// Paths per thread of the formula shape: two (packed FP32x2 stepping, 512 threads) unless the
+// autotuner measured one faster for the launch shape.
+static constexpr int kDefaultPpt = 2;
+
+// Formula tile depth of a block of Pb paths.
+static int formula_tt(const Prepared& P, int Pb) {
+  int tt = (32768 / (Pb * P.n) - P.stack_max) / 2;
+  return tt < 8 ? 8 : (tt > 64 ? 64 : tt);
+}
+
+// Whether a tile of Pb paths at `ppt` paths per thread and `tt` steps fits: the shared-memory
+// layout within 227 KB.
+static bool p32_fits(const Prepared& P, int Pb, int ppt, int tt) {
+  return p32_layout(P.n, Pb, tt, tt + P.stack_max, P.stack_max, ppt).total <= 227u * 1024u;
+}
+
 // The tiled kernel's block and formula tile depth.  Scenario slots: S rounded up to a power of
-// two, at least 4 (two scenarios run padded: a CTA of 1024 threads on half the slots beats both
-// the direct kernel and a smaller CTA); the largest block of 1024, 512 or 256 threads whose
-// shared-memory layout fits.
-static void tiled_shape(const Prepared& P, Fp32Shape& sh) {
+// two, at least 4 (two scenarios run padded: a CTA on half the slots beats both the direct kernel
+// and a smaller CTA); Pb = 1024 / slots paths per tile (at least 32: the path chunks of the sums
+// lie inside one tile), served by 1024 threads (one path per thread) or 512 (two).
+static void tiled_shape(const Prepared& P, Fp32Shape& sh, int ppt) {
   int sb = 4;
   while (sb < P.n_scen) sb <<= 1;
   sh.Sb = sb;
-  const int N = P.n;
-  for (int threads = 1024; threads >= 256; threads >>= 1) {
-    sh.threads = threads;
-    sh.Pb = threads / sb;
-    const int PbN = sh.Pb * N;
-    int tt = (32768 / PbN - P.stack_max) / 2;
-    tt = tt < 8 ? 8 : (tt > 64 ? 64 : tt);
-    sh.TT = tt;
-    sh.smem = (int)p32_layout(P.n_scen, N, sh.Pb, tt, tt + P.stack_max, P.stack_max, threads).total;
-    if (sh.smem <= 227 * 1024 || threads == 256) break;
-  }
+  sh.Pb = 1024 / sb;
+  sh.TT = formula_tt(P, sh.Pb);
+  if (ppt == 2 && !p32_fits(P, sh.Pb, 2, sh.TT)) ppt = 1;
+  sh.ppt = ppt;
+  sh.threads = sb * sh.Pb / ppt;
+  sh.smem = (int)p32_layout(P.n, sh.Pb, sh.TT, sh.TT + P.stack_max, P.stack_max, ppt).total;
 }
 
 // Tile depths the autotuner times besides the formula depth.
@@ -494,7 +651,7 @@ static void build_bridge_plan(const std::vector<int32_t>& node_off, int64_t T, i
 
 std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P) {
   Fp32Shape sh{};
-  tiled_shape(P, sh);
+  tiled_shape(P, sh, kDefaultPpt);
   static std::mutex mu;
   static std::map<std::pair<int64_t, int>, std::shared_ptr<const BridgePlans>> cache;
   const std::pair<int64_t, int> key{P.T, sh.TT};
@@ -520,6 +677,44 @@ std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P) {
   return out;
 }
 
+// Function attributes are process-wide: raise every instantiation's dynamic shared-memory limit to
+// the device maximum once per device, so engines pricing concurrently never lower it under each other.
+static void p32_set_attributes() {
+  static std::mutex mu;
+  static std::vector<char> done;
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+  if (done[dev]) return;
+  int optin = 0;
+  cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem opt-in");
+  for (int ppt = 1; ppt <= 2; ++ppt)
+    for (int n = 1; n <= RG_NMAX; ++n)
+      for (int lv = 0; lv < 2; ++lv)
+        for (int rec = 0; rec < 2; ++rec) {
+          const void* kr = select_kernel(n, lv != 0, rec != 0, ppt);
+          cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
+                     "phoenix32 smem attribute");
+          cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                     "phoenix32 carveout");
+        }
+  done[dev] = 1;
+}
+
+// Grid of a tiled shape: as many CTAs as are resident on the SMs, at most one per tile.
+static int tiled_grid(const Prepared& P, const Fp32Shape& sh, uint64_t npaths, int sm_count) {
+  const void* k = select_kernel(P.n, P.trade.has_lv != 0, false, sh.ppt);
+  int per_sm = 0;
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, sh.threads, sh.smem),
+             "phoenix32 occupancy");
+  if (per_sm < 1) raise(RG_ERR_GPU_ERROR, "phoenix32: launch shape does not fit on an SM");
+  const uint64_t tiles = (npaths + sh.Pb - 1) / sh.Pb;
+  const uint64_t cap = (uint64_t)sm_count * per_sm;
+  const int grid = (int)(tiles < cap ? tiles : cap);
+  return grid < 1 ? 1 : grid;
+}
+
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
   Fp32Shape sh{};
   if (P.n_scen > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per fused launch");
@@ -528,59 +723,35 @@ Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count) {
     sh.direct = 1;
     sh.Sb = P.n_scen;
     sh.threads = 256;
+    sh.ppt = 1;
     sh.grid = phoenix32d_grid(P, npaths, sm_count);
     sh.smem = P.stack_max * P.n * 256 * (int)sizeof(float);  // the bridge stacks (dynamic)
     return sh;
   }
-  tiled_shape(P, sh);
-  // Function attributes are process-wide: raise every instantiation's dynamic shared-memory limit
-  // to the device maximum once, so engines pricing concurrently never lower it under each other.
-  {
-    static std::mutex mu;
-    static std::vector<char> done;
-    int dev = 0;
-    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-    std::lock_guard<std::mutex> lock(mu);
-    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
-    if (!done[dev]) {
-      int optin = 0;
-      cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem opt-in");
-      for (int n = 1; n <= RG_NMAX; ++n)
-        for (int lv = 0; lv < 2; ++lv)
-          for (int rec = 0; rec < 2; ++rec) {
-            const void* kr = select_kernel(n, lv != 0, rec != 0);
-            cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
-                       "phoenix32 smem attribute");
-            cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
-                       "phoenix32 carveout");
-          }
-      done[dev] = 1;
-    }
-  }
-  const void* k = select_kernel(P.n, P.trade.has_lv != 0, false);
-  int per_sm = 0;
-  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, sh.threads, sh.smem),
-             "phoenix32 occupancy");
-  if (per_sm < 1) raise(RG_ERR_GPU_ERROR, "phoenix32: launch shape does not fit on an SM");
-  uint64_t tiles = (npaths + sh.Pb - 1) / sh.Pb;
-  uint64_t cap = (uint64_t)sm_count * per_sm;
-  sh.grid = (int)(tiles < cap ? tiles : cap);
-  if (sh.grid < 1) sh.grid = 1;
+  tiled_shape(P, sh, kDefaultPpt);
+  if (sh.smem > 227 * 1024) raise(RG_ERR_GPU_ERROR, "phoenix32: the tile does not fit in shared memory");
+  p32_set_attributes();
+  sh.grid = tiled_grid(P, sh, npaths, sm_count);
   return sh;
 }
 
-// ---------------------------------------------------------------------- tile-depth autotuner --
+// Rows of the FP32 kernels' partial sums: one per 32-path chunk of the launch.
+uint64_t p32_chunks(uint64_t npaths) { return (npaths + 31) / 32; }
+
+// ---------------------------------------------------------------------- tiled-shape autotuner --
 namespace {
 std::mutex g_tune_mu;
-std::map<std::vector<int64_t>, int> g_tuned;  // launch shape -> tile depth
+std::map<std::vector<int64_t>, std::pair<int, int>> g_tuned;  // launch shape -> (paths per thread, tile depth)
 bool g_tune_enabled = true;
+std::pair<int, int> g_forced{0, 0};  // (paths per thread, tile depth) every tiled launch takes, or none
 
-// Sets the tile depth of a tiled-kernel shape if its layout fits next to the same block size.
-bool p32_with_tt(const Prepared& P, Fp32Shape& sh, int tt) {
-  const int smem = (int)p32_layout(P.n_scen, P.n, sh.Pb, tt, tt + P.stack_max, P.stack_max, sh.threads).total;
-  if (smem > 227 * 1024) return false;
+// Sets the paths per thread and tile depth of a tiled shape if its layout fits.
+bool p32_with(const Prepared& P, Fp32Shape& sh, int ppt, int tt) {
+  if (!p32_fits(P, sh.Pb, ppt, tt)) return false;
+  sh.ppt = ppt;
+  sh.threads = sh.Sb * sh.Pb / ppt;
   sh.TT = tt;
-  sh.smem = smem;
+  sh.smem = (int)p32_layout(P.n, sh.Pb, tt, tt + P.stack_max, P.stack_max, ppt).total;
   return true;
 }
 }  // namespace
@@ -591,37 +762,60 @@ void p32_set_autotune(bool enabled) {
   g_tuned.clear();
 }
 
+void p32_force_shape(int ppt, int tt) {
+  if (!((ppt == 0 && tt == 0) || ((ppt == 1 || ppt == 2) && tt > 0)))
+    raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: paths per thread 1 or 2 and a tile depth, or (0, 0)");
+  bool plan = tt == 0;
+  for (int c : kTileCandidates) plan = plan || c == tt;
+  if (!plan) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the tile depth must be one of the autotuner's candidates");
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_forced = {ppt, tt};
+}
+
+// Times every (paths per thread, tile depth) candidate on a prefix of the launch's paths and keeps
+// the fastest for the launch shape.  Neither knob changes a path's arithmetic or the 32-path chunks
+// of the sums, so prices are identical whichever wins.
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
                          const LaunchOut& out, bool may_tune, cudaStream_t st) {
-  // only the 1024-thread shapes, which hold one CTA per SM whatever the tile depth (the grid, the
-  // partial-sum buffer and the block's path grouping stay as they are)
-  if (sh.direct || sh.threads != 1024) return sh;
+  if (sh.direct) return sh;
   int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  int sm_count = 0;
+  cuda_check(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "SM count");
   const std::vector<int64_t> key{dev, P.n, P.trade.has_lv, P.n_scen, sh.Sb, P.T, P.stack_max,
                                  P.trade.vr, P.trade.scrambler, P.trade.gx};
+  auto apply = [&](std::pair<int, int> c, uint64_t paths) {
+    Fp32Shape t = sh;
+    if (!p32_with(P, t, c.first, c.second)) return sh;
+    t.grid = tiled_grid(P, t, paths, sm_count);
+    t.tuned = 1;
+    return t;
+  };
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (g_forced.first) {
+      Fp32Shape t = apply(g_forced, npaths);
+      if (!t.tuned) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the forced tile does not fit in shared memory");
+      return t;
+    }
     if (!g_tune_enabled) return sh;
     auto it = g_tuned.find(key);
-    if (it != g_tuned.end()) {
-      Fp32Shape t = sh;
-      if (p32_with_tt(P, t, it->second)) t.tuned = 1;
-      return t.tuned ? t : sh;
-    }
+    if (it != g_tuned.end()) return apply(it->second, npaths);
   }
   // a tuning pass costs about (candidates × 2) launches over two waves of tiles: only for
   // launches of at least eight waves
   const uint64_t prefix = (uint64_t)sh.grid * (uint64_t)sh.Pb * 2;
   if (!may_tune || npaths < prefix * 4) return sh;
-  std::vector<int> cand;
+  std::vector<std::pair<int, int>> cand;
   std::vector<int> tts{sh.TT};
   tts.insert(tts.end(), std::begin(kTileCandidates), std::end(kTileCandidates));
-  for (int tt : tts) {
-    Fp32Shape c = sh;
-    if (std::find(cand.begin(), cand.end(), tt) == cand.end() && p32_with_tt(P, c, tt)) cand.push_back(tt);
-  }
+  for (int ppt = 1; ppt <= 2; ++ppt)
+    for (int tt : tts) {
+      Fp32Shape c = sh;
+      const std::pair<int, int> pc{ppt, tt};
+      if (std::find(cand.begin(), cand.end(), pc) == cand.end() && p32_with(P, c, ppt, tt)) cand.push_back(pc);
+    }
   LaunchOut lo = out;  // the partial sums are overwritten by the real launch afterwards
   lo.ko_steps = nullptr;
   lo.records = nullptr;
@@ -631,8 +825,7 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   std::vector<float> best(cand.size(), 1e30f);
   for (int rep = 0; rep < 2; ++rep)
     for (size_t i = 0; i < cand.size(); ++i) {
-      Fp32Shape c = sh;
-      p32_with_tt(P, c, cand[i]);
+      const Fp32Shape c = apply(cand[i], prefix);
       cuda_check(cudaEventRecord(e0, st), "event");
       launch_phoenix32(P, tb, scen, scen32, path0, prefix, c, lo, st);
       cuda_check(cudaEventRecord(e1, st), "event");
@@ -644,12 +837,11 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   const size_t win = (size_t)(std::min_element(best.begin(), best.end()) - best.begin());
-  Fp32Shape t = sh;
-  p32_with_tt(P, t, cand[win]);
-  t.tuned = 1;
-  std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_tuned[key] = cand[win];
-  return t;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[key] = cand[win];
+  }
+  return apply(cand[win], npaths);
 }
 
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen,
@@ -665,13 +857,16 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
   for (int i = 0; i < tb.n_bplan; ++i)
     if (tb.bplan_tt[i] == sh.TT) plan = tb.bplan + tb.bplan_at[i];
   if (!plan) raise(RG_ERR_GPU_ERROR, "phoenix32: no bridge plan staged for the tile depth");
-  // the bridge phase gives each warp at most 64 chains (two per lane)
-  if ((sh.Pb * P.n + sh.threads / 32 - 1) / (sh.threads / 32) > 64)
-    raise(RG_ERR_GPU_ERROR, "phoenix32: too many bridge chains per warp");
+  if (sh.Pb < 32 || (sh.Pb & (sh.Pb - 1)) || sh.threads * sh.ppt != sh.Sb * sh.Pb || (sh.ppt != 1 && sh.ppt != 2))
+    raise(RG_ERR_GPU_ERROR, "phoenix32: invalid tile shape");
 #define RG_LAUNCH(NN, LVV)                                                                        \
-  if (out.records) RG_LAUNCH_R(NN, LVV, true) else RG_LAUNCH_R(NN, LVV, false)
-#define RG_LAUNCH_R(NN, LVV, REC)                                                                 \
-  phoenix32_kernel<NN, LVV, REC><<<sh.grid, sh.threads, sh.smem, st>>>(                           \
+  if (sh.ppt == 2) {                                                                              \
+    if (out.records) RG_LAUNCH_R(NN, LVV, true, 2) else RG_LAUNCH_R(NN, LVV, false, 2)            \
+  } else {                                                                                        \
+    if (out.records) RG_LAUNCH_R(NN, LVV, true, 1) else RG_LAUNCH_R(NN, LVV, false, 1)            \
+  }
+#define RG_LAUNCH_R(NN, LVV, REC, PPT)                                                            \
+  phoenix32_kernel<NN, LVV, REC, PPT><<<sh.grid, sh.threads, sh.smem, st>>>(                      \
       P.trade, tb, scen, scen32, P.n_scen, sh.Pb, sh.TT, NNmax, P.stack_max, ln_ko, ln_cb, ln_ki, \
       path0, npaths, plan, out.partial, out.ko_steps, out.records);
   const bool lv = P.trade.has_lv != 0;
@@ -686,6 +881,21 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
 #undef RG_LAUNCH
 #undef RG_LAUNCH_R
   cuda_check(cudaGetLastError(), "phoenix32_kernel launch");
+}
+
+int p32_phase_clocks(unsigned long long out[4], bool reset) {
+#ifdef RG_PHASE_CLOCKS
+  cuda_check(cudaMemcpyFromSymbol(out, g_p32_phase_clocks, sizeof(unsigned long long) * 4), "phase clocks");
+  if (reset) {
+    const unsigned long long zero[4] = {0, 0, 0, 0};
+    cuda_check(cudaMemcpyToSymbol(g_p32_phase_clocks, zero, sizeof zero), "phase clocks");
+  }
+  return 1;
+#else
+  (void)out;
+  (void)reset;
+  return 0;
+#endif
 }
 
 }  // namespace rg

@@ -18,10 +18,10 @@
 //   * the correlation with the scenario's Cholesky factor, the log-space GBM / Dupire step and the
 //     Phoenix state machine.
 // Every operation of the per-path arithmetic is the one phoenix32.cu performs, in the same order,
-// so a path's FP32 payoff values are identical in both kernels.  The 32 paths of a warp are summed
-// by the same FP32 shuffle butterfly; above that, lane k of each warp keeps an FP64 running sum of
-// quantity k over the warp's path groups, and each CTA adds its warps' sums in warp order, so a
-// launch of a given shape is bit-reproducible.
+// so a path's FP32 payoff values are identical in both kernels.  The 32 paths of a warp are one
+// chunk of the sums, added by the same FP32 shuffle butterfly and written as FP64 to
+// partial[chunk][scenario] as the tiled kernel writes them, so both kernels — and every launch
+// shape of either — give the same sums.
 #include "p32_path.cuh"
 #include "rg_internal.h"
 
@@ -29,22 +29,6 @@ namespace rg {
 
 #define P32D_THREADS 256
 #define P32D_WARPS (P32D_THREADS / 32)
-
-// Sobol integers x(n1 + lane) of one QMC dimension (direction numbers `row`) for the 32 lanes.
-__device__ __forceinline__ uint32_t warp_sobol(const uint32_t* __restrict__ row, uint64_t n1, int lane) {
-  const uint32_t g = (uint32_t)(n1 ^ (n1 >> 1));
-  uint32_t v = ((g >> lane) & 1u) ? __ldg(row + lane) : 0u;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, off);
-  // lanes past the request's last point may reach n = 2^32 (ctz 32); their values are never used
-  uint32_t d = lane == 0 ? v : __ldg(row + ((__ffsll((long long)(n1 + (uint64_t)lane)) - 1) & 31));
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, d, off);
-    if (lane >= off) d ^= t;
-  }
-  return d;
-}
 
 // Up to three assets the state fits 64 registers (four CTAs per SM, measured 2.3% faster on three
 // assets); four or five assets keep 80 registers at three CTAs per SM (four spilled, 12% slower).
@@ -55,7 +39,6 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     uint64_t npaths, double* __restrict__ partial, int32_t* __restrict__ ko_steps,
     rg_path_record* __restrict__ records) {
   __shared__ float4 s_lv[32 * RG_NMAX];
-  __shared__ double s_acc[P32D_WARPS][RG_ACC];
   extern __shared__ float s_stk[];  // [stack depth][N][P32D_THREADS]
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
   const int T = (int)tr.steps;
@@ -91,7 +74,6 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
   const float4* lvc = s_lv + s * N;
   __syncthreads();
 
-  double lane_sum = 0.0;  // lane k < RG_ACC: this warp's FP64 sum of quantity k
   const uint64_t groups = (npaths + 31) / 32;
   for (uint64_t grp = (uint64_t)(gw / S); grp < groups; grp += (uint64_t)(nw / S)) {
     const uint64_t gi = grp * 32 + lane;
@@ -116,7 +98,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
         if (tr.vr == RG_VR_SOBOL) {
 #pragma unroll
           for (int f = 0; f < N; ++f) {
-            const uint32_t xs = warp_sobol(tb.sobol + 32 * (size_t)__ldg(tb.nf_row + c * N + f), n1, lane);
+            const uint32_t xs = rg_warp_sobol(tb.sobol + 32 * (size_t)__ldg(tb.nf_row + c * N + f), n1, lane);
             zf[f] = rg_probit32(tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT
                                     ? xs ^ __ldg(tb.nf_shift + c * N + f)
                                     : rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed));
@@ -178,7 +160,8 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     float out[RG_ACC];
     p32_close_path<REC>(tr, tb, s, T, ok, s == 0, path0, gi, ph.ko_step, worst, ln_ki, ph.cpv, ph.mpv,
                         ph.received, ph.qualified, ph.paid, ko_steps, records, out);
-    // the same FP32 butterfly over the warp's 32 paths as phoenix32.cu, then lane k keeps quantity k
+    // the same FP32 butterfly over the warp's 32 paths (one chunk) as phoenix32.cu, then lane k
+    // writes the chunk's quantity k as FP64 to partial[chunk][scenario]
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
@@ -186,17 +169,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     float mine = 0.0f;
 #pragma unroll
     for (int k = 0; k < RG_ACC; ++k) mine = lane == k ? out[k] : mine;
-    lane_sum += (double)mine;
-  }
-  if (lane < RG_ACC) s_acc[wib][lane] = lane_sum;
-  __syncthreads();
-  // this CTA's sums per scenario, its warps added in warp order
-  for (int j = tid; j < S * RG_ACC; j += blockDim.x) {
-    const int ss = j / RG_ACC, k = j % RG_ACC;
-    double v = 0.0;
-    for (int w = 0; w < P32D_WARPS; ++w)
-      if ((blockIdx.x * P32D_WARPS + w) % S == ss) v += s_acc[w][k];
-    partial[(size_t)blockIdx.x * S * RG_ACC + j] = v;
+    if (lane < RG_ACC) partial[((size_t)grp * S + s) * RG_ACC + lane] = (double)mine;
   }
 }
 

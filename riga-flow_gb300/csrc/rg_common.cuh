@@ -135,6 +135,25 @@ __device__ __forceinline__ uint32_t rg_sobol_gray(const uint32_t* __restrict__ r
   return x;
 }
 
+// Sobol integers x(n1 + lane) of one QMC dimension (direction numbers `row`) for the 32 lanes of a
+// warp: x(n1) is the XOR of the direction numbers at the set bits of n1's Gray code (lane k
+// contributes bit k, a shuffle reduction), and x(n1 + lane) follows by the Gray recurrence
+// x(n) = x(n-1) ^ v[ctz(n)] as an inclusive XOR scan over the lanes.  All 32 lanes must call it.
+__device__ __forceinline__ uint32_t rg_warp_sobol(const uint32_t* __restrict__ row, uint64_t n1, int lane) {
+  const uint32_t g = (uint32_t)(n1 ^ (n1 >> 1));
+  uint32_t v = ((g >> lane) & 1u) ? __ldg(row + lane) : 0u;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, off);
+  // lanes past the request's last point may reach n = 2^32 (ctz 32); their values are never used
+  uint32_t d = lane == 0 ? v : __ldg(row + ((__ffsll((long long)(n1 + (uint64_t)lane)) - 1) & 31));
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, d, off);
+    if (lane >= off) d ^= t;
+  }
+  return d;
+}
+
 // ------------------------------------------------------------------ inverse normal ------------
 // Acklam's rational approximation (qmc.rs:37-91), FP64, reference operation order.
 __device__ __forceinline__ double rg_probit64(double p) {

@@ -221,7 +221,7 @@ void launch_lvrows(const double* lv_v, const int32_t* surf_cell_off, const int32
                    cudaStream_t s);
 
 struct LaunchOut {
-  double* partial;      // [grid][n_scen][RG_ACC]
+  double* partial;      // [grid][n_scen][RG_ACC] (FP64 kernel), [32-path chunk][n_scen][RG_ACC] (FP32)
   int32_t* ko_steps;    // [npaths] (scenario 0) or null
   rg_path_record* records;  // [npaths] or null
   int grid;
@@ -235,7 +235,8 @@ void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario*
                       uint64_t path0, uint64_t npaths, const LaunchOut& out, cudaStream_t s);
 struct Fp32Shape {
   int Sb, Pb, TT, threads, grid, smem;
-  int tuned;   // 1: TT came from the autotuner's cache
+  int ppt;     // paths per thread of the tiled kernel (1 or 2)
+  int tuned;   // 1: ppt and TT came from the autotuner's cache (or were forced)
   int direct;  // 1: the per-thread kernel of phoenix32d.cu; then only grid and threads are used
 };
 // Scenario counts up to this value run on the direct kernel (phoenix32d.cu), when the launch has
@@ -250,6 +251,8 @@ int phoenix32d_grid(const Prepared& P, uint64_t npaths, int sm_count);
 void launch_phoenix32d(const Prepared& P, const DevTables& tb, const DevScenario* scen, const DevScen32* scen32,
                        uint64_t path0, uint64_t npaths, int grid, const LaunchOut& out, cudaStream_t st);
 Fp32Shape phoenix32_shape(const Prepared& P, uint64_t npaths, int sm_count);
+// Rows of the FP32 kernels' partial sums partial[chunk][scenario][RG_ACC]: one per 32 paths.
+uint64_t p32_chunks(uint64_t npaths);
 // The level-ordered evaluation plans of the streamed Brownian bridge for every tile depth the tiled
 // FP32 kernel may launch with (its formula depth and the autotuner's candidates): packed words,
 // and per depth its value and word offset.
@@ -267,6 +270,9 @@ std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P);
 // changes the schedule, never the arithmetic) and caches the fastest.  Returns `sh` with TT set.
 // Enables or disables the autotuner process-wide; either way its cache is cleared.
 void p32_set_autotune(bool enabled);
+void p32_force_shape(int ppt, int tt);
+// Phase clocks of the tiled FP32 kernel (a build option); 0 when the build has none.
+int p32_phase_clocks(unsigned long long out[4], bool reset);
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
                          const LaunchOut& out, bool may_tune, cudaStream_t st);

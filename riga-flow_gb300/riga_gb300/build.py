@@ -21,6 +21,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr",
           "-Xptxas", "-warn-spills"]
 NO_FMA = {"phoenix64.cu", "prologue.cu", "book64.cu", "mclane.cu"}
+# RG_PHASE_CLOCKS=1 builds the tiled FP32 kernel with per-phase clock counters (rg_phase_clocks)
+PHASE_CLOCKS = os.environ.get("RG_PHASE_CLOCKS", "0") not in ("", "0")
 
 
 def nvcc() -> str:
@@ -39,6 +41,7 @@ def _stamp(srcs) -> str:
     for p in srcs + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [
             ROOT_DIR.parent / "include" / "riga_gb300.h", Path(__file__)]:
         parts.append(f"{p.name}:{p.stat().st_mtime_ns}:{p.stat().st_size}")
+    parts.append(f"phase_clocks:{int(PHASE_CLOCKS)}")
     return "\n".join(parts)
 
 
@@ -56,6 +59,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         flags = list(COMMON)
         if src.name in NO_FMA:
             flags += ["-fmad=false"]
+        if PHASE_CLOCKS:
+            flags += ["-DRG_PHASE_CLOCKS"]
         cmd = [cc, *ARCH, *flags, "-I", str(CSRC), "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

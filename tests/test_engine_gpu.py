@@ -267,8 +267,8 @@ def test_fp32_time_tiles_at_awkward_step_counts(engine, steps, n_scen):
 def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv, owen):
     """A single scenario at 2^18 paths runs on the direct kernel (one path per thread); the same
     scenario twice runs on the tiled kernel.  Both compute every path's FP32 payoff with the same
-    operations in the same order and sum warps of 32 paths by the same butterfly, so the prices
-    agree to FP64 summation order (1e-12 relative)."""
+    operations in the same order, sum each 32-path chunk by the same butterfly and reduce the chunks
+    in chunk order, so the prices are identical to the last bit."""
     if lv:
         r = workloads.lv5_large(paths=1 << 18, steps=252) if n == 5 else workloads.lv3(paths=1 << 18, steps=252)
     else:
@@ -286,16 +286,17 @@ def test_direct_and_tiled_fp32_kernels_agree(engine, n, lv, owen):
     assert engine.last_timing().smem_bytes < 64 * 1024 and engine.last_timing().block == 256
     base = (copy.deepcopy(r.market), [0.0] * n)
     two = engine.price_scenarios_raw(r, [base, base])
-    assert engine.last_timing().block == 1024
+    assert engine.last_timing().tile_steps > 0  # the tiled kernel
     for t in two:
-        assert abs(t.pv - one.pv) <= 1e-12 * abs(one.pv), (t.pv, one.pv)
-        assert t.ki_probability == one.ki_probability
+        assert (t.pv, t.mc_error, t.ki_probability, t.ko_count, t.coupon_path_count) == \
+            (one.pv, one.mc_error, one.ki_probability, one.ko_count, one.coupon_path_count)
 
 
 def test_autotuned_tile_depth_keeps_prices(engine):
-    """The step-tiling autotuner changes the tiled kernel's time-tile depth, never its arithmetic:
-    16 CRN scenarios priced with the autotuner off (the default depth), then on (the first call
-    tunes, the second reuses the tuned depth) are identical byte for byte."""
+    """The tiled kernel's autotuner changes the paths per thread and the time-tile depth, never a
+    path's arithmetic nor the 32-path chunks of the sums: 16 CRN scenarios priced with the
+    autotuner off (the formula shape), then on (the first call tunes, the second reuses the tuned
+    shape) are identical byte for byte."""
     lib = engine.lib
     r = workloads.lv3(paths=1 << 19, steps=252)
     scen = [(m, s) for _, m, s in workloads.crn15_scenarios(r)]
@@ -309,8 +310,49 @@ def test_autotuned_tile_depth_keeps_prices(engine):
     second = engine.price_scenarios_raw(r, scen)
     t_on = engine.last_timing().tile_steps
     assert t_off > 0 and t_on in (t_off, 24, 32, 48, 64, 80, 96, 128)
+    assert engine.last_timing().paths_per_thread in (1, 2)
     for a, b, c in zip(off, first, second):
         assert bytes(a) == bytes(b) == bytes(c)
+
+
+@pytest.mark.parametrize("n,lv", [(3, True), (5, True), (2, False)])
+def test_every_tiled_shape_prices_identically(engine, n, lv):
+    """Paths per thread (one, or two in packed FP32x2 arithmetic), tile depth and the resulting
+    block size are schedule only: every forced shape gives the same bytes, on a ragged path count."""
+    lib = engine.lib
+    paths = (1 << 15) + 77
+    if lv:
+        r = workloads.lv5_large(paths=paths, steps=252) if n == 5 else workloads.lv3(paths=paths, steps=252)
+    else:
+        r = workloads.plain3(paths, steps=252, fp32=True)
+        r.trade.initial_spots = [100.0] * n
+        r.market.spots = [100.0 + 3 * i for i in range(n)]
+        r.market.vols = [0.2 + 0.03 * i for i in range(n)]
+        r.market.dividend_yields = [0.01] * n
+        r.market.correlation = [[1.0 if i == j else 0.3 for j in range(n)] for i in range(n)]
+        r.config.variance_reduction = VarianceReduction("sobol", n * 252)
+    scen = []
+    for k in range(16):  # base, spot and vol bumps of each asset in turn, a rate bump
+        m = copy.deepcopy(r.market)
+        f = k % n
+        if k % 4 == 1:
+            m.spots[f] *= 1.01
+        elif k % 4 == 2:
+            m.vols[f] += 0.01
+        elif k % 4 == 3:
+            m.risk_free_rate += 1e-4
+        scen.append((m, [0.01 if (lv and k % 4 == 2 and i == f) else 0.0 for i in range(n)]))
+    got = []
+    try:
+        for ppt, tt in ((1, 24), (2, 24), (2, 48), (1, 32)):
+            abi.check(lib, lib.rg_set_tiled_shape(ppt, tt))
+            got.append(engine.price_scenarios_raw(r, scen))
+            tm = engine.last_timing()
+            assert (tm.paths_per_thread, tm.tile_steps) == (ppt, tt)
+    finally:
+        abi.check(lib, lib.rg_set_tiled_shape(0, 0))
+    for g in got[1:]:
+        assert [bytes(a) for a in g] == [bytes(a) for a in got[0]]
 
 
 def test_resident_surfaces_reproduce_the_calibration():
