@@ -38,7 +38,7 @@ namespace rg {
 // Byte offsets of the kernel's dynamic shared-memory regions, 16-byte aligned, and their total.
 // Computed by the same function on the host (to size the launch) and in the kernel (to carve).
 struct P32Layout {
-  uint32_t flags, per, thr, noff, ncf, qmc, plan, z, dw, total;
+  uint32_t flags, per, thr, noff, ncf, qmc, node4, plan, z, dw, total;
 };
 
 // Floats per row of the Z array: N·(Pb + 4) and one more, so that rows start in different banks.
@@ -67,7 +67,8 @@ __host__ __device__ inline P32Layout p32_layout(int N, int Pb, int TT, int NNmax
   // per (tile node, factor): Sobol row and digital-shift mask; per tile node: preorder index
   put(L.qmc, (uint32_t)NNmax * (uint32_t)(2 * N + 1) * 4u);
   // the tile's bridge plan: node words, level offsets, step codes, stack entries
-  put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + TT + stack_max) * 4u);
+  put(L.node4, (uint32_t)NNmax * 16u);  // per tile node in level order: Z offsets and coefficient
+  put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + (TT + 1) + stack_max) * 4u);
   put(L.z, zb);
   put(L.dw, (uint32_t)TT * (uint32_t)p32_dwstep(N, Pb, ppt) * 4u);  // dW[step][factor][path]
   L.total = o;
@@ -169,10 +170,13 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   uint32_t* s_nfrow = reinterpret_cast<uint32_t*>(smem_raw + L.qmc);  // [node][factor]
   uint32_t* s_nfsh = s_nfrow + NNmax * N;                              // [node][factor]
   uint32_t* s_nodek = s_nfsh + NNmax * N;                              // [node]
+  // node q of the tile in level order: (its Z row offset, left and right anchor row offsets, cf bits),
+  // bit 31 of the first field set for the bridge's first node (no anchors)
+  int4* s_node4 = reinterpret_cast<int4*>(smem_raw + L.node4);
   uint32_t* s_pnode = reinterpret_cast<uint32_t*>(smem_raw + L.plan);
   uint32_t* s_plev = s_pnode + NNmax;
-  uint32_t* s_pstep = s_plev + NNmax + 1;
-  uint32_t* s_pstk = s_pstep + TT;
+  int32_t* s_poff = reinterpret_cast<int32_t*>(s_plev + NNmax + 1);  // Z row offset of W at step k (k = 0: tile start)
+  uint32_t* s_pstk = reinterpret_cast<uint32_t*>(s_poff + TT + 1);
   float* Z = reinterpret_cast<float*>(smem_raw + L.z);
   float* dW = reinterpret_cast<float*>(smem_raw + L.dw);
 
@@ -262,9 +266,15 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       {
         const uint32_t node_base = __ldg(hd), lev_base = __ldg(hd + 1), stk_base = __ldg(hd + 3),
                        steps_base = __ldg(hd + 5);
-        for (int i = tid; i < nn; i += blockDim.x) s_pnode[i] = __ldg(plan + node_base + i);
+        for (int i = tid; i < nn; i += blockDim.x) {
+          const uint32_t e = __ldg(plan + node_base + i);
+          s_pnode[i] = e;
+          s_node4[i] = make_int4((int)(e & 511u) * zs | (int)((e >> 27) << 31), (int)((e >> 9) & 511u) * zs,
+                                 (int)((e >> 18) & 511u) * zs, __float_as_int(__ldg(tb.node_cf + n0 + (e & 511u))));
+        }
         for (int i = tid; i <= (int)nlev; i += blockDim.x) s_plev[i] = __ldg(plan + lev_base + i);
-        for (int i = tid; i < tn; i += blockDim.x) s_pstep[i] = __ldg(plan + steps_base + t0 + i);
+        for (int i = tid; i <= tn; i += blockDim.x)
+          s_poff[i] = i == 0 ? NNmax * zs : (int)__ldg(plan + steps_base + t0 + i - 1) * zs;
         for (int i = tid; i < (int)stk_cnt; i += blockDim.x) s_pstk[i] = __ldg(plan + stk_base + i);
       }
       {
@@ -321,53 +331,64 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       RG_PHASE_MARK(0);
       // ---- B: the tile's bridge nodes level by level from the plan (every node after its
       // anchors), W = z·c + (W_left + W_right) / 2 on the streamed bridge's anchors — so the
-      // values are its values — each written over its normal in Z.  Warp w takes chain groups
-      // (factor, 32-path group) w, w + nwarp, ...; a lane owns one chain (one column of Z), so it
-      // needs no synchronisation with other lanes, and the nodes of one level, which never read
-      // each other, are loaded kB at a time before any of them is stored.  Then the chain's dW of
-      // every step, and the state it carries to the next tile (the value at the tile end, the
-      // stack entries pushed in the tile).
-      for (int cg = wid; cg < ncg; cg += nwarp) {
-        const int c = (cg >> lg_ngrp) * (Pb + 4) + ((cg & (ngrp - 1)) << 5) + lane;
-        constexpr int kB = 8;
-        for (uint32_t lv = 0; lv < nlev; ++lv) {
-          const int a = (int)s_plev[lv], b = (int)s_plev[lv + 1];
-          for (int q = a; q < b; q += kB) {
-            // straight-line batch: surplus slots recompute the level's last node (same value)
-            float val[kB];
-            int row[kB];
+      // values are its values — each written over its normal in Z.  A chain (factor, path) is one
+      // column of Z served by two lanes of one warp (16 chains a warp): each takes every other node
+      // of a level, kB at a time loaded before any is stored (a level's nodes never read each
+      // other), with a warp barrier between levels.  Then the chain's dW of every step (the two
+      // lanes alternate steps), and the state it carries to the next tile (the value at the tile
+      // end, the stack entries pushed in the tile).
+      {
+        constexpr int kB = 4;
+        const int slot = lane >> 4;
+        const int nch = N * Pb;  // chains
+        for (int cb = wid * 16; cb < nch; cb += nwarp * 16) {
+          const int ch = cb + (lane & 15);
+          const bool chain_on = ch < nch;
+          const int c = chain_on ? (ch >> lg_pb) * (Pb + 4) + (ch & (Pb - 1)) : 0;
+          for (uint32_t lv = 0; lv < nlev; ++lv) {
+            const int a = (int)s_plev[lv], b = (int)s_plev[lv + 1];
+            for (int q = a + slot; q < b; q += 2 * kB) {
+              float val[kB];
+              int dst[kB];
+#pragma unroll
+              for (int u = 0; u < kB; ++u) {
+                // surplus slots recompute the lane's last node of the level (the same value)
+                const int qq = min(q + 2 * u, q + 2 * ((b - 1 - q) >> 1));
+                const int4 nd = s_node4[qq];
+                dst[u] = (nd.x & 0x7fffffff) + c;
+                const float z = Z[dst[u]], cf = __int_as_float(nd.w);
+                const float l = Z[nd.y + c], r = Z[nd.z + c];
+                val[u] = nd.x < 0 ? z * cf : fmaf(z, cf, 0.5f * (l + r));
+              }
+              if (chain_on)
+#pragma unroll
+                for (int u = 0; u < kB; ++u) Z[dst[u]] = val[u];
+            }
+            __syncwarp();
+          }
+          float* dwc = dW + ch;
+          for (int t1 = slot; t1 < tn; t1 += 2 * kB) {
+            float dv[kB];
+            int tt[kB];
 #pragma unroll
             for (int u = 0; u < kB; ++u) {
-              const uint32_t e = s_pnode[min(q + u, b - 1)];
-              const float cf = s_ncf[e & 511u];
-              row[u] = (int)(e & 511u) * zs + c;
-              const float z = Z[row[u]];
-              const float l = Z[(int)((e >> 9) & 511u) * zs + c], r = Z[(int)((e >> 18) & 511u) * zs + c];
-              val[u] = (e >> 27) ? z * cf : fmaf(z, cf, 0.5f * (l + r));
+              tt[u] = min(t1 + 2 * u, t1 + 2 * ((tn - 1 - t1) >> 1));
+              dv[u] = Z[s_poff[tt[u] + 1] + c] - Z[s_poff[tt[u]] + c];
             }
+            if (chain_on)
 #pragma unroll
-            for (int u = 0; u < kB; ++u) Z[row[u]] = val[u];
+              for (int u = 0; u < kB; ++u) dwc[tt[u] * dws] = dv[u];
+          }
+          __syncwarp();
+          if (chain_on && slot == 0) {
+            const float wend = Z[s_poff[tn] + c];  // the value at the tile end
+            for (uint32_t k = 0; k < stk_cnt; ++k) {
+              const uint32_t e = s_pstk[k];  // (destination row, tile node)
+              Z[(int)(e >> 9) * zs + c] = Z[(int)(e & 511u) * zs + c];
+            }
+            Z[NNmax * zs + c] = wend;
           }
         }
-        float* dwc = dW + (cg >> lg_ngrp) * Pb + ((cg & (ngrp - 1)) << 5) + lane;
-        for (int t1 = 0; t1 < tn; t1 += kB) {
-          float dv[kB];
-          int tt[kB];
-#pragma unroll
-          for (int u = 0; u < kB; ++u) {
-            tt[u] = min(t1 + u, tn - 1);
-            const int lo = tt[u] == 0 ? NNmax * zs : (int)s_pstep[tt[u] - 1] * zs;
-            dv[u] = Z[(int)s_pstep[tt[u]] * zs + c] - Z[lo + c];
-          }
-#pragma unroll
-          for (int u = 0; u < kB; ++u) dwc[tt[u] * dws] = dv[u];
-        }
-        const float wlo = Z[(int)s_pstep[tn - 1] * zs + c];  // the value at the tile end
-        for (uint32_t k = 0; k < stk_cnt; ++k) {
-          const uint32_t e = s_pstk[k];  // (destination row, tile node)
-          Z[(int)(e >> 9) * zs + c] = Z[(int)(e & 511u) * zs + c];
-        }
-        Z[NNmax * zs + c] = wlo;  // the value at the tile end
       }
       __syncthreads();
       RG_PHASE_MARK(1);
