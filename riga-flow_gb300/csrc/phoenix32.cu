@@ -394,11 +394,14 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       RG_PHASE_MARK(1);
       // ---- S: scenario stepping.  Every thread of a warp with a scenario runs it (threads of
       // padded slots and paths past the request with their Phoenix state dead), so the
-      // knock-out test can vote warp-wide.
+      // knock-out test can vote warp-wide.  Steps go in pairs: the Euler steps of both, then the
+      // Phoenix machine of both in order, so that the second step's local-vol lookups overlap the
+      // first step's barrier tests and one vote serves two steps.
       if (warp_on) {
-        for (int tt = 0; tt < tn; ++tt) {
-          const int t = t0 + tt;
-          const int tg = t * gx;
+        // one Euler step of every asset (correlated increment, local-vol lookup, log-space update);
+        // returns the worst-of log performance of each path after the step
+        auto euler = [&](int tt, float (&wmin)[PPT]) {
+          const int tg = (t0 + tt) * gx;
           V d[N], y[N];
 #pragma unroll
           for (int f = 0; f < N; ++f) {
@@ -414,7 +417,6 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
             for (int b = 1; b <= a; ++b) acc_y = V::fma(Lf[q++], d[b], acc_y);
             y[a] = acc_y;
           }
-          float wmin[PPT];
 #pragma unroll
           for (int j = 0; j < PPT; ++j) wmin[j] = INFINITY;
 #pragma unroll
@@ -443,13 +445,13 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
 #pragma unroll
             for (int j = 0; j < PPT; ++j) wmin[j] = fminf(wmin[j], x[f].v[j]);
           }
-#pragma unroll
-          for (int j = 0; j < PPT; ++j) worst[j] = wmin[j];
-          // Phoenix state machine (note.rs:150-218).  Steps that reset or close a coupon period
-          // (two in a period) take the full machine; on every other step a live path accrues and
-          // tests the knock-out branch-free against the step's thresholds (+inf where the step
-          // does not accrue or cannot call), and the knock-out branch runs when some path of the
-          // warp knocks out.
+        };
+        // Phoenix state machine (note.rs:150-218) of one step in full: steps that reset or close a
+        // coupon period take p32_phoenix_step; on the others a live path accrues and tests the
+        // knock-out branch-free against the step's thresholds (+inf where the step does not accrue
+        // or cannot call), and the knock-out branch runs when some path of the warp knocks out
+        auto phoenix = [&](int tt, const float (&wmin)[PPT]) {
+          const int t = t0 + tt;
           const uint32_t fl = s_flags[tt];
           if (fl & (STEP_PERIOD_RESET | STEP_PERIOD_END)) {
 #pragma unroll
@@ -474,6 +476,44 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
                 if (hit[j]) p32_knock_out<REC>(ph[j], fl, t, tr, tb, dfs, s_per[tt]);
             }
           }
+        };
+        int tt = 0;
+        for (; tt + 1 < tn; tt += 2) {
+          float w0[PPT], w1[PPT];
+          euler(tt, w0);
+          euler(tt + 1, w1);
+#pragma unroll
+          for (int j = 0; j < PPT; ++j) worst[j] = w1[j];
+          const uint32_t f0 = s_flags[tt], f1 = s_flags[tt + 1];
+          if ((f0 | f1) & (STEP_PERIOD_RESET | STEP_PERIOD_END)) {
+            phoenix(tt, w0);
+            phoenix(tt + 1, w1);
+          } else {
+            // two plain steps: when no path of the warp knocks out in either, both only accrue
+            const float2 th0 = s_thr[tt], th1 = s_thr[tt + 1];
+            bool any = false;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) any |= ph[j].alive & ((w0[j] >= th0.y) | (w1[j] >= th1.y));
+            if (__any_sync(0xffffffffu, any)) {
+              phoenix(tt, w0);
+              phoenix(tt + 1, w1);
+            } else {
+#pragma unroll
+              for (int j = 0; j < PPT; ++j) {
+                const bool a = ph[j].alive;
+                const int acc = (int)(a & (w0[j] >= th0.x)) + (int)(a & (w1[j] >= th1.x));
+                ph[j].qual += acc;
+                if (REC) ph[j].qualified += acc;
+              }
+            }
+          }
+        }
+        if (tt < tn) {
+          float w0[PPT];
+          euler(tt, w0);
+#pragma unroll
+          for (int j = 0; j < PPT; ++j) worst[j] = w0[j];
+          phoenix(tt, w0);
         }
       }
       __syncthreads();
