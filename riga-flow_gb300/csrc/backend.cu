@@ -8,29 +8,43 @@
 
 namespace rg {
 
-// partial[grid][S][RG_ACC] -> out[S][RG_ACC].  One CTA per scenario; each thread adds a strided
-// subset of the blocks in order with Neumaier compensation, then a pairwise tree in shared
-// memory.  The order depends only on `grid`, so repeated launches are bit-identical.
-__global__ void reduce_kernel(const double* __restrict__ partial, int grid, int S, double* __restrict__ out) {
-  __shared__ double sh[256];
+// partial[rows][S][RG_ACC] -> out[S][RG_ACC].  One CTA per scenario; thread i adds rows i, i + 256,
+// ... in order with Neumaier compensation, all RG_ACC quantities of a row at once (one 128-byte
+// line), then a pairwise tree over the threads in shared memory.  The order depends only on the
+// row count, so repeated launches — and every launch shape of the kernels that wrote the rows —
+// give the same bits.
+__global__ void __launch_bounds__(256) reduce_kernel(const double* __restrict__ partial, int rows, int S,
+                                                     double* __restrict__ out) {
+  __shared__ double sh[RG_ACC][256];
   const int s = blockIdx.x, tid = threadIdx.x;
-  for (int k = 0; k < RG_ACC; ++k) {
-    double sum = 0.0, comp = 0.0;
-    for (int b = tid; b < grid; b += blockDim.x) {
-      double v = partial[((size_t)b * S + s) * RG_ACC + k];
-      double t = sum + v;
-      comp += fabs(sum) >= fabs(v) ? (sum - t) + v : (v - t) + sum;
-      sum = t;
+  double sum[RG_ACC], comp[RG_ACC];
+#pragma unroll
+  for (int k = 0; k < RG_ACC; ++k) sum[k] = comp[k] = 0.0;
+  for (int b = tid; b < rows; b += blockDim.x) {
+    const double2* row = reinterpret_cast<const double2*>(partial + ((size_t)b * S + s) * RG_ACC);
+#pragma unroll
+    for (int k2 = 0; k2 < RG_ACC / 2; ++k2) {
+      const double2 v2 = __ldg(row + k2);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = 2 * k2 + h;
+        const double v = h ? v2.y : v2.x;
+        const double t = sum[k] + v;
+        comp[k] += fabs(sum[k]) >= fabs(v) ? (sum[k] - t) + v : (v - t) + sum[k];
+        sum[k] = t;
+      }
     }
-    sh[tid] = sum + comp;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (tid < w) sh[tid] += sh[tid + w];
-      __syncthreads();
-    }
-    if (tid == 0) out[(size_t)s * RG_ACC + k] = sh[0];
+  }
+#pragma unroll
+  for (int k = 0; k < RG_ACC; ++k) sh[k][tid] = sum[k] + comp[k];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (tid < w)
+#pragma unroll
+      for (int k = 0; k < RG_ACC; ++k) sh[k][tid] += sh[k][tid + w];
     __syncthreads();
   }
+  if (tid < RG_ACC) out[(size_t)s * RG_ACC + tid] = sh[tid][0];
 }
 
 void launch_reduce(const double* partial, int grid, int S, double* out, cudaStream_t st) {
