@@ -171,51 +171,72 @@ def run_reference(args):
 # ----------------------------------------------------------------------------- book (cfg 2) --
 def book_measure(eng, n_trades: int, paths: int):
     """The book configuration in one call: `n_trades` trades of the 20-asset universe at `paths`
-    Sobol paths under the book's 16 common scenarios, FP32, host inputs (rg_price_book)."""
+    Sobol paths, every trade under its own 16 scenarios (base + 15 bumps on its own underlyings),
+    FP32, host inputs (rg_price_book_trade_bumps); then the same book resident (graph replay)."""
     import torch
-    from riga_gb300 import workloads
+    from riga_gb300 import abi, workloads
 
+    S = abi.BOOK_TRADE_SCENARIOS
     b = workloads.book(paths=paths, n_trades=n_trades, fp32=True)
-    sc = [m for _, m in workloads.book_scenarios(b.universe)]
     warm = copy.deepcopy(b)
     warm.config.paths = 1 << 12
-    eng.price_book_raw(warm, sc)
+    eng.price_book_trade_bumps_raw(warm)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    eng.price_book_raw(b, sc)
+    eng.price_book_trade_bumps_raw(b)
     wall = time.perf_counter() - t0
-    units = float(sum(t.terms.steps for t in b.trades)) * paths * len(sc)
-    # accuracy: FP32 against the FP64 book on the same points, first 16 trades at 2^14 paths
-    sub32 = workloads.book(paths=1 << 14, n_trades=16, fp32=True)
-    sub64 = workloads.book(paths=1 << 14, n_trades=16, fp32=False)
-    r32 = eng.price_book_raw(sub32, sc)
-    r64 = eng.price_book_raw(sub64, sc)
-    errs = [abs(a.pv - w.pv) for a, w in zip(r32, r64)]
-    within = all(abs(a.pv - w.pv) <= min(0.1 * w.mc_error, 1e-4) for a, w in zip(r32, r64))
+    units = float(sum(t.terms.steps for t in b.trades)) * paths * S
+    # accuracy at the book's path count: FP32 against the FP64 book on the same points, a seeded
+    # sample of 64 trades of the book distribution (1-5 underlyings), every price and every bump
+    # difference (bumped minus base) within min(0.1 SE, 1bp)
+    t_acc = time.perf_counter()
+    sample = workloads.book(paths=paths, n_trades=64, fp32=True, seed=11)
+    r32 = eng.price_book_trade_bumps_raw(sample)
+    r64 = eng.price_book_trade_bumps_raw(workloads.book(paths=paths, n_trades=64, fp32=False, seed=11))
+    acc_s = time.perf_counter() - t_acc
+    err_p = err_d = 0.0
+    within = True
+    for j in range(64):
+        b32, b64 = r32[j * S], r64[j * S]
+        for k in range(S):
+            a, w = r32[j * S + k], r64[j * S + k]
+            bound = min(0.1 * w.mc_error, 1e-4)
+            e = abs(a.pv - w.pv)
+            d = abs((a.pv - b32.pv) - (w.pv - b64.pv))
+            err_p, err_d = max(err_p, e), max(err_d, d)
+            within = within and e <= bound and d <= bound
+    counts = [0] * 5
+    for t in sample.trades:
+        counts[len(t.underlyings) - 1] += 1
     # the same book resident on the device: created once (increments generated), the first price
-    # tunes and captures, the second replays the graph under the same scenarios
+    # tunes and captures, the second replays the graph
     t0 = time.perf_counter()
     rb = eng.resident_book(b)
     create_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    rb.price_raw(sc)
+    rb.price_trade_bumps_raw()
     first_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    rb.price_raw(sc)
+    rb.price_trade_bumps_raw()
     replay_s = time.perf_counter() - t0
-    stage = rb.tuned_stage(len(sc))
+    stage = rb.tuned_stage(1000 + S)
     rb.close()
     return {"workload": f"book: {n_trades} Phoenix trades (1-5 underlyings, 1-5y) on a 20-asset 4-factor "
-                        f"universe, one universe path set on 1260 daily steps, {paths} Sobol paths, "
-                        f"{len(sc)} common CRN scenarios, one rg_price_book call with host inputs",
-            "trades": n_trades, "paths": paths, "scenarios": len(sc), "wall_s": wall,
-            "path_steps_per_s": units / wall, "trades_bumps_per_s": n_trades * len(sc) / wall,
-            "accuracy": {"max_abs_err_vs_fp64": max(errs), "within_min_0.1se_1bp": within,
-                         "sample": "first 16 trades, 2^14 paths, 16 scenarios"},
+                        f"universe, one universe path set on 1260 daily steps, {paths} Sobol paths, every "
+                        f"trade under {S} scenarios of its own (base + 15 bumps on its own underlyings: spot "
+                        f"+-1%, vol +1pt, rate +1bp, cross-gamma corners, ...), one rg_price_book_trade_bumps "
+                        f"call with host inputs",
+            "trades": n_trades, "paths": paths, "scenarios_per_trade": S, "wall_s": wall,
+            "path_steps_per_s": units / wall, "trades_bumps_per_s": n_trades * S / wall,
+            "accuracy": {"max_abs_err_price": err_p, "max_abs_err_bump_difference": err_d,
+                         "within_min_0.1se_1bp": within, "fp64_and_fp32_s": acc_s,
+                         "sample": f"64 trades (seed 11; by underlying count 1-5: {counts}), {paths} paths, "
+                                   f"{S} per-trade scenarios, every price and every bump difference"},
             "resident": {"create_s": create_s, "first_price_s": first_s, "replay_s": replay_s,
-                         "path_steps_per_s": units / replay_s, "trades_bumps_per_s": n_trades * len(sc) / replay_s,
+                         "path_steps_per_s": units / replay_s, "trades_bumps_per_s": n_trades * S / replay_s,
                          "tuned_steps_per_stage": stage,
-                         "note": "rg_book_create once, then rg_book_price: CUDA-graph replay, increments resident"}}
+                         "note": "rg_book_create once, then rg_book_price_trade_bumps: CUDA-graph replay, "
+                                 "increments resident"}}
 
 
 def fp64_plain_rate(eng):

@@ -413,6 +413,39 @@ int32_t rg_price_book(rg_engine* engine, const rg_book_request* request,
                       const rg_market_snapshot* scenarios, int32_t n_scenarios,
                       rg_price_result* out);
 
+/* Per-trade bump sets (this scenario layout has no single counterpart in the reference, which bumps
+ * one trade's own underlyings per risk call: crates/riga-risk/src/lib.rs:117-186, 573-626, and the
+ * cross-gamma corners of crates/riga-mcp/src/main.rs:1366-1393).  Every trade of a book is priced
+ * under RG_BOOK_TRADE_SCENARIOS scenarios on its own underlyings, all on the same universe paths:
+ * scenario 0 is the base market and scenarios 1..15 are bumps, taken in this order until there are
+ * 15 (h = spot_relative, v = vol_absolute, r = rate_absolute; underlying positions within the
+ * trade, pairs in the order (0,1), (0,2), (1,2), (0,3), (1,3), (2,3), (0,4), ...):
+ *   spot ×(1 + h) and ×(1 - h) of each underlying; vol + v of each underlying; rate + r;
+ *   spot ×(1 + h) of both underlyings of each pair (cross-gamma corner); vol - v of each underlying;
+ *   rate - r; spot ×(1 - h) of both of each pair; spot ×(1 ± 2h), ×(1 ± 5h), ×(1 ± 10h) of each
+ *   underlying; vol ± 2v of each underlying; rate ± 2r.
+ * So a 5-underlying trade gets spot ± and vol + of every underlying, a 3-underlying trade also the
+ * rate, the three ++ corners, and vol - of two underlyings.  Vols are floored at 0. */
+#define RG_BOOK_TRADE_SCENARIOS 16
+typedef struct rg_book_bumps {
+  double spot_relative; /* 0 = 0.01 */
+  double vol_absolute;  /* 0 = 0.01 */
+  double rate_absolute; /* 0 = 1e-4 */
+} rg_book_bumps;
+enum { RG_BUMP_BASE = 0, RG_BUMP_SPOT = 1, RG_BUMP_VOL = 2, RG_BUMP_RATE = 3, RG_BUMP_SPOT_PAIR = 4 };
+typedef struct rg_book_bump_spec {
+  int32_t kind;          /* RG_BUMP_* */
+  int32_t first, second; /* underlying positions within the trade (-1 when unused) */
+  double size;           /* relative spot move, absolute vol or rate move (signed) */
+} rg_book_bump_spec;
+/* The bump of scenario `scenario` (0..15) of a trade with n_underlyings underlyings. */
+int32_t rg_book_trade_bump(int32_t n_underlyings, int32_t scenario, const rg_book_bumps* sizes,
+                           rg_book_bump_spec* out);
+/* Prices every trade of the book under its own 16 scenarios: out[j * 16 + k] is trade j under its
+ * scenario k.  sizes NULL = the defaults. */
+int32_t rg_price_book_trade_bumps(rg_engine* engine, const rg_book_request* request,
+                                  const rg_book_bumps* sizes, rg_price_result* out);
+
 /* Per-path records of book paths [first_path, first_path + count) for every (trade, scenario):
  * out[(p * n_trades + j) * S + s] (explain.rs:90-316 applied to each trade of the book). */
 int32_t rg_book_run_paths(rg_engine* engine, const rg_book_request* request,
@@ -432,6 +465,8 @@ typedef struct rg_book rg_book;
 int32_t rg_book_create(rg_engine* engine, const rg_book_request* request, rg_book** out);
 int32_t rg_book_price(rg_book* book, const rg_market_snapshot* scenarios, int32_t n_scenarios,
                       rg_price_result* out);
+/* The resident book under per-trade bump sets (rg_price_book_trade_bumps): out[j * 16 + k]. */
+int32_t rg_book_price_trade_bumps(rg_book* book, const rg_book_bumps* sizes, rg_price_result* out);
 /* The stage depth the autotuner chose for n_scenarios (0 before the first price at that count). */
 int32_t rg_book_tuned_stage(rg_book* book, int32_t n_scenarios, int32_t* steps_per_stage);
 void rg_book_destroy(rg_book* book);

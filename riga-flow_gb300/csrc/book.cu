@@ -13,13 +13,14 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 
 #include "rg_book.h"
 
 namespace rg {
 namespace bk {
 
-void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen) {
+void validate_book(const rg_book_request* r, const BookScenarios& sc) {
   if (!r) raise(RG_ERR_INVALID_ARGUMENT, "request is null");
   const rg_market_snapshot& u = r->universe;
   const int U = u.n_assets;
@@ -87,11 +88,20 @@ void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n
   for (int a = 0; a < U; ++a)
     if (!(u.spots[a] > 0.0) || !(u.vols[a] >= 0.0) || !std::isfinite(u.vols[a]) || !std::isfinite(u.dividend_yields[a]))
       raise(RG_ERR_INVALID_MARKET, "universe spots must be positive and vols non-negative");
-  validate_book_scenarios(u, sc, n_scen);
+  validate_book_scenarios(u, sc);
 }
 
-void validate_book_scenarios(const rg_market_snapshot& u, const rg_market_snapshot* sc, int n_scen) {
+void validate_book_scenarios(const rg_market_snapshot& u, const BookScenarios& spec) {
   const int U = u.n_assets;
+  if (spec.per_trade) {
+    const rg_book_bumps* b = spec.bumps;
+    if (b && (!std::isfinite(b->spot_relative) || !std::isfinite(b->vol_absolute) || !std::isfinite(b->rate_absolute) ||
+              b->spot_relative < 0.0 || b->spot_relative >= 0.1 || b->vol_absolute < 0.0 || b->rate_absolute < 0.0))
+      raise(RG_ERR_INVALID_ARGUMENT, "bump sizes must be finite and non-negative, the spot move below 10%");
+    return;
+  }
+  const rg_market_snapshot* sc = spec.sc;
+  const int n_scen = spec.n;
   if (n_scen < 0 || (n_scen > 0 && !sc)) raise(RG_ERR_INVALID_ARGUMENT, "bad scenario list");
   for (int s = 0; s < n_scen; ++s) {
     if (sc[s].n_assets != U || !sc[s].spots || !sc[s].vols || !sc[s].dividend_yields)
@@ -108,7 +118,7 @@ void validate_book_scenarios(const rg_market_snapshot& u, const rg_market_snapsh
   }
 }
 
-void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B) {
+void plan_book(const rg_book_request* r, const BookScenarios& sc, BookPlan& B) {
   const rg_market_snapshot& u = r->universe;
   const rg_simulation_config& c = r->config;
   B.U = u.n_assets;
@@ -176,39 +186,147 @@ void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_sce
     const int n = B.trades[B.order[i]].n;
     if (B.group_n[n - 1]++ == 0) B.group_lo[n - 1] = i;
   }
-  plan_book_scenarios(r, sc, n_scen, B);
+  plan_book_scenarios(r, sc, B);
 }
 
-// The scenario-dependent tables: markets, discount factors, per-(trade, scenario) FP32 constants.
-void plan_book_scenarios(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B) {
-  if (n_scen == 0) {
-    sc = &r->universe;
-    n_scen = 1;
-  }
-  B.S = n_scen;
-  B.scen.resize(B.S);
-  B.df.resize((size_t)B.S * B.TU);
-  for (int s = 0; s < B.S; ++s) {
-    BookScenDev& d = B.scen[s];
-    memset(&d, 0, sizeof d);
-    d.rate = sc[s].risk_free_rate;
-    for (int a = 0; a < B.U; ++a) {
-      d.spots[a] = sc[s].spots[a];
-      d.vols[a] = sc[s].vols[a];
-      d.q[a] = sc[s].dividend_yields[a];
+rg_book_bump_spec trade_bump(int n, int k, const rg_book_bumps* sizes) {
+  const double h = sizes && sizes->spot_relative > 0.0 ? sizes->spot_relative : 0.01;
+  const double v = sizes && sizes->vol_absolute > 0.0 ? sizes->vol_absolute : 0.01;
+  const double rr = sizes && sizes->rate_absolute > 0.0 ? sizes->rate_absolute : 1e-4;
+  rg_book_bump_spec b{RG_BUMP_BASE, -1, -1, 0.0};
+  if (k == 0) return b;
+  int left = k - 1;  // position in the bump order
+  auto take = [&left](int count) {
+    if (left < count) return true;
+    left -= count;
+    return false;
+  };
+  const int npairs = n * (n - 1) / 2;
+  auto pair_of = [](int idx, int& a, int& c) {  // (0,1), (0,2), (1,2), (0,3), ...
+    for (c = 1;; ++c) {
+      if (idx < c) {
+        a = idx;
+        return;
+      }
+      idx -= c;
     }
-    // exp(-r (t+1) dt) on the universe grid (note.rs:189, 210)
-    for (int64_t t = 0; t < B.TU; ++t) B.df[(size_t)s * B.TU + t] = std::exp(-d.rate * ((double)(t + 1) * B.dt));
+  };
+  if (take(2 * n)) return {RG_BUMP_SPOT, left / 2, -1, left % 2 ? -h : h};
+  if (take(n)) return {RG_BUMP_VOL, left, -1, v};
+  if (take(1)) return {RG_BUMP_RATE, -1, -1, rr};
+  if (take(npairs)) {
+    int a, c;
+    pair_of(left, a, c);
+    return {RG_BUMP_SPOT_PAIR, a, c, h};
   }
+  if (take(n)) return {RG_BUMP_VOL, left, -1, -v};
+  if (take(1)) return {RG_BUMP_RATE, -1, -1, -rr};
+  if (take(npairs)) {
+    int a, c;
+    pair_of(left, a, c);
+    return {RG_BUMP_SPOT_PAIR, a, c, -h};
+  }
+  for (double m : {2.0, 5.0, 10.0})
+    if (take(2 * n)) return {RG_BUMP_SPOT, left / 2, -1, left % 2 ? -m * h : m * h};
+  if (take(2 * n)) return {RG_BUMP_VOL, left / 2, -1, left % 2 ? -2.0 * v : 2.0 * v};
+  if (take(2)) return {RG_BUMP_RATE, -1, -1, left ? -2.0 * rr : 2.0 * rr};
+  raise(RG_ERR_INVALID_ARGUMENT, "no such bump scenario");
+}
+
+// The scenario-dependent tables: the markets the (trade, scenario) pairs price under, discount
+// factors per distinct rate, per-pair FP32 constants.  Common scenarios are markets 0..S-1 in
+// order; per-trade bump markets are the base market with one trade's bump applied, each distinct
+// market kept once.
+void plan_book_scenarios(const rg_book_request* r, const BookScenarios& spec, BookPlan& B) {
+  const rg_market_snapshot& u = r->universe;
+  const int U = B.U;
+  B.scen.clear();
+  std::vector<int32_t> pair_mkt;
+  auto market_of = [&](const rg_market_snapshot& m) {
+    BookScenDev d;
+    memset(&d, 0, sizeof d);
+    d.rate = m.risk_free_rate;
+    for (int a = 0; a < U; ++a) {
+      d.spots[a] = m.spots[a];
+      d.vols[a] = m.vols[a];
+      d.q[a] = m.dividend_yields[a];
+    }
+    return d;
+  };
+  if (!spec.per_trade) {
+    const rg_market_snapshot* sc = spec.sc;
+    int n_scen = spec.n;
+    if (n_scen == 0) {
+      sc = &u;
+      n_scen = 1;
+    }
+    B.S = n_scen;
+    for (int s = 0; s < B.S; ++s) B.scen.push_back(market_of(sc[s]));
+    pair_mkt.resize((size_t)B.n_trades * B.S);
+    for (int j = 0; j < B.n_trades; ++j)
+      for (int s = 0; s < B.S; ++s) pair_mkt[(size_t)j * B.S + s] = s;
+  } else {
+    B.S = RG_BOOK_TRADE_SCENARIOS;
+    const BookScenDev base = market_of(u);
+    std::map<std::vector<uint8_t>, int32_t> seen;
+    pair_mkt.resize((size_t)B.n_trades * B.S);
+    for (int j = 0; j < B.n_trades; ++j) {
+      const BookTradeDev& t = B.trades[j];
+      for (int k = 0; k < B.S; ++k) {
+        const rg_book_bump_spec b = trade_bump(t.n, k, spec.bumps);
+        BookScenDev d = base;
+        switch (b.kind) {
+          case RG_BUMP_SPOT: d.spots[t.idx[b.first]] *= 1.0 + b.size; break;
+          case RG_BUMP_SPOT_PAIR:
+            d.spots[t.idx[b.first]] *= 1.0 + b.size;
+            d.spots[t.idx[b.second]] *= 1.0 + b.size;
+            break;
+          case RG_BUMP_VOL: d.vols[t.idx[b.first]] = std::max(0.0, d.vols[t.idx[b.first]] + b.size); break;
+          case RG_BUMP_RATE: d.rate += b.size; break;
+          default: break;
+        }
+        std::vector<uint8_t> key(reinterpret_cast<const uint8_t*>(&d), reinterpret_cast<const uint8_t*>(&d) + sizeof d);
+        auto it = seen.find(key);
+        int32_t m;
+        if (it == seen.end()) {
+          m = (int32_t)B.scen.size();
+          seen.emplace(std::move(key), m);
+          B.scen.push_back(d);
+        } else {
+          m = it->second;
+        }
+        pair_mkt[(size_t)j * B.S + k] = m;
+      }
+    }
+  }
+  // discount factors exp(-r (t+1) dt) on the universe grid (note.rs:189, 210), one row per
+  // distinct rate, with the platform libm's exp
+  std::vector<double> rates;
+  for (BookScenDev& d : B.scen) {
+    int row = -1;
+    for (size_t i = 0; i < rates.size(); ++i)
+      if (rates[i] == d.rate) row = (int)i;
+    if (row < 0) {
+      row = (int)rates.size();
+      rates.push_back(d.rate);
+    }
+    d.dfrow = row;
+  }
+  B.df.resize(rates.size() * (size_t)B.TU);
+  for (size_t i = 0; i < rates.size(); ++i)
+    for (int64_t t = 0; t < B.TU; ++t) B.df[i * B.TU + t] = std::exp(-rates[i] * ((double)(t + 1) * B.dt));
   B.dfm.resize((size_t)B.n_trades * B.S);
   B.pair32.resize((size_t)B.n_trades * B.S);
   for (int j = 0; j < B.n_trades; ++j)
     for (int s = 0; s < B.S; ++s) {
       const BookTradeDev& t = B.trades[j];
-      const BookScenDev& m = B.scen[s];
+      const int32_t mi = pair_mkt[(size_t)j * B.S + s];
+      const BookScenDev& m = B.scen[mi];
       B.dfm[(size_t)j * B.S + s] = std::exp(-m.rate * t.maturity);  // note.rs:221, 238 (libm)
       BookPair32& p = B.pair32[(size_t)j * B.S + s];
       memset(&p, 0, sizeof p);
+      p.mkt = mi;
+      p.dfrow = m.dfrow;
       for (int f = 0; f < t.n; ++f) {
         const int a = t.idx[f];
         const double v = m.vols[a];
@@ -389,11 +507,11 @@ static std::vector<uint8_t> universe_key_bytes(const rg_book_request* r, uint64_
   return b;
 }
 
-void run_book(rg_engine* E, const rg_book_request* r, const rg_market_snapshot* sc, int n_scen,
-              rg_price_result* out, uint64_t first, uint64_t count, rg_path_record* records) {
-  validate_book(r, sc, n_scen);
+void run_book(rg_engine* E, const rg_book_request* r, const BookScenarios& sc, rg_price_result* out,
+              uint64_t first, uint64_t count, rg_path_record* records) {
+  validate_book(r, sc);
   BookPlan B;
-  plan_book(r, sc, n_scen, B);
+  plan_book(r, sc, B);
   const int pairs = B.n_trades * B.S;
   const bool fp32 = r->config.precision == RG_PRECISION_FP32 && !records;
   BookStaged st = stage_book_static(E->book_bufs[BK_TABLES], E->stream, r, B);
@@ -518,7 +636,35 @@ extern "C" int32_t rg_price_book(rg_engine* e, const rg_book_request* request, c
     if (g) return g;
     std::lock_guard<std::mutex> lock(e->mu);
     cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
-    run_book(e, request, scenarios, n_scenarios, out, 0, 0, nullptr);
+    BookScenarios sc;
+    sc.sc = scenarios;
+    sc.n = n_scenarios;
+    run_book(e, request, sc, out, 0, 0, nullptr);
+  })
+}
+
+extern "C" int32_t rg_price_book_trade_bumps(rg_engine* e, const rg_book_request* request, const rg_book_bumps* sizes,
+                                             rg_price_result* out) {
+  RG_TRY({
+    if (!e || !request || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    int32_t g = rg_guard_device();
+    if (g) return g;
+    std::lock_guard<std::mutex> lock(e->mu);
+    cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
+    BookScenarios sc;
+    sc.bumps = sizes;
+    sc.per_trade = true;
+    run_book(e, request, sc, out, 0, 0, nullptr);
+  })
+}
+
+extern "C" int32_t rg_book_trade_bump(int32_t n_underlyings, int32_t scenario, const rg_book_bumps* sizes,
+                                      rg_book_bump_spec* out) {
+  RG_TRY({
+    if (!out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n_underlyings < 1 || n_underlyings > RG_NMAX || scenario < 0 || scenario >= RG_BOOK_TRADE_SCENARIOS)
+      raise(RG_ERR_INVALID_ARGUMENT, "1..5 underlyings and scenarios 0..15");
+    *out = bk::trade_bump(n_underlyings, scenario, sizes);
   })
 }
 
@@ -533,6 +679,9 @@ extern "C" int32_t rg_book_run_paths(rg_engine* e, const rg_book_request* reques
       raise(RG_ERR_PATH_OUT_OF_RANGE, "path range is outside the configured path count");
     std::lock_guard<std::mutex> lock(e->mu);
     cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
-    run_book(e, request, scenarios, n_scenarios, nullptr, first_path, count, out);
+    BookScenarios sc;
+    sc.sc = scenarios;
+    sc.n = n_scenarios;
+    run_book(e, request, sc, nullptr, first_path, count, out);
   })
 }

@@ -131,7 +131,7 @@ __device__ __forceinline__ bool book_scan32_tma(const BookDev& bk, const BookTra
     drift[f] = pc.drift[f];
     sig[f] = pc.sig[f];
   }
-  const float* df = bk.df_f + (size_t)ss * bk.TU;
+  const float* df = bk.df_f + (size_t)pc.dfrow * bk.TU;
   const float dfm = bk.dfm_f[(size_t)j * bk.S + ss];
   const int T = tr.T, PER = tr.periods;
   const int ntiles = (int)((p_hi - p_lo + Pb - 1) / Pb);

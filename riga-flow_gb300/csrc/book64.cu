@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(128) book_trade64_kernel(DevTrade gen, BookDev
   const int pairs = bk.n_trades * bk.S;
   const int j = pair / bk.S, s = pair % bk.S;
   const BookTradeDev& tr = bk.trades[j];
-  const BookScenDev& sc = bk.scen[s];
+  const BookPair32& pc = bk.pair32[(size_t)j * bk.S + s];
+  const BookScenDev& sc = bk.scen[pc.mkt];
   const uint64_t p = (uint64_t)blk * blockDim.x + tid;
   double out[RG_ACC];
 #pragma unroll
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(128) book_trade64_kernel(DevTrade gen, BookDev
       row[f] = incr + (uint64_t)a * npaths + p;
     }
     const uint64_t step_stride = (uint64_t)bk.U * npaths;
-    const double* df = bk.df + (size_t)s * bk.TU;
+    const double* df = bk.df + (size_t)pc.dfrow * bk.TU;
     int ko = 0, received = 0, ko_step = -1, qualified = 0, paid = 0;
     double accrual = 0.0, unpaid = 0.0, cpv = 0.0, mpv = 0.0, final_worst = 1.0;
     int64_t current = 0;

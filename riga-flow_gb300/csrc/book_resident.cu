@@ -106,20 +106,28 @@ int autotune_stage(rg_book* b, const Book32Shape& base) {
   return best;
 }
 
-void price_resident(rg_book* b, const rg_market_snapshot* sc, int n_scen, rg_price_result* out) {
+void price_resident(rg_book* b, const BookScenarios& spec, rg_price_result* out) {
   rg_engine* E = b->E;
-  validate_book_scenarios(b->universe, sc, n_scen);
+  validate_book_scenarios(b->universe, spec);
   rg_book_request view{};
   view.universe = b->universe;
-  plan_book_scenarios(&view, sc, n_scen, b->B);
+  plan_book_scenarios(&view, spec, b->B);
   const int S = b->B.S;
   if (S > 32) raise(RG_ERR_INVALID_ARGUMENT, "at most 32 scenarios per book price");
   const int pairs = b->B.n_trades * S;
   const ScenarioPack sp = pack_book_scenarios(b->B);
   const size_t scen_bytes = sp.pk.host.size();
-  GraphEntry& g = b->graphs[S];
+  // one graph per scenario count, per-trade bump sets apart; tables of another size (other bump
+  // sizes can merge or split markets) are captured again
+  GraphEntry& g = b->graphs[spec.per_trade ? 1000 + S : S];
+  if (g.exec && scen_bytes != g.scen_bytes) {
+    cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+  }
   if (!g.exec) {
     // this scenario count's buffers, then tune the stage depth, then capture
+    g.scen_dev.release();
+    g.scen_host.release();
     g.scen_dev.ensure(scen_bytes);
     g.scen_host.ensure(scen_bytes);
     memcpy(g.scen_host.ptr, sp.pk.host.data(), scen_bytes);
@@ -128,7 +136,7 @@ void price_resident(rg_book* b, const rg_market_snapshot* sc, int n_scen, rg_pri
     Book32Shape sh = book32_shape(S, device_sm_count(), b->P, b->B.min_group());
     sh.TT = autotune_stage(b, sh);
     sh.smem = 2 * 5 * sh.TT * sh.Pb * 4 + 64;
-    b->tuned[S] = sh.TT;
+    b->tuned[spec.per_trade ? 1000 + S : S] = sh.TT;
     const uint64_t blocks = (b->P + sh.blk_paths - 1) / sh.blk_paths;
     g.partial.ensure(sizeof(double) * blocks * pairs * RG_ACC);
     g.sums.ensure(sizeof(double) * pairs * RG_ACC);
@@ -190,7 +198,7 @@ extern "C" int32_t rg_book_create(rg_engine* e, const rg_book_request* request, 
     if (g) return g;
     if (request->config.precision != RG_PRECISION_FP32)
       raise(RG_ERR_UNSUPPORTED, "resident books run the FP32 production kernels (use rg_price_book for FP64 parity)");
-    bk::validate_book(request, nullptr, 0);
+    bk::validate_book(request, bk::BookScenarios{});
     std::lock_guard<std::mutex> lock(e->mu);
     cuda_check(cudaSetDevice(e->device), "cudaSetDevice");
     std::unique_ptr<rg_book> b(new rg_book());
@@ -209,7 +217,7 @@ extern "C" int32_t rg_book_create(rg_engine* e, const rg_book_request* request, 
     b->universe.dividend_yields = b->q.data();
     b->universe.correlation = b->corr.data();
     b->config = request->config;
-    bk::plan_book(request, nullptr, 0, b->B);
+    bk::plan_book(request, bk::BookScenarios{}, b->B);
     b->st = bk::stage_book_static(b->tables, e->stream, request, b->B);
     b->P = request->config.paths;
     b->rowlen = (b->P + 63) / 64 * 64;
@@ -232,7 +240,22 @@ extern "C" int32_t rg_book_price(rg_book* book, const rg_market_snapshot* scenar
     if (!book || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lock(book->E->mu);
     cuda_check(cudaSetDevice(book->E->device), "cudaSetDevice");
-    price_resident(book, scenarios, n_scenarios, out);
+    bk::BookScenarios sc;
+    sc.sc = scenarios;
+    sc.n = n_scenarios;
+    price_resident(book, sc, out);
+  })
+}
+
+extern "C" int32_t rg_book_price_trade_bumps(rg_book* book, const rg_book_bumps* sizes, rg_price_result* out) {
+  RG_TRY({
+    if (!book || !out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(book->E->mu);
+    cuda_check(cudaSetDevice(book->E->device), "cudaSetDevice");
+    bk::BookScenarios sc;
+    sc.bumps = sizes;
+    sc.per_trade = true;
+    price_resident(book, sc, out);
   })
 }
 

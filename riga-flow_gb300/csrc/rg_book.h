@@ -34,12 +34,23 @@ struct BookPlan {
   }
 };
 
+// The scenarios a book is priced under: a common list of universe markets (n = 0: the base market
+// alone), or, with `bumps`, RG_BOOK_TRADE_SCENARIOS bump scenarios on each trade's own underlyings.
+struct BookScenarios {
+  const rg_market_snapshot* sc = nullptr;
+  int n = 0;
+  const rg_book_bumps* bumps = nullptr;
+  bool per_trade = false;
+};
+// The bump of scenario k of a trade on n underlyings (the rule documented with rg_book_trade_bump).
+rg_book_bump_spec trade_bump(int n, int k, const rg_book_bumps* sizes);
+
 // Request checks (each trade with the reference's own request validation on its slice of the
 // universe) and the plan: static tables, then the scenario tables.
-void validate_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen);
-void validate_book_scenarios(const rg_market_snapshot& universe, const rg_market_snapshot* sc, int n_scen);
-void plan_book(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B);
-void plan_book_scenarios(const rg_book_request* r, const rg_market_snapshot* sc, int n_scen, BookPlan& B);
+void validate_book(const rg_book_request* r, const BookScenarios& sc);
+void validate_book_scenarios(const rg_market_snapshot& universe, const BookScenarios& sc);
+void plan_book(const rg_book_request* r, const BookScenarios& sc, BookPlan& B);
+void plan_book_scenarios(const rg_book_request* r, const BookScenarios& sc, BookPlan& B);
 
 struct BookStaged {
   DevTables tb{};

@@ -305,19 +305,22 @@ struct BookTradeDev {
 struct BookScenDev {
   double rate;
   double spots[RG_BOOK_MAX_UNIVERSE], vols[RG_BOOK_MAX_UNIVERSE], q[RG_BOOK_MAX_UNIVERSE];
+  int32_t dfrow;  // row of the discount tables for this market's rate
 };
-// FP32 constants of one (trade, scenario) pair: ln(S/S0), the log drift per step and the vol.
+// One (trade, scenario) pair: its market (index into the book's markets), the discount-table row
+// of that market's rate, and the FP32 constants ln(S/S0), the log drift per step and the vol.
 struct BookPair32 {
   float x0[RG_NMAX], drift[RG_NMAX], sig[RG_NMAX];
+  int32_t mkt, dfrow;
 };
 // Device pointers of a staged book.
 struct BookDev {
   int32_t U, S, n_trades;
   int64_t TU;
   const BookTradeDev* trades;  // [n_trades]
-  const BookScenDev* scen;     // [S]
+  const BookScenDev* scen;     // the markets the pairs price under
   const BookPair32* pair32;    // [n_trades][S]
-  const double* df;            // [S][TU]  exp(-r_s (t+1) dt)
+  const double* df;            // [rate row][TU]  exp(-r (t+1) dt)
   const double* dfm;           // [n_trades][S] exp(-r_s maturity_j)
   const float* df_f;           // df and dfm rounded to FP32 for the FP32 scan
   const float* dfm_f;

@@ -277,6 +277,18 @@ class BookRequest(C.Structure):
                 ("trades", C.POINTER(BookTrade)), ("config", SimConfig)]
 
 
+class BookBumps(C.Structure):
+    _fields_ = [("spot_relative", C.c_double), ("vol_absolute", C.c_double), ("rate_absolute", C.c_double)]
+
+
+class BookBumpSpec(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("first", C.c_int32), ("second", C.c_int32), ("size", C.c_double)]
+
+
+BOOK_TRADE_SCENARIOS = 16
+BUMP_BASE, BUMP_SPOT, BUMP_VOL, BUMP_RATE, BUMP_SPOT_PAIR = 0, 1, 2, 3, 4
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("device_memory_budget", C.c_uint64),
                 ("max_large_slots", C.c_int32), ("large_work", C.c_uint64)]
@@ -341,6 +353,9 @@ SIGNATURES = {
                              C.POINTER(PriceResult)]),
     "rg_book_run_paths": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32, _u64, _u64,
                                  C.POINTER(PathRecord)]),
+    "rg_price_book_trade_bumps": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(BookBumps), C.POINTER(PriceResult)]),
+    "rg_book_trade_bump": (_i32, [_i32, _i32, C.POINTER(BookBumps), C.POINTER(BookBumpSpec)]),
+    "rg_book_price_trade_bumps": (_i32, [_vp, C.POINTER(BookBumps), C.POINTER(PriceResult)]),
     "rg_book_create": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(_vp)]),
     "rg_book_price": (_i32, [_vp, C.POINTER(Market), _i32, C.POINTER(PriceResult)]),
     "rg_book_tuned_stage": (_i32, [_vp, _i32, C.POINTER(_i32)]),

@@ -69,6 +69,16 @@ class Engine:
         check(self.lib, self.lib.rg_price_book(self.handle, a.ptr, arr, n, out))
         return list(out)
 
+    def price_book_trade_bumps_raw(self, book: BookRequest, sizes=None) -> list:
+        """Every trade under its own 16 scenarios (rg_price_book_trade_bumps): ``out[j * 16 + k]`` is
+        trade j under its bump k (``trade_bump``).  ``sizes``: (spot relative, vol absolute, rate
+        absolute) or None for (1%, 1 vol point, 1bp)."""
+        a = book.to_abi()
+        b = abi.BookBumps(*(sizes or (0.0, 0.0, 0.0)))
+        out = (abi.PriceResult * (len(book.trades) * abi.BOOK_TRADE_SCENARIOS))()
+        check(self.lib, self.lib.rg_price_book_trade_bumps(self.handle, a.ptr, C.byref(b), out))
+        return list(out)
+
     def resident_book(self, book: BookRequest) -> "ResidentBook":
         """Upload `book` once (rg_book_create); price it under many scenario sets."""
         return ResidentBook(self, book)
@@ -211,6 +221,13 @@ class ResidentBook:
         check(self.lib, self.lib.rg_book_price(self.handle, arr, n, out))
         return list(out)
 
+    def price_trade_bumps_raw(self, sizes=None) -> list:
+        """rg_book_price_trade_bumps: ``out[j * 16 + k]``, trade j under its bump k."""
+        b = abi.BookBumps(*(sizes or (0.0, 0.0, 0.0)))
+        out = (abi.PriceResult * (self.n_trades * abi.BOOK_TRADE_SCENARIOS))()
+        check(self.lib, self.lib.rg_book_price_trade_bumps(self.handle, C.byref(b), out))
+        return list(out)
+
     def tuned_stage(self, n_scenarios: int) -> int:
         v = C.c_int32()
         check(self.lib, self.lib.rg_book_tuned_stage(self.handle, n_scenarios, C.byref(v)))
@@ -226,3 +243,13 @@ class ResidentBook:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def trade_bump(n_underlyings: int, scenario: int, sizes=None):
+    """The bump of scenario ``scenario`` (0..15) of a book trade on ``n_underlyings`` underlyings
+    (rg_book_trade_bump): (kind, first, second, size) with kind one of abi.BUMP_*."""
+    lib = load_library()
+    b = abi.BookBumps(*(sizes or (0.0, 0.0, 0.0)))
+    out = abi.BookBumpSpec()
+    check(lib, lib.rg_book_trade_bump(n_underlyings, scenario, C.byref(b), C.byref(out)))
+    return out.kind, out.first, out.second, out.size

@@ -95,3 +95,27 @@ def test_streamed_bridge_schedule_reproduces_the_depth_first_bridge(lib, steps):
         out.append(nxt - cur)
         cur = nxt
     assert max(abs(a - b) for a, b in zip(out, ref)) == 0.0
+
+
+def test_per_trade_bump_rule(lib):
+    """rg_book_trade_bump (host only): scenario 0 is the base; every trade gets 15 distinct bumps
+    on its own underlyings in the documented order — spot up and down and vol up of each
+    underlying first, then the rate and the cross-gamma corners."""
+    from riga_gb300.engine import trade_bump
+
+    for n in range(1, 6):
+        specs = [trade_bump(n, k) for k in range(abi.BOOK_TRADE_SCENARIOS)]
+        assert specs[0][0] == abi.BUMP_BASE
+        assert len(set(specs[1:])) == 15
+        for i in range(n):
+            assert specs[1 + 2 * i] == (abi.BUMP_SPOT, i, -1, 0.01)
+            assert specs[2 + 2 * i] == (abi.BUMP_SPOT, i, -1, -0.01)
+        vols = [s for s in specs if s[0] == abi.BUMP_VOL and s[3] == 0.01]
+        assert [s[1] for s in vols] == list(range(n))
+        for s in specs[1:]:
+            assert 0 <= s[1] < n or s[0] == abi.BUMP_RATE
+    three = [trade_bump(3, k) for k in range(16)]
+    assert three[10] == (abi.BUMP_RATE, -1, -1, 1e-4)
+    assert three[11:14] == [(abi.BUMP_SPOT_PAIR, 0, 1, 0.01), (abi.BUMP_SPOT_PAIR, 0, 2, 0.01),
+                            (abi.BUMP_SPOT_PAIR, 1, 2, 0.01)]
+    assert trade_bump(2, 1, (0.02, 0.0, 0.0))[3] == 0.02

@@ -206,3 +206,61 @@ def test_resident_universe_increments_equal_a_fresh_generation(engine):
         assert r2[0].pv != reused[0].pv
     finally:
         fresh.close()
+
+
+# ------------------------------------------------------------------ per-trade bump sets -------
+def _bumped_markets(universe, underlyings, n):
+    """The 16 universe markets of one trade's bump set, built here from the published rule
+    (rg_book_trade_bump) — the check that the library applied each bump to the right asset."""
+    from riga_gb300.engine import trade_bump
+
+    out = []
+    for k in range(abi.BOOK_TRADE_SCENARIOS):
+        kind, first, second, size = trade_bump(n, k)
+        m = copy.deepcopy(universe)
+        if kind == abi.BUMP_SPOT:
+            m.spots[underlyings[first]] *= 1.0 + size
+        elif kind == abi.BUMP_SPOT_PAIR:
+            m.spots[underlyings[first]] *= 1.0 + size
+            m.spots[underlyings[second]] *= 1.0 + size
+        elif kind == abi.BUMP_VOL:
+            m.vols[underlyings[first]] = max(0.0, m.vols[underlyings[first]] + size)
+        elif kind == abi.BUMP_RATE:
+            m.risk_free_rate += size
+        out.append(m)
+    return out
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_per_trade_bumps_equal_the_bumped_markets(engine, fp32):
+    """rg_price_book_trade_bumps prices trade j under its own 16 scenarios.  For trades of every
+    underlying count, the same 16 bumped universe markets given as a common scenario list price that
+    trade to the same bytes: the bump set is exactly the published rule, applied to the trade's own
+    underlyings, on the same paths and arithmetic."""
+    b = workloads.small_book(paths=1024 if not fp32 else 8192, n_trades=10, fp32=fp32)
+    per = engine.price_book_trade_bumps_raw(b)
+    S = abi.BOOK_TRADE_SCENARIOS
+    assert len(per) == len(b.trades) * S
+    seen = set()
+    for j, bt in enumerate(b.trades):
+        n = len(bt.underlyings)
+        if n in seen:
+            continue
+        seen.add(n)
+        common = engine.price_book_raw(b, _bumped_markets(b.universe, bt.underlyings, n))
+        for k in range(S):
+            assert bytes(per[j * S + k]) == bytes(common[j * S + k]), (j, n, k)
+    assert len(seen) >= 3
+
+
+def test_resident_per_trade_bumps_replay_the_one_shot_price(engine):
+    b = workloads.small_book(paths=8192, n_trades=10, fp32=True)
+    one = engine.price_book_trade_bumps_raw(b)
+    with engine.resident_book(b) as rb:
+        first = rb.price_trade_bumps_raw()
+        again = rb.price_trade_bumps_raw()
+        half = rb.price_trade_bumps_raw((0.005, 0.0, 0.0))  # other sizes: recaptured tables
+        back = rb.price_trade_bumps_raw()
+    assert [bytes(x) for x in first] == [bytes(x) for x in one] == [bytes(x) for x in again] == \
+        [bytes(x) for x in back]
+    assert [bytes(x) for x in half] != [bytes(x) for x in one]
