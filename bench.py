@@ -279,6 +279,21 @@ def large_measure(eng, paths: int = 1 << 24, sample_paths: int = 1 << 16):
                      "kernel_path_steps_per_s": float(paths) * 1260 / (tm.kernel_ms / 1e3)}
     s, h = res["sobol"], res["halton"]
     out["halton_vs_sobol_in_se"] = abs(s.pv - h.pv) / math.sqrt(s.mc_error ** 2 + h.mc_error ** 2)
+    # the cross-check by randomized QMC: independent scramblings (seeds 1-4) of each lane, the
+    # lanes' means compared in units of the replicates' own standard error (the MC standard error
+    # of one run does not measure a QMC estimate's error)
+    reps = {"sobol": [], "halton": []}
+    for kind in reps:
+        for seed in (1, 2, 3, 4):
+            req = workloads.lv5_large(paths=paths, kind=kind)
+            req.config.seed = seed
+            reps[kind].append(eng.price_raw(req).pv)
+    rq = {}
+    for kind, v in reps.items():
+        m = statistics.mean(v)
+        rq[kind] = {"seeds": [1, 2, 3, 4], "pv": v, "mean": m, "rqmc_se": statistics.stdev(v) / math.sqrt(len(v))}
+    se = math.sqrt(rq["sobol"]["rqmc_se"] ** 2 + rq["halton"]["rqmc_se"] ** 2)
+    out["rqmc_cross_check"] = dict(rq, halton_vs_sobol_in_rqmc_se=abs(rq["sobol"]["mean"] - rq["halton"]["mean"]) / se)
     r32 = eng.price_raw(workloads.lv5_large(paths=sample_paths))
     r64 = eng.price_raw(workloads.lv5_large(paths=sample_paths, fp32=False))
     out["accuracy"] = {"abs_err_vs_fp64": abs(r32.pv - r64.pv), "bound_min_0.1se_1bp": min(0.1 * r64.mc_error, 1e-4),

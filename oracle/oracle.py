@@ -39,6 +39,7 @@ def lib() -> C.CDLL:
             "or_probit": (d, [d]),
             "or_radical_inverse": (d, [u64, u32]),
             "or_mix64": (u64, [u64]),
+            "or_halton_hashed_u": (d, [u32, u32, u64, u64]),
             "or_owen_scramble": (u32, [u32, u64, u64]),
             "or_digital_shift": (u32, [u64, u64]),
             "or_primitive_polynomials": (None, [i64, P(u32)]),

@@ -183,6 +183,25 @@ uint64_t or_mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
+/* The engine's production Halton lane (no counterpart in the reference, whose lane wraps at 512
+ * primes): dimension d uses the (d+1)-th prime b, no wrap; digit i of the point (least
+ * significant first) goes through x -> (a·x + c) mod b with a in [1, b-1], c in [0, b-1] from a
+ * SplitMix64 hash of (seed, d, i); u = R / b^k exactly as the engine forms it. */
+double or_halton_hashed_u(uint32_t n, uint32_t b, uint64_t seed, uint64_t dim) {
+  const uint64_t key = seed ^ ((dim + 1) * 0xA0761D6478BD642FULL);
+  uint64_t R = 0, Bk = 1;
+  for (uint32_t i = 0; n; ++i) {
+    const uint32_t q = n / b, d = n - q * b;
+    const uint64_t h = or_mix64(key ^ ((uint64_t)(i + 1) * 0xE7037ED1A0B428DBULL));
+    const uint64_t a = 1u + (((uint64_t)(uint32_t)h * (uint64_t)(b - 1u)) >> 32);
+    const uint64_t cc = ((h >> 32) * (uint64_t)b) >> 32;
+    R = R * b + (a * d + cc) % b;
+    Bk *= b;
+    n = q;
+  }
+  return (double)R / (double)Bk;
+}
+
 /* Nested (Owen) scramble keyed on the scrambled prefix, qmc.rs:292-308 */
 uint32_t or_owen_scramble(uint32_t x, uint64_t dim, uint64_t seed) {
   uint32_t result = 0, prefix = 0;
@@ -809,6 +828,7 @@ typedef struct model {
   uint32_t* hal_bases;
   uint32_t** hal_perm;
   int32_t hal_dim;
+  int hal_hash; /* the engine's production Halton lane (full dimensions, hashed affine digits) */
 } model;
 
 static void model_free(model* m) {
@@ -839,6 +859,13 @@ static void qmc_init(model* m, const rg_simulation_config* c, int64_t need) {
     m->sob_dim = d;
     m->sob_v = (uint32_t*)malloc(sizeof(uint32_t) * 32 * (size_t)d);
     or_sobol_table(d, m->sob_v);
+  } else if (m->vr == RG_VR_HALTON && c->dim_mode == RG_DIM_FULL) {
+    int64_t d = (int64_t)c->qmc_dimension;
+    if (d < need) d = need;
+    m->hal_dim = (int32_t)d;
+    m->hal_hash = 1;
+    m->hal_bases = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)d);
+    or_first_primes((int32_t)d, m->hal_bases);
   } else if (m->vr == RG_VR_HALTON) {
     int64_t d = (int64_t)c->qmc_dimension;
     if (d < 1) d = 1;
@@ -914,6 +941,8 @@ static double ladder_normal(const model* m, uint64_t point, uint64_t dim) {
     x = m->scrambler == RG_SCRAMBLE_DIGITAL_SHIFT ? x ^ or_digital_shift(dim, m->seed)
                                                   : or_owen_scramble(x, dim, m->seed);
     u = ((double)x + 0.5) / 4294967296.0;
+  } else if (m->hal_hash) {
+    u = or_halton_hashed_u((uint32_t)(point + 1), m->hal_bases[dim], m->seed, dim);
   } else {
     uint64_t idx = dim % (uint64_t)m->hal_dim;
     u = radical_inverse_scrambled(point + 1, m->hal_bases[idx], m->hal_perm[idx]);

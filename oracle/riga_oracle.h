@@ -33,6 +33,7 @@ double or_plog(double x);
 double or_probit(double p);
 double or_radical_inverse(uint64_t index, uint32_t base);
 uint64_t or_mix64(uint64_t z);
+double or_halton_hashed_u(uint32_t n, uint32_t b, uint64_t seed, uint64_t dim);
 uint32_t or_owen_scramble(uint32_t x, uint64_t dim, uint64_t seed);
 uint32_t or_digital_shift(uint64_t dim, uint64_t seed);
 /* Fills masks[0..count) with the first `count` primitive GF(2) polynomials of degree >= 2. */

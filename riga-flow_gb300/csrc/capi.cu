@@ -286,6 +286,9 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   if (tr.vr == RG_VR_SOBOL) {
     const std::vector<uint32_t>& v = sobol_table(tr.sob_dim);
     o_sobol = pk.add(v);
+  } else if (tr.vr == RG_VR_HALTON && tr.hal_hash) {
+    o_hb = pk.add(first_primes(tr.hal_dim).data(), (size_t)tr.hal_dim);  // no permutation tables
+    o_ho = o_hp = o_hb;
   } else if (tr.vr == RG_VR_HALTON) {
     halton_tables(tr.hal_dim, tr.seed, hb, ho, hp);
     o_hb = pk.add(hb);

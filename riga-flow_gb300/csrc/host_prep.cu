@@ -196,6 +196,25 @@ const std::vector<uint32_t>& sobol_table(int64_t dim) {
 
 // ------------------------------------------------------------------ Halton tables ------------
 // First primes and their seeded Fisher–Yates digit permutations (qmc.rs:12-22, 128-140).
+const std::vector<uint32_t>& first_primes(int count) {
+  static std::mutex mu;
+  static std::vector<uint32_t> primes;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)primes.size() < count) {
+    // sieve of Eratosthenes past the count-th prime (p_n < n (ln n + ln ln n) for n >= 6)
+    const double x = std::max(count, 6);
+    const size_t lim = (size_t)(x * (std::log(x) + std::log(std::log(x)))) + 16;
+    std::vector<char> comp(lim + 1, 0);
+    primes.clear();
+    for (size_t i = 2; i <= lim && (int)primes.size() < count; ++i) {
+      if (comp[i]) continue;
+      primes.push_back((uint32_t)i);
+      for (size_t k = i * i; k <= lim; k += i) comp[k] = 1;
+    }
+  }
+  return primes;
+}
+
 void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vector<uint32_t>& off,
                    std::vector<uint32_t>& perm) {
   base.clear();
@@ -339,7 +358,15 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
     }
     tr.sob_dim = d;
   } else if (tr.vr == RG_VR_HALTON) {
-    tr.hal_dim = (int32_t)std::min<int64_t>(std::max<int64_t>((int64_t)c.qmc_dimension, 1), 512);
+    if (c.dim_mode == RG_DIM_FULL) {
+      // the production Halton lane: one prime per dimension, no wrap
+      const int64_t d = std::max<int64_t>((int64_t)c.qmc_dimension, (int64_t)n * T);
+      if (d > (int64_t(1) << 20)) raise(RG_ERR_UNSUPPORTED, "the full-dimension Halton lane holds at most 2^20 dimensions");
+      tr.hal_dim = (int32_t)d;
+      tr.hal_hash = 1;
+    } else {
+      tr.hal_dim = (int32_t)std::min<int64_t>(std::max<int64_t>((int64_t)c.qmc_dimension, 1), 512);
+    }
   }
 
   // Phoenix step schedule (note.rs:150-218)
@@ -376,7 +403,7 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
       const uint64_t dim = (uint64_t)P.node_k[nd] * (uint64_t)n + (uint64_t)f;
       int32_t row = 0;
       if (tr.vr == RG_VR_SOBOL) row = (int32_t)(dim % (uint64_t)tr.sob_dim);
-      else if (tr.vr == RG_VR_HALTON) row = (int32_t)(dim % (uint64_t)tr.hal_dim);
+      else if (tr.vr == RG_VR_HALTON) row = (int32_t)(dim % (uint64_t)tr.hal_dim);  // = dim when hashed
       P.nf_row[size_t(nd) * n + f] = row;
       P.nf_shift[size_t(nd) * n + f] = rg_digital_shift(dim, tr.seed);
     }

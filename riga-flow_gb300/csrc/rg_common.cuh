@@ -39,6 +39,7 @@ struct DevTrade {
   int64_t steps, periods;
   int64_t sob_dim;     // rows of the Sobol table (the wrap modulus)
   int32_t hal_dim;
+  int32_t hal_hash;    // 1: the production Halton lane (hashed affine digit scrambling, no wrap)
   int32_t gx;          // Dupire log-strike points
   uint64_t seed;
   double dt, sqrt_dt, inv_sqrt_dt, maturity;
@@ -217,6 +218,31 @@ __device__ __forceinline__ uint32_t rg_sobol_scrambled(const DevTrade& tr, const
                                                    : rg_owen(x, dim, tr.seed);
 }
 
+// The production Halton lane (dimension mode "full"; the engine's own construction, with no
+// counterpart in the reference, whose Halton lane wraps at its first 512 primes): dimension d uses
+// the (d+1)-th prime b and no wrap; the point's base-b digits (least significant first, digit i)
+// are each scrambled by the affine map x -> (a·x + c) mod b, with a in [1, b-1] and c in [0, b-1]
+// drawn from a SplitMix64 hash of (seed, d, i); u = Σ σ_i(d_i) b^-(i+1) formed exactly as an
+// integer over b^k.  Random affine digit scrambling decorrelates the high bases, whose first digits
+// would otherwise rise in lockstep along the points.
+__host__ __device__ __forceinline__ uint64_t rg_halton_key(uint64_t seed, uint64_t dim) {
+  return seed ^ ((dim + 1) * 0xA0761D6478BD642FULL);
+}
+__host__ __device__ __forceinline__ double rg_halton_hashed_u(uint32_t n, uint32_t b, uint64_t key) {
+  uint64_t R = 0, Bk = 1;
+  for (uint32_t i = 0; n; ++i) {
+    const uint32_t q = n / b, d = n - q * b;
+    const uint64_t h = rg_mix64(key ^ ((uint64_t)(i + 1) * 0xE7037ED1A0B428DBULL));
+    const uint64_t a = 1u + ((uint64_t)(uint32_t)h * (uint64_t)(b - 1u) >> 32);
+    const uint64_t cc = (h >> 32) * (uint64_t)b >> 32;
+    // exact either way; 32-bit arithmetic while a·d + c fits (bases below 2^16)
+    R = R * b + (b < 65536u ? (uint64_t)((uint32_t)(a * d + cc) % b) : (a * d + cc) % b);
+    Bk *= b;
+    n = q;
+  }
+  return (double)R / (double)Bk;
+}
+
 // FP64 normal of the QMC lanes (Ladder::normal, qmc.rs:119-125, 284-289).
 __device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevTables& tb,
                                                   uint64_t point, uint64_t dim) {
@@ -224,6 +250,8 @@ __device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevT
   if (tr.vr == RG_VR_SOBOL) {
     uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
     u = ((double)x + 0.5) / 4294967296.0;
+  } else if (tr.hal_hash) {
+    u = rg_halton_hashed_u((uint32_t)(point + 1), __ldg(tb.hal_base + dim), rg_halton_key(tr.seed, dim));
   } else {
     uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
     u = rg_halton_u(point + 1, __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx));
@@ -258,6 +286,11 @@ __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTa
   if (tr.vr == RG_VR_SOBOL) {
     uint32_t x = rg_sobol_scrambled(tr, tb.sobol, point, dim);
     return rg_probit32(x);
+  }
+  if (tr.hal_hash) {
+    const double u = rg_halton_hashed_u((uint32_t)(point + 1), __ldg(tb.hal_base + dim), rg_halton_key(tr.seed, dim));
+    const float z = normcdfinvf((float)fmax(fmin(u, 1.0 - u), 1.0e-12));
+    return u < 0.5 ? z : -z;
   }
   const uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
   return rg_halton_normal32((uint32_t)(point + 1), __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx));

@@ -159,6 +159,8 @@ void bridge_schedule_into(int64_t T, double dt, Prepared& P);
 // The Sobol direction table for `dim` dimensions (process-wide cache).
 const std::vector<uint32_t>& sobol_table(int64_t dim);
 std::vector<double> calib_axes(const rg_implied_vol_grid& g, double spot, double rate, int gx);
+// The first `count` primes (cached process-wide; at least `count` entries).
+const std::vector<uint32_t>& first_primes(int count);
 // Halton bases and permutations.
 void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vector<uint32_t>& off,
                    std::vector<uint32_t>& perm);

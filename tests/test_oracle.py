@@ -437,3 +437,21 @@ def test_portable_math_oracle_stays_close_to_the_libm_oracle(termsheet1, golden_
         res = O.price_put_leg(termsheet1.request, threads=1)
     got = result_to_json(res, termsheet1.request)
     assert json_close(got, golden_result, tol=1e-12) == []
+
+
+def test_production_halton_lane_is_a_scrambled_radical_inverse():
+    """The engine's full-dimension Halton lane (no counterpart in the reference): each digit goes
+    through an invertible affine map mod the prime base, so points 1..b-1 of base b take b-1
+    distinct first digits — one per stratum of width 1/b — and every value lies in [0, 1)."""
+    L = lib()
+    for dim, b in ((0, 2), (7, 19), (6299, 62989)):
+        us = [L.or_halton_hashed_u(n, b, 1, dim) for n in range(1, min(b, 4000))]
+        assert all(0.0 <= u < 1.0 for u in us)
+        strata = {int(u * b) for u in us}
+        assert len(strata) == len(us)
+    # two dimensions of neighbouring large primes are not in lockstep (the unscrambled radical
+    # inverse n/b would give a correlation near 1 over the first points)
+    import statistics
+    a = [L.or_halton_hashed_u(n, 62983, 1, 6298) for n in range(1, 4001)]
+    c = [L.or_halton_hashed_u(n, 62989, 1, 6299) for n in range(1, 4001)]
+    assert abs(statistics.correlation(a, c)) < 0.1
