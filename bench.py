@@ -67,6 +67,15 @@ def flops_per_launch(paths, steps, n_assets, n_scen):
     return float(paths) * steps * per_path_step
 
 
+def n_scen_slots(n_scen):
+    """Scenario slots of the tiled FP32 kernel's CTA: the scenario count rounded up to a power of two,
+    at least 4."""
+    sb = 4
+    while sb < n_scen:
+        sb <<= 1
+    return sb
+
+
 def measured_peaks():
     try:
         return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -303,69 +312,103 @@ def large_measure(eng, paths: int = 1 << 24, sample_paths: int = 1 << 16):
 
 
 # ----------------------------------------------------------------------------- serving (cfg 3) -
-def serving_measure(duration_s: float = 5.0, rate_per_s: float = 200.0, seed: int = 7):
-    """Seeded Poisson arrivals into the continuous-batching server (4 slots): 90% single trades
-    (3-asset local vol, 2^14 paths, 756 steps, FP32) with 0, 7 or 15 CRN bumps, 10% books of
-    16-64 trades of the book universe at 2^14 paths under 8 common scenarios.  Latency is submit
-    to completion; throughput counts every finished request's path-steps."""
+def serving_measure(duration_s: float = 60.0, rate_per_s: float = 200.0, book_rate_per_s: float = 1.0,
+                    budget_gib: float = 24.0, seed: int = 7):
+    """Seeded Poisson arrivals at `rate_per_s` into the continuous-batching server (4 slots) for
+    `duration_s` seconds: single 3-asset local-vol trades at 2^14 paths (756 steps, FP32) and, at
+    `book_rate_per_s` of the arrivals, books of 16-256 trades of the book distribution at 2^18 paths;
+    every request takes 0, 7 or 15 CRN bumps (a book's 15 are per-trade bumps on its own underlyings,
+    its 7 the first 8 scenarios of the universe-wide common set).  The server admits requests within
+    a device-memory budget of `budget_gib` GiB, which holds one 2^18-path book (its double-buffered
+    universe increments) beside the singles, so overlapping books wait for memory.  Latency is
+    submit to completion per request; throughput counts every finished request's path-steps."""
     from riga_gb300 import workloads
     from riga_gb300.serve import Server
 
     rng = workloads.SplitMix64(seed)
     single = workloads.lv3(paths=1 << 14, steps=756, fp32=True)
     scen = [(m, s) for _, m, s in workloads.crn15_scenarios(single)]
-    bk = workloads.book(paths=1 << 14, n_trades=64, fp32=True)
+    book_paths = 1 << 18
+    bk = workloads.book(paths=book_paths, n_trades=256, fp32=True)
     bsc = [m for _, m in workloads.book_scenarios(bk.universe)][:8]
     plan, t = [], 0.0
     while True:
         t += -math.log(1.0 - rng.uniform(0.0, 1.0)) / rate_per_s
         if t >= duration_s:
             break
-        if rng.uniform(0.0, 1.0) < 0.9:
-            k = (0, 7, 15)[rng.next_u64() % 3]
-            plan.append((t, "price", k))
+        k = (0, 7, 15)[rng.next_u64() % 3]
+        if rng.uniform(0.0, 1.0) < book_rate_per_s / rate_per_s:
+            plan.append((t, "book", k, 16 + rng.next_u64() % 241))
         else:
-            plan.append((t, "book", 16 + rng.next_u64() % 49))
+            plan.append((t, "price", k, 1))
+
+    def submit(srv, kind, k, n_trades):
+        if kind == "price":
+            return srv.submit_price(single, scen[: k + 1] if k else None), float(1 << 14) * 756 * (k + 1)
+        b = copy.copy(bk)
+        b.trades = bk.trades[:n_trades]
+        steps = float(sum(tr.terms.steps for tr in b.trades)) * book_paths
+        if k == 15:
+            return srv.submit_book_trade_bumps(b), steps * 16
+        return srv.submit_book(b, bsc if k == 7 else None), steps * (k + 1)
+
+    budget = int(budget_gib * (1 << 30))
+    lat = {}
     units = 0.0
-    with Server(slots=4) as srv:
+    with Server(slots=4, memory_budget=budget) as srv:
         # warm-up outside the timed window: every request shape once per slot (the first book on
         # an engine pays the one-time cost of its tables and kernel loading)
-        warm = copy.deepcopy(bk)
-        warm.trades = bk.trades[:16]
         tickets = []
         for _ in range(4):
-            tickets += [srv.submit_book(warm, bsc)] + [srv.submit_price(single, scen[:k + 1] if k else None)
-                                                       for k in (0, 7, 15)]
+            for k in (0, 7, 15):
+                tickets += [submit(srv, "book", k, 16)[0], submit(srv, "price", k, 1)[0]]
         for tk in tickets:
             srv.wait(tk)
-        busy0 = srv.stats().busy_s
+            srv.release(tk)
+        st0 = srv.stats()
         t0 = time.perf_counter()
-        tickets = []
-        for at, kind, k in plan:
+        live = []
+        for at, kind, k, n_trades in plan:
             delay = at - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
-            if kind == "price":
-                tickets.append(srv.submit_price(single, scen[: k + 1] if k else None))
-                units += float(1 << 14) * 756 * (k + 1)
-            else:
-                b = copy.deepcopy(bk)
-                b.trades = bk.trades[:k]
-                tickets.append(srv.submit_book(b, bsc))
-                units += float(sum(tr.terms.steps for tr in b.trades)) * (1 << 14) * len(bsc)
-        infos = [srv.wait(tk) for tk in tickets]
+            tk, u = submit(srv, kind, k, n_trades)
+            live.append((tk, kind, k, n_trades))
+            units += u
+        for tk, kind, k, n_trades in live:
+            info = srv.wait(tk)
+            srv.release(tk)
+            lat.setdefault((kind, k), []).append(1e3 * (info.end_s - info.submit_s))
         wall = time.perf_counter() - t0
         st = srv.stats()
-    # latencies of the timed requests only (the server's own statistics include the warm-up)
-    lat = sorted(1e3 * (i.end_s - i.submit_s) for i in infos)
-    pct = lambda q: lat[min(len(lat) - 1, max(0, math.ceil(q * len(lat)) - 1))]
-    return {"workload": f"Poisson arrivals at {rate_per_s:g}/s for {duration_s:g} s (seed {seed}): 90% single "
-                        f"3-asset local-vol trades at 2^14 paths with 0/7/15 bumps, 10% 16-64-trade books at "
-                        f"2^14 paths x 8 scenarios; 4 slots",
-            "requests": len(plan), "completed": st.completed - 16, "failed": st.failed,
-            "p50_ms": pct(0.50), "p99_ms": pct(0.99), "max_ms": lat[-1], "wall_s": wall,
-            "path_steps_per_s": units / wall, "busy_s": st.busy_s - busy0,
-            "warm_up": "16 requests (each slot: one 16-trade book, singles with 0/7/15 bumps) before the timed window"}
+
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, max(0, math.ceil(q * len(v)) - 1))]
+
+    every = [x for v in lat.values() for x in v]
+    classes = {}
+    for (kind, k), v in sorted(lat.items()):
+        name = ("single_2^14_paths" if kind == "price" else "book_16-256_trades_2^18_paths") + f"_{k}_bumps"
+        classes[name] = {"requests": len(v), "p50_ms": pct(v, 0.50), "p99_ms": pct(v, 0.99), "max_ms": max(v)}
+    n_books = sum(1 for p in plan if p[1] == "book")
+    return {"workload": f"Poisson arrivals at {rate_per_s:g}/s for {duration_s:g} s (seed {seed}): single 3-asset "
+                        f"local-vol trades at 2^14 paths x 756 steps and, at {book_rate_per_s:g}/s, books of "
+                        f"16-256 trades of the book distribution at 2^18 paths; 0, 7 or 15 CRN bumps per request "
+                        f"(books: 15 per-trade bumps, or the first 8 common scenarios); 4 slots, device-memory "
+                        f"budget {budget_gib:g} GiB",
+            "requests": len(plan), "books": n_books, "completed": st.completed - st0.completed,
+            "failed": st.failed - st0.failed, "p50_ms": pct(every, 0.50), "p99_ms": pct(every, 0.99),
+            "max_ms": max(every), "classes": classes, "wall_s": wall, "path_steps_per_s": units / wall,
+            "busy_s": st.busy_s - st0.busy_s,
+            "admission": {"device_memory_budget_bytes": budget, "memory_waits": st.memory_waits - st0.memory_waits,
+                          "peak_reserved_bytes": st.peak_reserved_bytes,
+                          "note": "memory_waits: requests that waited at the head of the queue because their "
+                                  "device-memory estimate did not fit beside the running requests"},
+            "sustained_rate": f"{rate_per_s:g} requests/s, of which {book_rate_per_s:g}/s books (the book rate "
+                              f"the GPU sustains beside the singles)",
+            "warm_up": "24 requests (each slot: a 16-trade book and a single with 0, 7 and 15 bumps) before the "
+                       "timed window"}
 
 
 # ----------------------------------------------------------------------------- GPU arm --------
@@ -387,6 +430,9 @@ def run_gpu(args):
 
     build_library()
     eng = Engine(local)
+    if args.shape:
+        knobs = [int(x) for x in args.shape.split(",")] + [0]
+        abi.check(eng.lib, eng.lib.rg_set_tiled_shape(knobs[0], knobs[1], knobs[2]))
     P, T = args.paths, args.timesteps
     req, scen = workload_request(P, T, fp32=True, rank=rank, world=world)
     n_scen = len(scen)
@@ -475,7 +521,10 @@ def run_gpu(args):
         "gpu_launches": int(tm.kernel_launches) * args.steps,
         "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes,
                    "tile_steps": tm.tile_steps, "paths_per_thread": tm.paths_per_thread,
-                   "tuned_by": "autotuner (rg_set_autotune): paths per thread and tile depth, timed during warm-up"},
+                   "paths_per_cta_tile": tm.block * tm.paths_per_thread // n_scen_slots(n_scen),
+                   "tuned_by": (f"forced by --shape {args.shape} (rg_set_tiled_shape)" if args.shape else
+                                "autotuner (rg_set_autotune): paths per CTA tile, paths per thread and tile depth, "
+                                "timed during warm-up")},
         "clocks": clocks,
     }
     if merged_pv is not None:
@@ -491,7 +540,7 @@ def run_gpu(args):
     if world == 1 and not args.no_large:
         line["large"] = large_measure(eng, paths=args.large_paths, sample_paths=min(1 << 16, args.large_paths))
     if world == 1 and not args.no_serving:
-        line["serving"] = serving_measure()
+        line["serving"] = serving_measure(duration_s=args.serving_seconds)
     if world == 1 and not args.no_cpu_baseline:
         rate, cores, paths, dt = cpu_rate(P, T, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -518,6 +567,11 @@ def main():
     ap.add_argument("--large-paths", type=int, default=1 << 24, help="paths of the large fused (cfg 4) run")
     ap.add_argument("--book-trades", type=int, default=4096)
     ap.add_argument("--book-paths", type=int, default=1 << 18)
+    ap.add_argument("--serving-seconds", type=float, default=60.0, help="window of the serving (cfg 3) run")
+    ap.add_argument("--shape", default=None, metavar="PPT,TT[,PB]",
+                    help="force the tiled FP32 kernel's paths per thread, tile depth and paths per CTA tile "
+                         "(rg_set_tiled_shape) instead of autotuning them, e.g. for a profiler capture with no "
+                         "tuning launches")
     args = ap.parse_args()
     if args.only:
         import torch
@@ -533,7 +587,7 @@ def main():
             print(json.dumps(large_measure(Engine(0), paths=args.large_paths,
                                            sample_paths=min(1 << 16, args.large_paths))), flush=True)
         else:
-            print(json.dumps(serving_measure()), flush=True)
+            print(json.dumps(serving_measure(duration_s=args.serving_seconds)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -344,12 +344,14 @@ int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
  * through rg_price_put_leg_static never tune.  Disabling also clears the tuned shapes.  No
  * counterpart in the reference. */
 int32_t rg_set_autotune(int32_t enabled);
-/* Forces every tiled FP32 launch of the process onto one schedule: paths per thread 1 or 2 and a
- * tile depth among the autotuner's candidates (24, 32, 48, 64, 80, 96, 128); (0, 0) returns to the
- * formula shape or the autotuner.  A forced tile that does not fit in shared memory fails the
- * pricing call with RG_ERR_INVALID_ARGUMENT.  For callers that need a fixed schedule, and for
- * checking that schedules do not change prices.  No counterpart in the reference. */
-int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps);
+/* Forces every tiled FP32 launch of the process onto one schedule: paths per thread 1 or 2, a tile
+ * depth among the autotuner's candidates (24, 32, 48, 64, 80, 96, 128) and a block of
+ * paths_per_block paths per CTA tile (0 = the formula block of 1024 / scenario slots; otherwise a
+ * power of two of at least 32 × paths per thread); (0, 0, 0) returns to the formula shape or the
+ * autotuner.  A forced shape that does not fit (shared memory, 1024 threads) fails the pricing
+ * call with RG_ERR_INVALID_ARGUMENT.  For callers that need a fixed schedule, and for checking
+ * that schedules do not change prices.  No counterpart in the reference. */
+int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block);
 /* Clock cycles the tiled FP32 kernel's CTAs spent in generation, bridge, stepping and path close
  * (out[0..3], summed over CTAs since the last reset), for profiling.  Only a library built with
  * RG_PHASE_CLOCKS=1 records them; others return RG_ERR_UNSUPPORTED.  No counterpart in the
@@ -493,7 +495,7 @@ typedef struct rg_server_config {
 } rg_server_config;
 
 enum { RG_JOB_QUEUED = 0, RG_JOB_RUNNING = 1, RG_JOB_DONE = 2, RG_JOB_FAILED = 3, RG_JOB_CANCELLED = 4 };
-enum { RG_JOB_PRICE = 0, RG_JOB_RISK = 1, RG_JOB_BOOK = 2 };
+enum { RG_JOB_PRICE = 0, RG_JOB_RISK = 1, RG_JOB_BOOK = 2, RG_JOB_BOOK_BUMPS = 3 };
 
 typedef struct rg_job_info {
   int32_t state;          /* RG_JOB_* */
@@ -510,6 +512,10 @@ typedef struct rg_server_stats {
   uint64_t device_bytes_held, device_memory_budget;
   double p50_ms, p99_ms, max_ms; /* submit-to-completion latency of completed requests */
   double busy_s;                 /* wall time with at least one request running */
+  uint64_t memory_waits;         /* requests that waited at the head of the queue because their
+                                    device-memory estimate did not fit beside the running ones */
+  uint64_t peak_reserved_bytes;  /* largest reservation seen: the slots' holdings and the running
+                                    requests' estimates */
 } rg_server_stats;
 
 int32_t rg_server_create(const rg_server_config* config, rg_server** out);
@@ -524,6 +530,10 @@ int32_t rg_server_submit_risk(rg_server* server, const rg_price_request* request
 /* A book under a common scenario set (rg_price_book). */
 int32_t rg_server_submit_book(rg_server* server, const rg_book_request* request,
                               const rg_market_snapshot* scenarios, int32_t n_scenarios, uint64_t* ticket);
+/* A book with every trade under its own 16 scenarios (rg_price_book_trade_bumps; sizes NULL = the
+ * defaults): n_results = n_trades * 16, out[j * 16 + k]. */
+int32_t rg_server_submit_book_trade_bumps(rg_server* server, const rg_book_request* request,
+                                          const rg_book_bumps* sizes, uint64_t* ticket);
 /* Current state without blocking. */
 int32_t rg_server_poll(rg_server* server, uint64_t ticket, rg_job_info* info);
 /* Blocks until the request is DONE, FAILED or CANCELLED, or `timeout_ms` passes (negative = no

@@ -481,6 +481,15 @@ size_t estimate_book_bytes(const rg_book_request* r, int n_scen) {
   return b + b / 8 + (size_t(1) << 20);
 }
 
+// Under per-trade bump sets a book prices 16 (trade, scenario) pairs per trade, as under 16 common
+// scenarios, and plans one market per distinct bumped universe market (at most 16 per trade), each
+// with its per-step tables.
+size_t estimate_book_trade_bumps_bytes(const rg_book_request* r) {
+  const size_t TU = (size_t)(r->universe_steps > 0 ? r->universe_steps : 1);
+  const size_t markets = std::min<size_t>((size_t)(r->n_trades > 0 ? r->n_trades : 1) * RG_BOOK_TRADE_SCENARIOS, 4096);
+  return estimate_book_bytes(r, RG_BOOK_TRADE_SCENARIOS) + markets * (TU * 16 + 256);
+}
+
 namespace {
 
 using namespace bk;

@@ -960,8 +960,8 @@ extern "C" int32_t rg_set_autotune(int32_t enabled) {
   RG_TRY({ p32_set_autotune(enabled != 0); })
 }
 
-extern "C" int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps) {
-  RG_TRY({ p32_force_shape(paths_per_thread, tile_steps); })
+extern "C" int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block) {
+  RG_TRY({ p32_force_shape(paths_per_thread, tile_steps, paths_per_block); })
 }
 
 extern "C" int32_t rg_phase_clocks(uint64_t out[4], int32_t reset) {

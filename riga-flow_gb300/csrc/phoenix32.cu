@@ -801,20 +801,31 @@ uint64_t p32_chunks(uint64_t npaths) { return (npaths + 31) / 32; }
 
 // ---------------------------------------------------------------------- tiled-shape autotuner --
 namespace {
-std::mutex g_tune_mu;
-std::map<std::vector<int64_t>, std::pair<int, int>> g_tuned;  // launch shape -> (paths per thread, tile depth)
-bool g_tune_enabled = true;
-std::pair<int, int> g_forced{0, 0};  // (paths per thread, tile depth) every tiled launch takes, or none
+// A tiled launch shape: paths per CTA tile, paths per thread, tile depth.
+struct TiledKnobs {
+  int pb, ppt, tt;
+  bool operator==(const TiledKnobs& o) const { return pb == o.pb && ppt == o.ppt && tt == o.tt; }
+};
 
-// Sets the paths per thread and tile depth of a tiled shape if its layout fits.
-bool p32_with(const Prepared& P, Fp32Shape& sh, int ppt, int tt) {
-  if (!p32_fits(P, sh.Pb, ppt, tt)) return false;
-  sh.ppt = ppt;
-  sh.threads = sh.Sb * sh.Pb / ppt;
-  sh.TT = tt;
-  sh.smem = (int)p32_layout(P.n, sh.Pb, tt, tt + P.stack_max, P.stack_max, ppt).total;
+// Sets the block (Pb paths per tile), paths per thread and tile depth of a tiled shape if the
+// block keeps a warp on 32·ppt paths of one scenario and its layout fits.
+bool p32_with(const Prepared& P, Fp32Shape& sh, TiledKnobs k) {
+  if (k.pb < 32 * k.ppt || (k.pb & (k.pb - 1)) || k.pb * sh.Sb > 1024 || !p32_fits(P, k.pb, k.ppt, k.tt)) return false;
+  sh.Pb = k.pb;
+  sh.ppt = k.ppt;
+  sh.threads = sh.Sb * k.pb / k.ppt;
+  sh.TT = k.tt;
+  sh.smem = (int)p32_layout(P.n, k.pb, k.tt, k.tt + P.stack_max, P.stack_max, k.ppt).total;
   return true;
 }
+
+std::mutex g_tune_mu;
+std::map<std::vector<int64_t>, TiledKnobs> g_tuned;  // launch shape -> (block, paths per thread, tile depth)
+bool g_tune_enabled = true;
+TiledKnobs g_forced{0, 0, 0};  // (block, paths per thread, tile depth) every tiled launch takes, or none
+                               // (pb 0: the formula block)
+
+
 }  // namespace
 
 void p32_set_autotune(bool enabled) {
@@ -823,19 +834,22 @@ void p32_set_autotune(bool enabled) {
   g_tuned.clear();
 }
 
-void p32_force_shape(int ppt, int tt) {
-  if (!((ppt == 0 && tt == 0) || ((ppt == 1 || ppt == 2) && tt > 0)))
-    raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: paths per thread 1 or 2 and a tile depth, or (0, 0)");
+void p32_force_shape(int ppt, int tt, int pb) {
+  if (!((ppt == 0 && tt == 0 && pb == 0) || ((ppt == 1 || ppt == 2) && tt > 0 && pb >= 0)))
+    raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: paths per thread 1 or 2, a tile depth and a block, or (0, 0, 0)");
+  if (pb != 0 && (pb < 32 * ppt || pb > 1024 || (pb & (pb - 1))))
+    raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the block must be a power of two of 32 x paths per thread to 1024 paths");
   bool plan = tt == 0;
   for (int c : kTileCandidates) plan = plan || c == tt;
   if (!plan) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the tile depth must be one of the autotuner's candidates");
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_forced = {ppt, tt};
+  g_forced = TiledKnobs{pb, ppt, tt};
 }
 
-// Times every (paths per thread, tile depth) candidate on a prefix of the launch's paths and keeps
-// the fastest for the launch shape.  Neither knob changes a path's arithmetic or the 32-path chunks
-// of the sums, so prices are identical whichever wins.
+// Times every (block, paths per thread, tile depth) candidate on a prefix of the launch's paths and
+// keeps the fastest for the launch shape.  No knob changes a path's arithmetic or the 32-path
+// chunks of the sums, so prices are identical whichever wins.  Blocks: the formula's Pb paths per
+// tile and half of it (two smaller CTAs per SM where they fit).
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
                          const LaunchOut& out, bool may_tune, cudaStream_t st) {
@@ -846,17 +860,17 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   cuda_check(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "SM count");
   const std::vector<int64_t> key{dev, P.n, P.trade.has_lv, P.n_scen, sh.Sb, P.T, P.stack_max,
                                  P.trade.vr, P.trade.scrambler, P.trade.gx};
-  auto apply = [&](std::pair<int, int> c, uint64_t paths) {
+  auto apply = [&](TiledKnobs c, uint64_t paths) {
     Fp32Shape t = sh;
-    if (!p32_with(P, t, c.first, c.second)) return sh;
+    if (!p32_with(P, t, c)) return sh;
     t.grid = tiled_grid(P, t, paths, sm_count);
     t.tuned = 1;
     return t;
   };
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    if (g_forced.first) {
-      Fp32Shape t = apply(g_forced, npaths);
+    if (g_forced.ppt) {
+      Fp32Shape t = apply({g_forced.pb ? g_forced.pb : sh.Pb, g_forced.ppt, g_forced.tt}, npaths);
       if (!t.tuned) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the forced tile does not fit in shared memory");
       return t;
     }
@@ -868,15 +882,16 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   // launches of at least eight waves
   const uint64_t prefix = (uint64_t)sh.grid * (uint64_t)sh.Pb * 2;
   if (!may_tune || npaths < prefix * 4) return sh;
-  std::vector<std::pair<int, int>> cand;
+  std::vector<TiledKnobs> cand;
   std::vector<int> tts{sh.TT};
   tts.insert(tts.end(), std::begin(kTileCandidates), std::end(kTileCandidates));
-  for (int ppt = 1; ppt <= 2; ++ppt)
-    for (int tt : tts) {
-      Fp32Shape c = sh;
-      const std::pair<int, int> pc{ppt, tt};
-      if (std::find(cand.begin(), cand.end(), pc) == cand.end() && p32_with(P, c, ppt, tt)) cand.push_back(pc);
-    }
+  for (int pb : {sh.Pb, sh.Pb / 2})
+    for (int ppt = 1; ppt <= 2; ++ppt)
+      for (int tt : tts) {
+        Fp32Shape c = sh;
+        const TiledKnobs k{pb, ppt, tt};
+        if (std::find(cand.begin(), cand.end(), k) == cand.end() && p32_with(P, c, k)) cand.push_back(k);
+      }
   LaunchOut lo = out;  // the partial sums are overwritten by the real launch afterwards
   lo.ko_steps = nullptr;
   lo.records = nullptr;

@@ -8,10 +8,12 @@
 // slots and memory free up, and the ones admitted run concurrently on their own streams.  Requests
 // whose work (paths × steps × scenarios, summed over a book's trades) reaches the large-work mark
 // may hold at most max_large_slots slots at once; a worker takes the first queued request it may
-// start, so small requests pass large ones that are waiting for a large slot, and a request that
-// waits for memory is never passed.  Each
+// start, so small requests pass large ones that are waiting for a large slot.  A request that waits
+// for memory is passed only by requests whose estimate is at most a sixteenth of the budget (single
+// trades beside a waiting book), which can hold back little of the memory it waits for.  Each
 // request runs through the same entry points as a direct call (rg_price_scenarios,
-// rg_price_risk_batch, rg_price_book), so its results are independent of what runs beside it.
+// rg_price_risk_batch, rg_price_book, rg_price_book_trade_bumps), so its results are independent of
+// what runs beside it.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -147,11 +149,14 @@ struct Job {
   std::vector<rg_scenario> scen_views;
   rg_central_difference_config risk_cfg{};
   OwnedBook book;
+  rg_book_bumps bumps{};  // per-trade bump sizes of an RG_JOB_BOOK_BUMPS request
+  bool has_bumps = false;
   std::vector<OwnedMarket> book_scen;
   std::vector<rg_market_snapshot> book_scen_views;
   size_t est = 0;
   double work = 0;     // path-steps × scenarios the request prices
   bool large = false;  // work at or above the server's large-work mark
+  bool waited_memory = false;  // was passed over at least once because it did not fit the budget
   uint64_t n_results = 0;
   int state = RG_JOB_QUEUED;
   int32_t status = RG_OK;
@@ -192,6 +197,8 @@ struct rg_server {
   int max_large = 1;        // slots large requests may hold at once
   double large_work = 0;    // work at which a request counts as large
   int n_large = 0;          // large requests running
+  uint64_t memory_waits = 0;  // requests that waited at the head of the queue for device memory
+  size_t peak_reserved = 0;   // largest reservation (the slots' holdings and running estimates)
 };
 
 namespace rg {
@@ -236,6 +243,9 @@ void run_job(rg_engine* E, Job* job) {
       st = rg_price_book(E, &job->book.r, job->book_scen_views.empty() ? nullptr : job->book_scen_views.data(),
                          (int32_t)job->book_scen_views.size(), job->results.data());
       break;
+    case RG_JOB_BOOK_BUMPS:
+      st = rg_price_book_trade_bumps(E, &job->book.r, job->has_bumps ? &job->bumps : nullptr, job->results.data());
+      break;
     default:
       st = RG_ERR_INVALID_ARGUMENT;
   }
@@ -248,12 +258,20 @@ void run_job(rg_engine* E, Job* job) {
 }
 
 // Under S->mu: the queued request slot k starts next, or null.  Requests go in arrival order,
-// except that a large one waiting for a large slot is passed; one that does not fit the memory
-// budget stops the scan (later requests never overtake it on memory).
+// except that a large one waiting for a large slot is passed, and one that does not fit the memory
+// budget is passed only by requests of at most a sixteenth of the budget (later requests with larger
+// estimates never overtake it on memory).
 Job* next_job(rg_server* S, int k) {
+  bool waiting = false;  // an earlier request waits for memory
   for (Job* j : S->queue) {
     if (j->large && S->n_large >= S->max_large) continue;
-    return admit(S, k, j) ? j : nullptr;
+    if (waiting && j->est > S->budget / 16) continue;
+    if (admit(S, k, j)) return j;
+    if (!j->waited_memory) {
+      j->waited_memory = true;
+      ++S->memory_waits;
+    }
+    waiting = true;
   }
   return nullptr;
 }
@@ -273,6 +291,7 @@ void worker(rg_server* S, int k) {
     Slot& slot = S->slots[k];
     slot.busy = true;
     slot.running = job->est;
+    S->peak_reserved = std::max(S->peak_reserved, reserved(S));
     job->state = RG_JOB_RUNNING;
     job->slot = k;
     job->t_start = now_s(S);
@@ -289,6 +308,7 @@ void worker(rg_server* S, int k) {
     slot.busy = false;
     slot.running = 0;
     slot.held = held;
+    S->peak_reserved = std::max(S->peak_reserved, reserved(S));
     if (job->cancel) {
       job->state = RG_JOB_CANCELLED;
       ++S->cancelled;
@@ -478,6 +498,28 @@ extern "C" int32_t rg_server_submit_book(rg_server* S, const rg_book_request* re
   })
 }
 
+extern "C" int32_t rg_server_submit_book_trade_bumps(rg_server* S, const rg_book_request* req,
+                                                     const rg_book_bumps* sizes, uint64_t* ticket) {
+  RG_TRY({
+    if (!S || !req || !ticket) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
+    std::unique_ptr<Job> job(new Job());
+    job->kind = RG_JOB_BOOK_BUMPS;
+    job->book.copy(*req);
+    if (sizes) {
+      job->bumps = *sizes;
+      job->has_bumps = true;
+    }
+    const uint64_t S_ = RG_BOOK_TRADE_SCENARIOS;
+    job->n_results = (uint64_t)(req->n_trades > 0 ? req->n_trades : 0) * S_;
+    job->results.resize(job->n_results);
+    job->est = estimate_book_trade_bumps_bytes(&job->book.r);
+    double steps = (double)req->universe_steps * (double)req->universe.n_assets;  // the universe generation
+    for (int32_t j = 0; j < req->n_trades; ++j) steps += (double)req->trades[j].terms.steps * (double)S_;
+    job->work = (double)req->config.paths * steps;
+    *ticket = enqueue(S, std::move(job));
+  })
+}
+
 extern "C" int32_t rg_server_poll(rg_server* S, uint64_t ticket, rg_job_info* info) {
   RG_TRY({
     if (!S) raise(RG_ERR_INVALID_ARGUMENT, "null server");
@@ -575,5 +617,7 @@ extern "C" int32_t rg_server_get_stats(rg_server* S, rg_server_stats* out) {
     out->p99_ms = percentile(S->latencies_ms, 0.99);
     out->max_ms = S->latencies_ms.empty() ? 0.0 : *std::max_element(S->latencies_ms.begin(), S->latencies_ms.end());
     out->busy_s = S->busy_s + (S->n_running ? now_s(S) - S->busy_since : 0.0);
+    out->memory_waits = S->memory_waits;
+    out->peak_reserved_bytes = S->peak_reserved;
   })
 }

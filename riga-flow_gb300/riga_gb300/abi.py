@@ -305,11 +305,11 @@ class ServerStats(C.Structure):
                 ("cancelled", C.c_uint64), ("queued", C.c_uint64), ("running", C.c_uint64),
                 ("device_bytes_held", C.c_uint64), ("device_memory_budget", C.c_uint64),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
-                ("busy_s", C.c_double)]
+                ("busy_s", C.c_double), ("memory_waits", C.c_uint64), ("peak_reserved_bytes", C.c_uint64)]
 
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED, JOB_CANCELLED = range(5)
-JOB_PRICE, JOB_RISK, JOB_BOOK = range(3)
+JOB_PRICE, JOB_RISK, JOB_BOOK, JOB_BOOK_BUMPS = range(4)
 
 
 class RigaError(Exception):
@@ -346,7 +346,7 @@ SIGNATURES = {
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
     "rg_set_autotune": (_i32, [_i32]),
-    "rg_set_tiled_shape": (_i32, [_i32, _i32]),
+    "rg_set_tiled_shape": (_i32, [_i32, _i32, _i32]),
     "rg_phase_clocks": (_i32, [C.POINTER(C.c_uint64), _i32]),
     "rg_surfaces_upload": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32, C.POINTER(_i32)]),
     "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
@@ -368,6 +368,8 @@ SIGNATURES = {
                                      C.POINTER(_u64)]),
     "rg_server_submit_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,
                                      C.POINTER(_u64)]),
+    "rg_server_submit_book_trade_bumps": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(BookBumps),
+                                                 C.POINTER(_u64)]),
     "rg_server_poll": (_i32, [_vp, _u64, C.POINTER(JobInfo)]),
     "rg_server_wait": (_i32, [_vp, _u64, _i64, C.POINTER(JobInfo)]),
     "rg_server_results": (_i32, [_vp, _u64, C.POINTER(PriceResult), _u64]),

@@ -101,6 +101,16 @@ class Server:
         self._kinds[t.value] = abi.JOB_BOOK
         return t.value
 
+    def submit_book_trade_bumps(self, book: BookRequest, sizes: Optional[abi.BookBumps] = None) -> int:
+        """Every trade of `book` under its own 16 scenarios (base + 15 bumps on its own underlyings);
+        results[j * 16 + k] is trade j under its scenario k."""
+        a = book.to_abi()
+        t = C.c_uint64()
+        check(self.lib, self.lib.rg_server_submit_book_trade_bumps(self.handle, a.ptr,
+                                                                   C.byref(sizes) if sizes else None, C.byref(t)))
+        self._kinds[t.value] = abi.JOB_BOOK_BUMPS
+        return t.value
+
     # -------------------------------------------------------------- collection --------------
     def poll(self, ticket: int) -> abi.JobInfo:
         info = abi.JobInfo()

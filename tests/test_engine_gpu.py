@@ -317,8 +317,9 @@ def test_autotuned_tile_depth_keeps_prices(engine):
 
 @pytest.mark.parametrize("n,lv", [(3, True), (5, True), (2, False)])
 def test_every_tiled_shape_prices_identically(engine, n, lv):
-    """Paths per thread (one, or two in packed FP32x2 arithmetic), tile depth and the resulting
-    block size are schedule only: every forced shape gives the same bytes, on a ragged path count."""
+    """Paths per thread (one, or two in packed FP32x2 arithmetic), tile depth and the paths per CTA
+    tile (the block) are schedule only: every forced shape gives the same bytes, on a ragged path
+    count."""
     lib = engine.lib
     paths = (1 << 15) + 77
     if lv:
@@ -344,13 +345,14 @@ def test_every_tiled_shape_prices_identically(engine, n, lv):
         scen.append((m, [0.01 if (lv and k % 4 == 2 and i == f) else 0.0 for i in range(n)]))
     got = []
     try:
-        for ppt, tt in ((1, 24), (2, 24), (2, 48), (1, 32)):
-            abi.check(lib, lib.rg_set_tiled_shape(ppt, tt))
+        for ppt, tt, pb in ((1, 24, 0), (2, 24, 0), (2, 48, 0), (1, 32, 0), (1, 48, 32), (2, 32, 64)):
+            abi.check(lib, lib.rg_set_tiled_shape(ppt, tt, pb))
             got.append(engine.price_scenarios_raw(r, scen))
             tm = engine.last_timing()
             assert (tm.paths_per_thread, tm.tile_steps) == (ppt, tt)
+            assert tm.block * ppt == 16 * (pb or 64)  # 16 scenario slots x paths per CTA tile
     finally:
-        abi.check(lib, lib.rg_set_tiled_shape(0, 0))
+        abi.check(lib, lib.rg_set_tiled_shape(0, 0, 0))
     for g in got[1:]:
         assert [bytes(a) for a in g] == [bytes(a) for a in got[0]]
 

@@ -5,7 +5,9 @@
   at a time through a plain engine.
 * Work overlaps: with several slots, requests that were queued together run at the same time.
 * Admission by device memory: with a budget that holds one request at a time, requests never
-  overlap and all complete; a request larger than the whole budget is rejected at submission.
+  overlap and all complete; single trades pass a book that waits for memory, and the server
+  counts the wait; a request larger than the whole budget is rejected at submission.
+* Books under per-trade bump sets through the server equal the direct call.
 * Tasks: a queued request can be cancelled, a wait can time out, and stats report p50/p99.
 """
 from __future__ import annotations
@@ -119,6 +121,36 @@ def test_memory_budget_admits_one_request_at_a_time():
     spans = sorted((i.start_s, i.end_s) for i in infos)
     assert all(spans[k + 1][0] >= spans[k][1] for k in range(len(spans) - 1))
     assert all(len(r) == 4 for r in results)
+
+
+def test_small_requests_pass_a_book_waiting_for_memory():
+    books = [workloads.small_book(paths=1 << 13, n_trades=4, steps_per_year=52, fp32=True, seed=s) for s in range(2)]
+    single = workloads.lv3(paths=1 << 12, steps=63, fp32=True)
+    with Server(slots=4, memory_budget=1 << 62) as probe:
+        est = probe.wait(probe.submit_book(books[0])).device_bytes
+        small = probe.wait(probe.submit_price(single)).device_bytes
+    budget = int(est * 1.5)
+    assert small <= budget // 16
+    with Server(slots=4, memory_budget=budget) as srv:
+        tb = [srv.submit_book(b) for b in books]
+        ts = [srv.submit_price(single) for _ in range(6)]
+        books_info = [srv.wait(t) for t in tb]
+        singles_info = [srv.wait(t) for t in ts]
+        st = srv.stats()
+    assert books_info[1].start_s >= books_info[0].end_s  # the books never overlap
+    assert st.memory_waits >= 1 and st.peak_reserved_bytes <= budget
+    assert any(i.start_s < books_info[1].start_s for i in singles_info)  # singles passed the waiting book
+    assert st.completed == 8 and st.failed == 0
+
+
+def test_book_trade_bumps_through_the_server_equal_the_direct_call(engine):
+    b = workloads.small_book(paths=1 << 12, n_trades=6, steps_per_year=52, fp32=True)
+    direct = engine.price_book_trade_bumps_raw(b)
+    with Server(slots=2) as srv:
+        got = srv.results(srv.submit_book_trade_bumps(b))
+    assert len(got) == len(direct) == 6 * abi.BOOK_TRADE_SCENARIOS
+    for a, d in zip(got, direct):
+        assert bytes(a) == bytes(d)
 
 
 def test_a_request_larger_than_the_budget_is_rejected():
