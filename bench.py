@@ -155,6 +155,40 @@ def cpu_rate(paths_hint: int, steps: int, target_s: float):
     return units / dt, threads, paths, dt
 
 
+def cpu_rows(steps: int, target_s: float):
+    """The CPU rows beside the headline baseline: the oracle on one thread (the shape of the
+    reference's own single-threaded loop) on a sample of the bench workload, and the plain
+    configuration (3-asset flat-vol Phoenix, FP64, 2^16 Sobol paths x 756 steps, price only) at its
+    full size on every host thread, with the time a full-size bench workload would take."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from riga_gb300 import workloads
+
+    O.build()
+    threads = os.cpu_count() or 1
+    req, scen = workload_request(16, steps, fp32=False)
+    t0 = time.perf_counter()
+    O.price_scenarios(req, scen, threads=1)
+    per_path = (time.perf_counter() - t0) / 16.0
+    paths = int(max(16, min(1 << 20, target_s / max(per_path, 1e-9)))) // 16 * 16
+    req, scen = workload_request(paths, steps, fp32=False)
+    t0 = time.perf_counter()
+    O.price_scenarios(req, scen, threads=1)
+    dt1 = time.perf_counter() - t0
+    one = float(paths) * steps * len(scen) / dt1
+    plain = workloads.plain3(paths=1 << 16, steps=756)
+    t0 = time.perf_counter()
+    O.price_put_leg(plain, threads=threads)
+    dtp = time.perf_counter() - t0
+    return {"one_thread": {"value": one, "unit": UNIT, "cores": 1, "kind": "port",
+                           "sample": f"oracle FP64 on 1 thread, {paths} paths x {steps} steps x {len(scen)} "
+                                     f"scenarios ({dt1:.1f} s)"},
+            "plain_full_size": {"value": float(1 << 16) * 756 / dtp, "unit": UNIT, "cores": threads, "kind": "port",
+                                "wall_s": dtp,
+                                "sample": "the plain configuration at full size: 3-asset flat-vol Phoenix, FP64, "
+                                          "2^16 Sobol paths x 756 steps, price only, every host thread"}}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -450,6 +484,11 @@ def run_gpu(args):
 
     for _ in range(args.warmup):
         one_step()
+    if args.phase_clocks:
+        # the tiled kernel's per-phase CTA clock cycles over the timed steps (a library built with
+        # RG_PHASE_CLOCKS=1 only; the counters add a few instructions per phase)
+        clk4 = (C.c_uint64 * 4)()
+        abi.check(eng.lib, eng.lib.rg_phase_clocks(clk4, 1))
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -529,6 +568,12 @@ def run_gpu(args):
     }
     if merged_pv is not None:
         line["merged_base_pv"] = merged_pv
+    if args.phase_clocks:
+        abi.check(eng.lib, eng.lib.rg_phase_clocks(clk4, 0))
+        tot = float(sum(clk4)) or 1.0
+        line["phase_clocks"] = {"cycles": list(clk4), "share": {k: v / tot for k, v in zip(
+            ("generation", "bridge", "stepping", "path_close"), clk4)},
+            "note": "CTA wall clock cycles per phase of the tiled kernel over the timed steps (RG_PHASE_CLOCKS=1 build)"}
     if world == 1 and not args.no_book:
         book = book_measure(eng, args.book_trades, args.book_paths)
         plain = fp64_plain_rate(eng)
@@ -546,6 +591,12 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"oracle FP64 on {cores} host threads, {paths} paths x {T} steps "
                                           f"x {n_scen} scenarios ({dt:.1f} s)"}
+        rows = cpu_rows(T, args.cpu_seconds)
+        rows["bench_workload_at_full_size_s"] = {
+            "value": float(P) * T * n_scen / rate, "cores": cores,
+            "note": "the bench workload (all its paths and scenarios) on every host thread at the sampled rate: "
+                    "too long to run inside the bench"}
+        line["cpu_baseline_rows"] = rows
     print(json.dumps(line), flush=True)
 
 
@@ -568,6 +619,8 @@ def main():
     ap.add_argument("--book-trades", type=int, default=4096)
     ap.add_argument("--book-paths", type=int, default=1 << 18)
     ap.add_argument("--serving-seconds", type=float, default=60.0, help="window of the serving (cfg 3) run")
+    ap.add_argument("--phase-clocks", action="store_true",
+                    help="report the tiled kernel's per-phase clock cycles (needs a library built with RG_PHASE_CLOCKS=1)")
     ap.add_argument("--shape", default=None, metavar="PPT,TT[,PB]",
                     help="force the tiled FP32 kernel's paths per thread, tile depth and paths per CTA tile "
                          "(rg_set_tiled_shape) instead of autotuning them, e.g. for a profiler capture with no "

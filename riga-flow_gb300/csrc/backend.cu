@@ -8,19 +8,25 @@
 
 namespace rg {
 
-// partial[rows][S][RG_ACC] -> out[S][RG_ACC].  One CTA per scenario; thread i adds rows i, i + 256,
-// ... in order with Neumaier compensation, all RG_ACC quantities of a row at once (one 128-byte
-// line), then a pairwise tree over the threads in shared memory.  The order depends only on the
-// row count, so repeated launches — and every launch shape of the kernels that wrote the rows —
-// give the same bits.
-__global__ void __launch_bounds__(256) reduce_kernel(const double* __restrict__ partial, int rows, int S,
-                                                     double* __restrict__ out) {
+// partial[rows][S][RG_ACC] -> out[S][RG_ACC] in two fixed-order passes, so that the FP64 adds
+// spread over every SM (GB300's FP64 pipe is narrow; one CTA per scenario kept 16 SMs busy for
+// about 1 ms on 32,768 rows).  Pass 1: CTA (s, g) sums rows [g·kReduceRows, (g+1)·kReduceRows) of
+// scenario s — thread i adds rows i, i + 256, ... of the range in order with Neumaier
+// compensation, all RG_ACC quantities of a row at once (one 128-byte line), then a pairwise tree
+// over the threads in shared memory — into group row g.  Pass 2: the same over the group rows.
+// The order depends only on the row count, so repeated launches — and every launch shape of the
+// kernels that wrote the rows — give the same bits.
+constexpr int kReduceRows = 512;
+
+__global__ void __launch_bounds__(256) reduce_kernel(const double* __restrict__ partial, int rows, int per_cta,
+                                                     int S, double* __restrict__ out) {
   __shared__ double sh[RG_ACC][256];
-  const int s = blockIdx.x, tid = threadIdx.x;
+  const int s = blockIdx.x, g = blockIdx.y, tid = threadIdx.x;
+  const int r0 = g * per_cta, r1 = min(rows, r0 + per_cta);
   double sum[RG_ACC], comp[RG_ACC];
 #pragma unroll
   for (int k = 0; k < RG_ACC; ++k) sum[k] = comp[k] = 0.0;
-  for (int b = tid; b < rows; b += blockDim.x) {
+  for (int b = r0 + tid; b < r1; b += blockDim.x) {
     const double2* row = reinterpret_cast<const double2*>(partial + ((size_t)b * S + s) * RG_ACC);
 #pragma unroll
     for (int k2 = 0; k2 < RG_ACC / 2; ++k2) {
@@ -44,13 +50,25 @@ __global__ void __launch_bounds__(256) reduce_kernel(const double* __restrict__ 
       for (int k = 0; k < RG_ACC; ++k) sh[k][tid] += sh[k][tid + w];
     __syncthreads();
   }
-  if (tid < RG_ACC) out[(size_t)s * RG_ACC + tid] = sh[tid][0];
+  if (tid < RG_ACC) out[((size_t)g * S + s) * RG_ACC + tid] = sh[tid][0];
 }
 
-void launch_reduce(const double* partial, int grid, int S, double* out, cudaStream_t st) {
-  reduce_kernel<<<S, 256, 0, st>>>(partial, grid, S, out);
+int reduce_groups(int rows) { return rows > kReduceRows ? (rows + kReduceRows - 1) / kReduceRows : 0; }
+
+void launch_reduce(const double* partial, int rows, int S, double* out, cudaStream_t st) {
+  const int G = reduce_groups(rows);
+  if (G == 0) {
+    reduce_kernel<<<dim3(S, 1), 256, 0, st>>>(partial, rows, rows, S, out);
+  } else {
+    double* groups = out + (size_t)S * RG_ACC;  // the caller's reduce_scratch_doubles beyond out[S][RG_ACC]
+    reduce_kernel<<<dim3(S, G), 256, 0, st>>>(partial, rows, kReduceRows, S, groups);
+    cuda_check(cudaGetLastError(), "reduce_kernel launch");
+    reduce_kernel<<<dim3(S, 1), 256, 0, st>>>(groups, G, G, S, out);
+  }
   cuda_check(cudaGetLastError(), "reduce_kernel launch");
 }
+
+size_t reduce_scratch_doubles(int rows, int S) { return (size_t)reduce_groups(rows) * S * RG_ACC; }
 
 // ------------------------------------------------------------------ worst_of ------------------
 // o = min(a, b) elementwise (gpu.rs:28-31); float4 loads for the aligned body.

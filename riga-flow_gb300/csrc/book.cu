@@ -138,6 +138,12 @@ void plan_book(const rg_book_request* r, const BookScenarios& sc, BookPlan& B) {
   if (g.vr == RG_VR_SOBOL) {
     int64_t d = (int64_t)c.qmc_dimension;
     g.sob_dim = c.dim_mode == RG_DIM_FULL ? std::max<int64_t>(d, need) : std::min<int64_t>(std::max<int64_t>(d, 1), 512);
+  } else if (c.dim_mode == RG_DIM_FULL) {
+    // the production Halton lane: one prime per dimension, hashed affine digit scrambling, no wrap
+    const int64_t d = std::max<int64_t>((int64_t)c.qmc_dimension, need);
+    if (d > (int64_t(1) << 20)) raise(RG_ERR_UNSUPPORTED, "the full-dimension Halton lane holds at most 2^20 dimensions");
+    g.hal_dim = (int32_t)d;
+    g.hal_hash = 1;
   } else {
     g.hal_dim = (int32_t)std::min<int64_t>(std::max<int64_t>((int64_t)c.qmc_dimension, 1), 512);
   }
@@ -349,6 +355,9 @@ BookStaged stage_book_static(DevBuf& tables, cudaStream_t st, const rg_book_requ
   std::vector<uint32_t> hb, ho, hp;
   if (B.gen.vr == RG_VR_SOBOL) {
     o_sobol = pk.add(sobol_table(B.gen.sob_dim));
+  } else if (B.gen.hal_hash) {
+    o_hb = pk.add(first_primes(B.gen.hal_dim).data(), (size_t)B.gen.hal_dim);  // no permutation tables
+    o_ho = o_hp = o_hb;
   } else {
     halton_tables(B.gen.hal_dim, B.gen.seed, hb, ho, hp);
     o_hb = pk.add(hb);

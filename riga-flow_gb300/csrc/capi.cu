@@ -576,7 +576,8 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     const int grid = (int)rows;
     const size_t sums_bytes = (size_t)P.n_scen * RG_ACC * sizeof(double);
     lo.partial = static_cast<double*>(W.device(WS_PARTIAL, rows * P.n_scen * RG_ACC * sizeof(double)));
-    double* dsums = static_cast<double*>(W.device(WS_SUMS, sums_bytes));
+    double* dsums = static_cast<double*>(
+        W.device(WS_SUMS, sums_bytes + reduce_scratch_doubles(grid, P.n_scen) * sizeof(double)));
     lo.grid = grid;
     if (trace) {
       // KO trace events are recorded for the first scenario of each fused launch
@@ -667,8 +668,10 @@ size_t estimate_price_bytes(const rg_price_request* r, int n_scen) {
     if (fp32) b += surf * T * gx * 8;                                            // step rows
   }
   if (fp32) b += T * 160;  // bridge plans of the tiled kernel
-  const size_t grid = fp32 ? (size_t)device_info().sm_count * 2 : 152 * 16;
+  // rows of partial sums: one per 32-path chunk (FP32 kernels) or per block (FP64 kernel)
+  const size_t grid = fp32 ? (size_t)p32_chunks(r->config.paths) : 152 * 16;
   b += grid * std::min<size_t>(S, 32) * RG_ACC * 8 + S * RG_ACC * 8;  // partial and reduced sums
+  b += reduce_scratch_doubles((int)std::min<size_t>(grid, INT32_MAX), (int)std::min<size_t>(S, 32)) * 8;
   if (r->config.trace_level != RG_TRACE_OFF) b += (size_t)r->config.paths * 4;
   return b + b / 4 + (size_t(1) << 20);
 }

@@ -196,7 +196,7 @@ const std::vector<uint32_t>& sobol_table(int64_t dim) {
 
 // ------------------------------------------------------------------ Halton tables ------------
 // First primes and their seeded Fisher–Yates digit permutations (qmc.rs:12-22, 128-140).
-const std::vector<uint32_t>& first_primes(int count) {
+std::vector<uint32_t> first_primes(int count) {
   static std::mutex mu;
   static std::vector<uint32_t> primes;
   std::lock_guard<std::mutex> lock(mu);

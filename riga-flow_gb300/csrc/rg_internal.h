@@ -159,8 +159,8 @@ void bridge_schedule_into(int64_t T, double dt, Prepared& P);
 // The Sobol direction table for `dim` dimensions (process-wide cache).
 const std::vector<uint32_t>& sobol_table(int64_t dim);
 std::vector<double> calib_axes(const rg_implied_vol_grid& g, double spot, double rate, int gx);
-// The first `count` primes (cached process-wide; at least `count` entries).
-const std::vector<uint32_t>& first_primes(int count);
+// The first `count` primes (a copy of a process-wide cache; at least `count` entries).
+std::vector<uint32_t> first_primes(int count);
 // Halton bases and permutations.
 void halton_tables(int dim, uint64_t seed, std::vector<uint32_t>& base, std::vector<uint32_t>& off,
                    std::vector<uint32_t>& perm);
@@ -281,7 +281,10 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
                       const DevScen32* scen32_dev, uint64_t path0, uint64_t npaths,
                       const Fp32Shape& shape, const LaunchOut& out, cudaStream_t s);
-void launch_reduce(const double* partial, int grid, int n_scen, double* out, cudaStream_t s);
+// out[S][RG_ACC] = Σ over rows of partial[rows][S][RG_ACC] in a fixed order; `out` must hold
+// reduce_scratch_doubles(rows, S) more doubles after its S·RG_ACC (the first pass's group sums).
+void launch_reduce(const double* partial, int rows, int n_scen, double* out, cudaStream_t s);
+size_t reduce_scratch_doubles(int rows, int n_scen);
 
 // The 32-bit Sobol integers at which the inverse normal switches between its central and tail
 // branches (computed in FP64 so the FP32 kernels branch exactly as the reference does).
