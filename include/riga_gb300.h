@@ -492,6 +492,9 @@ typedef struct rg_server_config {
   int32_t max_large_slots;       /* slots large requests may hold at once; 0 = half the slots */
   uint64_t large_work;           /* paths × steps × scenarios (summed over a book's trades, plus its
                                     universe generation) at which a request is large; 0 = 2^31 */
+  int32_t large_max_sms;         /* SMs a large request's kernels are sized for, leaving the rest to
+                                    small requests, whose streams also have the highest priority;
+                                    0 = two thirds of the SMs, negative = all */
 } rg_server_config;
 
 enum { RG_JOB_QUEUED = 0, RG_JOB_RUNNING = 1, RG_JOB_DONE = 2, RG_JOB_FAILED = 3, RG_JOB_CANCELLED = 4 };

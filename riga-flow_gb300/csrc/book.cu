@@ -544,7 +544,10 @@ void run_book(rg_engine* E, const rg_book_request* r, const BookScenarios& sc, r
   const uint64_t P = records ? count : r->config.paths;
   cudaStream_t s0 = E->stream, s1 = E->gen_stream;
   if (fp32) {
-    const Book32Shape sh = book32_shape(B.S, device_sm_count(), P, B.min_group());
+    // the path blocks (hence the sums) follow the device's SM count; the persistent scans' grid
+    // follows the engine's SM cap
+    Book32Shape sh = book32_shape(B.S, device_sm_count(), P, B.min_group());
+    sh.grid = std::min(sh.grid, book32_shape(B.S, engine_sm_count(E), P, B.min_group()).grid);
     const uint64_t PC = chunk_paths(P, B.U, B.TU, sizeof(float), (uint64_t)sh.blk_paths);
     const uint64_t n_chunks = (P + PC - 1) / PC;
     const uint64_t blocks_per_chunk = (PC + sh.blk_paths - 1) / sh.blk_paths;

@@ -168,8 +168,14 @@ extern "C" int32_t rg_engine_create(int32_t device, rg_engine** out) {
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     std::unique_ptr<rg_engine> e(new rg_engine());
     e->device = device;
-    cuda_check(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    cuda_check(cudaStreamCreateWithFlags(&e->gen_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&e->stream_lo, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithFlags(&e->gen_stream_lo, cudaStreamNonBlocking), "cudaStreamCreate");
+    int least = 0, greatest = 0;
+    cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    cuda_check(cudaStreamCreateWithPriority(&e->stream_hi, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    cuda_check(cudaStreamCreateWithPriority(&e->gen_stream_hi, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    e->stream = e->stream_lo;
+    e->gen_stream = e->gen_stream_lo;
     for (cudaEvent_t& ev : e->ev) cuda_check(cudaEventCreate(&ev), "cudaEventCreate");
     for (cudaEvent_t& ev : e->book_ev)
       cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
@@ -179,14 +185,11 @@ extern "C" int32_t rg_engine_create(int32_t device, rg_engine** out) {
 
 extern "C" void rg_engine_destroy(rg_engine* e) {
   if (!e) return;
-  if (e->stream) {
-    cudaStreamSynchronize(e->stream);
-    cudaStreamDestroy(e->stream);
-  }
-  if (e->gen_stream) {
-    cudaStreamSynchronize(e->gen_stream);
-    cudaStreamDestroy(e->gen_stream);
-  }
+  for (cudaStream_t s : {e->stream_lo, e->gen_stream_lo, e->stream_hi, e->gen_stream_hi})
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
   for (cudaEvent_t ev : e->ev)
     if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t ev : e->book_ev)
@@ -279,7 +282,6 @@ void SurfaceCache::release() {
 static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   Pack pk;
   const DevTrade& tr = P.trade;
-  const int64_t T = P.T;
   // QMC tables
   size_t o_sobol = 0, o_hb = 0, o_ho = 0, o_hp = 0;
   std::vector<uint32_t> hb, ho, hp;
@@ -307,6 +309,17 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
   if (req->config.precision == RG_PRECISION_FP32) {
     bp = p32_bridge_plans(P);
     o_bplan = pk.add(bp->words);
+  }
+  // the FP32 kernels' consumption-order Sobol tables (1.1 MB per 1,000 steps of 3 assets), for
+  // launches long enough that generating from them pays for their upload
+  size_t o_sobt = 0, o_slut = 0;
+  int32_t lut_o = -1;
+  if (req->config.precision == RG_PRECISION_FP32 && tr.vr == RG_VR_SOBOL && req->config.paths >= (uint64_t(1) << 16)) {
+    lut_o = (int32_t)((req->config.first_path + 1) & 31);
+    std::shared_ptr<const SobolLut> t =
+        sobol_lut_tables(P, tr.sob_dim, (uint32_t)lut_o, tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT);
+    o_sobt = pk.add(t->st);
+    o_slut = pk.add(t->lut);
   }
   size_t o_scen = pk.add(P.scen), o_s32 = pk.add(P.scen32);
   // local-vol surfaces: inputs (grids) and outputs
@@ -426,6 +439,10 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
     tb.bplan_at[i] = i < tb.n_bplan ? bp->at[i] : 0;
   }
   tb.lv_nt = P.lv_nt_max;
+  tb.sob_t = lut_o >= 0 ? reinterpret_cast<const uint32_t*>(base + o_sobt) : nullptr;
+  tb.sob_lut = lut_o >= 0 ? reinterpret_cast<const uint32_t*>(base + o_slut) : nullptr;
+  tb.sob_nq = (int32_t)(P.T * P.n);
+  tb.sob_lut_o = lut_o;
   S.scen = reinterpret_cast<DevScenario*>(base + o_scen);
   S.scen32 = reinterpret_cast<DevScen32*>(base + o_s32);
   if (tr.has_lv) {
@@ -585,7 +602,7 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
     }
     const uint64_t path0 = req->config.first_path;
     if (fp32) {
-      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.may_tune(), W.stream);
+      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.may_tune(), W.sm_count, W.stream);
       launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, paths, sh, lo, W.stream);
     } else {
       launch_phoenix64(P, S.tb, S.scen, path0, paths, lo, W.stream);
@@ -629,6 +646,18 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
 
 int device_sm_count() { return device_info().sm_count; }
 
+int engine_sm_count(const rg_engine* E) {
+  const int sms = device_info().sm_count;
+  return E->sm_cap > 0 && E->sm_cap < sms ? E->sm_cap : sms;
+}
+
+void engine_set_class(rg_engine* E, bool high_priority, int sm_cap) {
+  std::lock_guard<std::mutex> lock(E->mu);
+  E->stream = high_priority ? E->stream_hi : E->stream_lo;
+  E->gen_stream = high_priority ? E->gen_stream_hi : E->gen_stream_lo;
+  E->sm_cap = sm_cap;
+}
+
 // The engine's workspace: growable device buffers, pinned host sums, timing events.
 struct EngineWorkspace : Workspace {
   rg_engine* E;
@@ -636,7 +665,7 @@ struct EngineWorkspace : Workspace {
     stream = e->stream;
     ev = e->ev;
     timing = &e->timing;
-    sm_count = device_info().sm_count;
+    sm_count = engine_sm_count(e);
   }
   void* device(int slot, size_t bytes) override {
     E->bufs[slot].ensure(bytes);
@@ -917,14 +946,15 @@ static void run_path_range(rg_engine* e, const rg_price_request* req, uint64_t f
     LaunchOut lo{};
     lo.mcz = mcz;
     Fp32Shape sh{};
-    if (fp32) sh = phoenix32_shape(P, m, device_info().sm_count);
+    if (fp32) sh = phoenix32_shape(P, m, engine_sm_count(e));
     lo.grid = fp32 ? (int)p32_chunks(m) : phoenix64_grid(P, m);
     lo.partial = static_cast<double*>(W.device(WS_PARTIAL, (size_t)lo.grid * P.n_scen * RG_ACC * sizeof(double)));
     if (out) lo.records = static_cast<rg_path_record*>(W.device(WS_RECORDS, m * sizeof(rg_path_record)));
     if (cube) lo.cube = static_cast<float*>(W.device(WS_CUBE, m * cube_row * sizeof(float)));
     const uint64_t path0 = req->config.first_path + first + done;
     if (fp32) {
-      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, false, e->stream);  // cached depth only
+      sh = phoenix32_tune(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, false, engine_sm_count(e),
+                          e->stream);  // cached shape only
       launch_phoenix32(P, S.tb, S.scen, S.scen32, path0, m, sh, lo, e->stream);
     }
     else

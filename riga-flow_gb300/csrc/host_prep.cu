@@ -194,6 +194,48 @@ const std::vector<uint32_t>& sobol_table(int64_t dim) {
   return cache.emplace(dim, std::move(v)).first->second;
 }
 
+// The FP32 kernels' Sobol tables (phoenix32.cu, phoenix32d.cu), in consumption order
+// q = node·n + factor with row(q) = nf_row[q]: st[k][q] = v[row(q)][k], and lut[q][j] for the lane
+// j whose point is n1 + j, n1 = a + o with a a multiple of 32.  Gray codes are linear over XOR, so
+// for o + j < 32 x(n1 + j) = X(gray(a)) ^ X(gray(o + j)), and otherwise
+// x = X(gray(a + 32)) ^ X(gray(o + j - 32)) with X(gray(a + 32)) = X(gray(a)) ^ v[4] ^
+// v[ctz(a/32 + 1) + 5]; lut holds the lane's low-bit term X(gray((o + j) mod 32)) — with v[4] for
+// the upper lanes and the digital shift folded in — and the kernels add the 32-path group's
+// high-bit terms.
+std::shared_ptr<const SobolLut> sobol_lut_tables(const Prepared& P, int64_t sob_dim, uint32_t o, bool shift) {
+  // nf_row depends on (directions, assets, steps) and nf_shift on the seed as well
+  const std::vector<int64_t> key{sob_dim, P.n, P.T, (int64_t)P.trade.seed, shift ? 1 : 0, (int64_t)o};
+  static std::mutex mu;
+  static std::map<std::vector<int64_t>, std::shared_ptr<const SobolLut>> cache;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const std::vector<uint32_t>& v = sobol_table(sob_dim);
+  auto out = std::make_shared<SobolLut>();
+  const size_t nq = (size_t)P.T * (size_t)P.n;
+  out->st.assign(32 * nq, 0u);
+  out->lut.assign(nq * 32, 0u);
+  for (size_t q = 0; q < nq; ++q) {
+    const uint32_t* row = v.data() + 32 * (size_t)P.nf_row[q];
+    for (int k = 0; k < 32; ++k) out->st[(size_t)k * nq + q] = row[k];
+    for (uint32_t j = 0; j < 32; ++j) {
+      const uint32_t jj = (o + j) & 31u, g = jj ^ (jj >> 1);
+      uint32_t x = 0;
+      for (int k = 0; k < 5; ++k)
+        if ((g >> k) & 1u) x ^= row[k];
+      if (o + j >= 32u) x ^= row[4];
+      if (shift) x ^= P.nf_shift[q];
+      out->lut[q * 32 + j] = x;
+    }
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() >= 32) cache.clear();  // bounded: one entry per launch shape in use
+  cache[key] = out;
+  return out;
+}
+
 // ------------------------------------------------------------------ Halton tables ------------
 // First primes and their seeded Fisher–Yates digit permutations (qmc.rs:12-22, 128-140).
 std::vector<uint32_t> first_primes(int count) {

@@ -222,6 +222,10 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   }
   const float* __restrict__ dfs = tb.df_f + (size_t)ss * T;
 
+  // Sobol points from the staged consumption-order tables (as phoenix32d.cu) when they were built
+  // for this launch's offset within a 32-point block; a lane's point may lie in the next block
+  const bool sob_lut = tr.vr == RG_VR_SOBOL && tb.sob_lut != nullptr && (int32_t)((path0 + 1) & 31) == tb.sob_lut_o;
+  const bool upper = (uint32_t)tb.sob_lut_o + (uint32_t)lane >= 32u;
   RG_PHASE_BEGIN();
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -277,6 +281,31 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
           s_poff[i] = i == 0 ? NNmax * zs : (int)__ldg(plan + steps_base + t0 + i - 1) * zs;
         for (int i = tid; i < (int)stk_cnt; i += blockDim.x) s_pstk[i] = __ldg(plan + stk_base + i);
       }
+      // the high-bit Sobol terms X(gray(a)) of every (32-path group, tile dimension q), in the dW
+      // region (free until the bridge phase): rows [group][block 0 / next block][q], q = jj·N + f;
+      // a warp item is (group, 32 consecutive q), one coalesced row of transposed directions per
+      // set bit of the group's gray(a)
+      const int nq = nn * N, hs = ((nq + 31) & ~31) + 1;
+      const bool lut_tile = sob_lut && ngrp * 2 * hs <= TT * dws;
+      uint32_t* s_hq = reinterpret_cast<uint32_t*>(dW);
+      if (lut_tile) {
+        const int nb = (nq + 31) >> 5;
+        for (int it = wid; it < ngrp * nb; it += nwarp) {
+          const int hh = it / nb, ql = ((it - hh * nb) << 5) + lane;
+          const uint64_t n1 = path0 + tile0 + ((uint64_t)hh << 5) + 1;
+          const uint64_t a = n1 & ~(uint64_t)31;
+          const uint32_t ga = (uint32_t)(a ^ (a >> 1));
+          const int cw = __ffsll((long long)((n1 >> 5) + 1)) - 1 + 5;
+          if (ql < nq) {
+            const int q = n0 * N + ql;
+            uint32_t h = 0;
+            for (uint32_t g = ga; g; g &= g - 1u) h ^= __ldg(tb.sob_t + (size_t)(__ffs(g) - 1) * tb.sob_nq + q);
+            s_hq[(hh * 2) * hs + ql] = h;
+            s_hq[(hh * 2 + 1) * hs + ql] = h ^ __ldg(tb.sob_t + (size_t)cw * tb.sob_nq + q);
+          }
+        }
+        __syncthreads();
+      }
       {
         // kGB items per warp at a time in straight-line code, so that their global loads, shuffles
         // and inverse normals overlap; a warp's surplus slots recompute its last item (the same
@@ -292,7 +321,24 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
             jj[u] = it >> lg_ngrp;
             hh[u] = it & (ngrp - 1);
           }
-          if (shift_lane) {
+          if (lut_tile) {
+            // x = the group's high-bit term (this lane's block) ^ the lane's low-bit term, with the
+            // digital shift folded into the low-bit table
+            uint32_t xs[kGB][N];
+#pragma unroll
+            for (int u = 0; u < kGB; ++u) {
+              const int hb = (hh[u] * 2 + (upper ? 1 : 0)) * hs + jj[u] * N;
+              const uint32_t* lt = tb.sob_lut + (size_t)(n0 + jj[u]) * N * 32 + lane;
+#pragma unroll
+              for (int f = 0; f < N; ++f) xs[u][f] = s_hq[hb + f] ^ __ldg(lt + f * 32);
+            }
+#pragma unroll
+            for (int u = 0; u < kGB; ++u)
+#pragma unroll
+              for (int f = 0; f < N; ++f)
+                Z[(size_t)jj[u] * zs + f * (Pb + 4) + (hh[u] << 5) + lane] =
+                    rg_probit32(shift_lane ? xs[u][f] : rg_owen(xs[u][f], (uint64_t)s_nodek[jj[u]] * N + f, tr.seed));
+          } else if (shift_lane) {
             uint32_t xs[kGB][N];
 #pragma unroll
             for (int u = 0; u < kGB; ++u) {
@@ -852,13 +898,11 @@ void p32_force_shape(int ppt, int tt, int pb) {
 // tile and half of it (two smaller CTAs per SM where they fit).
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
-                         const LaunchOut& out, bool may_tune, cudaStream_t st) {
+                         const LaunchOut& out, bool may_tune, int sm_count, cudaStream_t st) {
   if (sh.direct) return sh;
   int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-  int sm_count = 0;
-  cuda_check(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev), "SM count");
-  const std::vector<int64_t> key{dev, P.n, P.trade.has_lv, P.n_scen, sh.Sb, P.T, P.stack_max,
+  const std::vector<int64_t> key{dev, sm_count, P.n, P.trade.has_lv, P.n_scen, sh.Sb, P.T, P.stack_max,
                                  P.trade.vr, P.trade.scrambler, P.trade.gx};
   auto apply = [&](TiledKnobs c, uint64_t paths) {
     Fp32Shape t = sh;

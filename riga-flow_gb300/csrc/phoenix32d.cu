@@ -8,10 +8,15 @@
 // tiled kernel wins with two or more scenarios, and below about 2^18 paths, where one path per
 // thread leaves too few warps to hide the per-step latency.)  Here a warp walks 32 consecutive
 // paths of one scenario through time:
-//   * Sobol points by warp cooperation: x(n) for the warp's first point is the XOR of the
-//     direction numbers at the set bits of its Gray code (lane k contributes bit k, a shuffle
-//     reduction), and the other lanes' points follow by the Gray recurrence
-//     x(n) = x(n-1) ^ v[ctz(n)] as an inclusive XOR scan over the lanes;
+//   * Sobol points from consumption-order tables staged for the launch (host_prep.cu,
+//     direct_sobol_tables): the warp's 32 points lie in at most two aligned 32-point blocks, and
+//     Gray codes are linear over XOR, so a point is the block's high-bit term X(gray(a)) — one
+//     coalesced row of transposed directions per set bit of gray(a), for a batch of the next
+//     32 / N nodes' dimensions at once, kept in shared memory — XOR the lane's low-bit term, one
+//     coalesced 128-byte row per dimension; without the tables (another offset within a block),
+//     by warp cooperation: x(n) for the warp's first point as a shuffle reduction over the set bits
+//     of its Gray code, and the Gray recurrence x(n) = x(n-1) ^ v[ctz(n)] as an XOR scan over the
+//     lanes;
 //   * the digital shift (or Owen scramble) and the FP32 inverse normal of rg_common.cuh;
 //   * the streamed Brownian bridge per factor with its anchor stack in shared memory, laid out
 //     [depth][factor][thread] so that a warp's accesses (the depth is warp-uniform) hit 32 banks;
@@ -39,6 +44,9 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     uint64_t npaths, double* __restrict__ partial, int32_t* __restrict__ ko_steps,
     rg_path_record* __restrict__ records) {
   __shared__ float4 s_lv[32 * RG_NMAX];
+  // per warp: the high-bit Sobol terms of a batch of consumption indices q (q0 + l for lane l):
+  // [0, 32) for lanes whose point lies in the warp's first 32-point block, [33, 65) for the next
+  __shared__ uint32_t s_hi[P32D_WARPS][66];
   extern __shared__ float s_stk[];  // [stack depth][N][P32D_THREADS]
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
   const int T = (int)tr.steps;
@@ -75,10 +83,18 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
   __syncthreads();
 
   const uint64_t groups = (npaths + 31) / 32;
+  // Sobol points from the staged consumption-order tables when they were built for this launch's
+  // offset within a 32-point block (else the warp cooperation of rg_warp_sobol)
+  const bool lut = tr.vr == RG_VR_SOBOL && tb.sob_lut != nullptr && (int32_t)((path0 + 1) & 31) == tb.sob_lut_o;
+  const bool upper = (uint32_t)tb.sob_lut_o + (uint32_t)lane >= 32u;  // point in the next 32-block
+  constexpr int kNb = 32 / N;  // nodes per batch of high-bit terms
   for (uint64_t grp = (uint64_t)(gw / S); grp < groups; grp += (uint64_t)(nw / S)) {
     const uint64_t gi = grp * 32 + lane;
     const bool ok = gi < npaths;
     const uint64_t n1 = path0 + grp * 32 + 1;  // Sobol point of the warp's first path
+    const uint32_t ga = (uint32_t)((n1 & ~(uint64_t)31) ^ ((n1 & ~(uint64_t)31) >> 1));  // gray(a)
+    const int cw = __ffsll((long long)((n1 >> 5) + 1)) - 1 + 5;  // a / 32 + 1: its lowest set bit + 5
+    int cb = -kNb;  // first node of the batch in s_hi
     float x[N], wcur[N];
     float* const stk = s_stk + tid;  // entry (depth d, factor f) at stk[(d * N + f) * P32D_THREADS]
 #pragma unroll
@@ -95,7 +111,30 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
       for (int c = c0; c < c1; ++c) {
         const float cf = __ldg(tb.node_cf + c);
         float zf[N];
-        if (tr.vr == RG_VR_SOBOL) {
+        if (lut) {
+          if (c >= cb + kNb) {
+            // the high-bit terms X(gray(a)) of q = c·N .. (c + kNb)·N - 1, lane l holding q0 + l:
+            // one coalesced row of transposed directions per set bit of gray(a)
+            cb = c;
+            __syncwarp();  // every lane has read the previous batch
+            const int q = c * N + lane;
+            if (lane < kNb * N && q < tb.sob_nq) {
+              uint32_t h = 0;
+              for (uint32_t g = ga; g; g &= g - 1u) h ^= __ldg(tb.sob_t + (size_t)(__ffs(g) - 1) * tb.sob_nq + q);
+              s_hi[wib][lane] = h;
+              s_hi[wib][33 + lane] = h ^ __ldg(tb.sob_t + (size_t)cw * tb.sob_nq + q);
+            }
+            __syncwarp();
+          }
+          const int hb = (c - cb) * N + (upper ? 33 : 0);
+#pragma unroll
+          for (int f = 0; f < N; ++f) {
+            const uint32_t xs = s_hi[wib][hb + f] ^ __ldg(tb.sob_lut + ((size_t)c * N + f) * 32 + lane);
+            zf[f] = rg_probit32(tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT
+                                    ? xs
+                                    : rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed));
+          }
+        } else if (tr.vr == RG_VR_SOBOL) {
 #pragma unroll
           for (int f = 0; f < N; ++f) {
             const uint32_t xs = rg_warp_sobol(tb.sobol + 32 * (size_t)__ldg(tb.nf_row + c * N + f), n1, lane);

@@ -86,6 +86,12 @@ struct DevTables {
   const float* df_f;
   const float* df_mat_f;
   int32_t lv_nt;
+  // the direct FP32 kernel's Sobol tables in consumption order q = node·n + factor (phoenix32d.cu):
+  // directions transposed [32][n·T], and per q the 32 lanes' low-bit terms for points starting at
+  // offset sob_lut_o within a 32-point block (digital shift folded in); null when not staged
+  const uint32_t* sob_t;
+  const uint32_t* sob_lut;
+  int32_t sob_nq, sob_lut_o;
   // level-ordered bridge plans of the FP32 tiled kernel (phoenix32.cu), one per tile depth
   const uint32_t* bplan;
   int32_t bplan_tt[RG_BPLAN_MAX], bplan_at[RG_BPLAN_MAX];
@@ -228,7 +234,9 @@ __device__ __forceinline__ uint32_t rg_sobol_scrambled(const DevTrade& tr, const
 __host__ __device__ __forceinline__ uint64_t rg_halton_key(uint64_t seed, uint64_t dim) {
   return seed ^ ((dim + 1) * 0xA0761D6478BD642FULL);
 }
-__host__ __device__ __forceinline__ double rg_halton_hashed_u(uint32_t n, uint32_t b, uint64_t key) {
+// The scrambled radical inverse as the exact fraction R / Bk (Bk = b^k, k the point's digit count).
+__host__ __device__ __forceinline__ void rg_halton_hashed_rb(uint32_t n, uint32_t b, uint64_t key, uint64_t& R_,
+                                                             uint64_t& Bk_) {
   uint64_t R = 0, Bk = 1;
   for (uint32_t i = 0; n; ++i) {
     const uint32_t q = n / b, d = n - q * b;
@@ -240,7 +248,23 @@ __host__ __device__ __forceinline__ double rg_halton_hashed_u(uint32_t n, uint32
     Bk *= b;
     n = q;
   }
+  R_ = R;
+  Bk_ = Bk;
+}
+__host__ __device__ __forceinline__ double rg_halton_hashed_u(uint32_t n, uint32_t b, uint64_t key) {
+  uint64_t R, Bk;
+  rg_halton_hashed_rb(n, b, key, R, Bk);
   return (double)R / (double)Bk;
+}
+
+// The FP32 inverse normal of u = R / Bk: the lower-tail probability min(R, Bk - R) / Bk formed in
+// FP32 from the exact integers (no FP64 division), clamped below at the reference's 1e-12, and the
+// sign by symmetry (as rg_probit32).
+__device__ __forceinline__ float rg_probit32_frac(uint64_t R, uint64_t Bk) {
+  const bool lower = 2 * R < Bk;
+  const float p = fmaxf(__fdiv_rn((float)(lower ? R : Bk - R), (float)Bk), 1.0e-12f);
+  const float z = normcdfinvf(p);
+  return lower ? z : -z;
 }
 
 // FP64 normal of the QMC lanes (Ladder::normal, qmc.rs:119-125, 284-289).
@@ -263,10 +287,10 @@ __device__ __forceinline__ double rg_qmc_normal64(const DevTrade& tr, const DevT
 // The scrambled Halton normal of the FP32 lanes.  The reference's permuted radical inverse
 // (qmc.rs:143-153) is the sum over the k digits d_i of the point (least significant first) of
 // perm[d_i] / b^(i+1); here it is accumulated exactly as the integer R = Σ perm[d_i] b^(k-1-i)
-// (Horner over the digits, 32-bit divisions) over b^k, so the only FP64 operation is one
-// division; then the FP32 inverse normal (as rg_probit32) of the lower-tail probability
-// min(u, 1 - u) taken in FP64, which the reference's clamp of u to [1e-12, 1 - 1e-12] bounds
-// below by 1e-12.  The FP64 parity lane keeps the reference's own accumulation (rg_halton_u).
+// (Horner over the digits, 32-bit divisions) over b^k; then the FP32 inverse normal of the
+// lower-tail probability min(R, b^k - R) / b^k (rg_probit32_frac: no FP64 operation), clamped
+// below at 1e-12 as the reference's clamp of u to [1e-12, 1 - 1e-12].  The FP64 parity lane keeps
+// the reference's own accumulation (rg_halton_u).
 __device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, const uint32_t* __restrict__ perm) {
   uint64_t R = 0, Bk = 1;
   while (n) {
@@ -275,9 +299,7 @@ __device__ __forceinline__ float rg_halton_normal32(uint32_t n, uint32_t b, cons
     Bk *= b;
     n = q;
   }
-  const double u = (double)R / (double)Bk;
-  const float z = normcdfinvf((float)fmax(fmin(u, 1.0 - u), 1.0e-12));
-  return u < 0.5 ? z : -z;
+  return rg_probit32_frac(R, Bk);
 }
 
 // FP32 normal of the QMC lanes.
@@ -288,9 +310,9 @@ __device__ __forceinline__ float rg_qmc_normal32(const DevTrade& tr, const DevTa
     return rg_probit32(x);
   }
   if (tr.hal_hash) {
-    const double u = rg_halton_hashed_u((uint32_t)(point + 1), __ldg(tb.hal_base + dim), rg_halton_key(tr.seed, dim));
-    const float z = normcdfinvf((float)fmax(fmin(u, 1.0 - u), 1.0e-12));
-    return u < 0.5 ? z : -z;
+    uint64_t R, Bk;
+    rg_halton_hashed_rb((uint32_t)(point + 1), __ldg(tb.hal_base + dim), rg_halton_key(tr.seed, dim), R, Bk);
+    return rg_probit32_frac(R, Bk);
   }
   const uint32_t idx = (uint32_t)(dim % (uint64_t)tr.hal_dim);
   return rg_halton_normal32((uint32_t)(point + 1), __ldg(tb.hal_base + idx), tb.hal_perm + __ldg(tb.hal_off + idx));

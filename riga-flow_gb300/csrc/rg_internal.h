@@ -159,6 +159,14 @@ void bridge_schedule_into(int64_t T, double dt, Prepared& P);
 // The Sobol direction table for `dim` dimensions (process-wide cache).
 const std::vector<uint32_t>& sobol_table(int64_t dim);
 std::vector<double> calib_axes(const rg_implied_vol_grid& g, double spot, double rate, int gx);
+// The FP32 kernels' consumption-order Sobol tables for points starting at offset o within a
+// 32-point block (host_prep.cu): transposed directions st[32][n·T] and the lanes' low-bit terms
+// lut[n·T][32]; built once per (directions, assets, steps, seed, scrambler, o) and shared
+// process-wide.
+struct SobolLut {
+  std::vector<uint32_t> st, lut;
+};
+std::shared_ptr<const SobolLut> sobol_lut_tables(const Prepared& P, int64_t sob_dim, uint32_t o, bool shift);
 // The first `count` primes (a copy of a process-wide cache; at least `count` entries).
 std::vector<uint32_t> first_primes(int count);
 // Halton bases and permutations.
@@ -277,7 +285,7 @@ void p32_force_shape(int ppt, int tt, int pb);
 int p32_phase_clocks(unsigned long long out[4], bool reset);
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
-                         const LaunchOut& out, bool may_tune, cudaStream_t st);
+                         const LaunchOut& out, bool may_tune, int sm_count, cudaStream_t st);
 void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario* scen_dev,
                       const DevScen32* scen32_dev, uint64_t path0, uint64_t npaths,
                       const Fp32Shape& shape, const LaunchOut& out, cudaStream_t s);
@@ -388,6 +396,11 @@ namespace rg {
 // Device bytes an engine's workspace holds, and releasing them (the engine must be idle).
 size_t engine_device_bytes(rg_engine* E);
 void engine_trim(rg_engine* E);
+// Before a request on an idle engine: its streams' priority (high or default) and the SMs its
+// grids are sized for (0: all), so a server's large requests leave SMs and priority to small ones.
+void engine_set_class(rg_engine* E, bool high_priority, int sm_cap);
+// The SM count the engine's launches size their grids for.
+int engine_sm_count(const rg_engine* E);
 // Device bytes one call will hold at its peak (workspace buffers; upper estimates).
 size_t estimate_price_bytes(const rg_price_request* r, int n_scen);
 size_t estimate_book_bytes(const rg_book_request* r, int n_scen);
@@ -399,6 +412,11 @@ struct rg_engine {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t gen_stream = nullptr;  // book path generation, overlapped with the scan
+  // the two stream pairs stream/gen_stream point to: default priority (direct calls and a server's
+  // large requests) and the device's highest priority (a server's small requests)
+  cudaStream_t stream_lo = nullptr, gen_stream_lo = nullptr;
+  cudaStream_t stream_hi = nullptr, gen_stream_hi = nullptr;
+  int sm_cap = 0;  // SMs the engine's grids are sized for (0: every SM of the device)
   std::mutex mu;
   rg::DevBuf bufs[rg::WS_NSLOTS];
   rg::DevBuf book_bufs[8];

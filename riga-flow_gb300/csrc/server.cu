@@ -173,6 +173,7 @@ struct Slot {
   size_t held = 0;      // device bytes the engine's workspace holds
   size_t running = 0;   // estimate of the request it runs (0 when idle)
   bool busy = false;
+  bool trimming = false;  // another worker releases this idle engine's buffers (outside the lock)
 };
 
 }  // namespace
@@ -196,6 +197,7 @@ struct rg_server {
   double busy_s = 0, busy_since = 0;
   int max_large = 1;        // slots large requests may hold at once
   double large_work = 0;    // work at which a request counts as large
+  int large_sms = 0;        // SMs a large request's grids are sized for (0: all)
   int n_large = 0;          // large requests running
   uint64_t memory_waits = 0;  // requests that waited at the head of the queue for device memory
   size_t peak_reserved = 0;   // largest reservation (the slots' holdings and running estimates)
@@ -214,18 +216,25 @@ size_t reserved(const rg_server* S) {
   return b;
 }
 
-// Under S->mu: whether `job` can start on slot k now; may release idle slots' buffers.
-bool admit(rg_server* S, int k, const Job* job) {
-  auto need = [&]() { return reserved(S) - S->slots[k].held + std::max(S->slots[k].held, job->est); };
+// Under S->mu: whether `job` can start on slot k now, counting as free the buffers of the idle
+// slots listed in `trim` (the smallest set, in slot order, that makes room).  Releasing buffers
+// (cudaFree) waits for the device, so the caller does it after dropping the lock.
+bool admit(rg_server* S, int k, const Job* job, std::vector<int>& trim) {
+  trim.clear();
+  size_t freed = 0;
+  auto need = [&]() {
+    return reserved(S) - freed - S->slots[k].held + std::max(S->slots[k].held, job->est);
+  };
   if (need() <= S->budget) return true;
   for (size_t i = 0; i < S->slots.size(); ++i) {
-    Slot& s = S->slots[i];
-    if (s.busy || s.held == 0) continue;
-    engine_trim(s.engine);
-    s.held = 0;
+    const Slot& s = S->slots[i];
+    if ((int)i == k || s.busy || s.trimming || s.held == 0) continue;
+    trim.push_back((int)i);
+    freed += s.held;
     if (need() <= S->budget) return true;
   }
-  return need() <= S->budget;
+  trim.clear();
+  return false;
 }
 
 void run_job(rg_engine* E, Job* job) {
@@ -261,12 +270,25 @@ void run_job(rg_engine* E, Job* job) {
 // except that a large one waiting for a large slot is passed, and one that does not fit the memory
 // budget is passed only by requests of at most a sixteenth of the budget (later requests with larger
 // estimates never overtake it on memory).
-Job* next_job(rg_server* S, int k) {
+// A request larger than a sixteenth of the budget goes to an idle slot whose buffers already hold
+// most of its estimate (80%; estimates are upper bounds) when there is one, so that no buffers are
+// released and allocated again.
+Job* next_job(rg_server* S, int k, std::vector<int>& trim) {
+  if (S->slots[k].trimming) return nullptr;
   bool waiting = false;  // an earlier request waits for memory
   for (Job* j : S->queue) {
     if (j->large && S->n_large >= S->max_large) continue;
     if (waiting && j->est > S->budget / 16) continue;
-    if (admit(S, k, j)) return j;
+    auto holds = [&](const Slot& s) { return s.held / 4 >= j->est / 5; };
+    if (j->est > S->budget / 16 && !holds(S->slots[k])) {
+      bool other = false;
+      for (size_t i = 0; i < S->slots.size(); ++i) {
+        const Slot& s = S->slots[i];
+        other = other || ((int)i != k && !s.busy && !s.trimming && holds(s));
+      }
+      if (other) continue;  // left to that slot's worker
+    }
+    if (admit(S, k, j, trim)) return j;
     if (!j->waited_memory) {
       j->waited_memory = true;
       ++S->memory_waits;
@@ -278,11 +300,12 @@ Job* next_job(rg_server* S, int k) {
 
 void worker(rg_server* S, int k) {
   std::unique_lock<std::mutex> lock(S->mu);
+  std::vector<int> trim;
   for (;;) {
     Job* job = nullptr;
     S->cv_work.wait(lock, [&] {
       if (S->stopping) return true;
-      job = next_job(S, k);
+      job = next_job(S, k, trim);
       return job != nullptr;
     });
     if (S->stopping) return;
@@ -291,6 +314,10 @@ void worker(rg_server* S, int k) {
     Slot& slot = S->slots[k];
     slot.busy = true;
     slot.running = job->est;
+    for (int i : trim) {  // counted free from now on; released below, outside the lock
+      S->slots[i].trimming = true;
+      S->slots[i].held = 0;
+    }
     S->peak_reserved = std::max(S->peak_reserved, reserved(S));
     job->state = RG_JOB_RUNNING;
     job->slot = k;
@@ -299,6 +326,16 @@ void worker(rg_server* S, int k) {
     // the head may have changed: let another idle worker look at the new head
     S->cv_work.notify_all();
     lock.unlock();
+    if (!trim.empty()) {
+      for (int i : trim) engine_trim(S->slots[i].engine);
+      lock.lock();
+      for (int i : trim) S->slots[i].trimming = false;
+      S->cv_work.notify_all();
+      lock.unlock();
+    }
+    // large requests run at default priority on a share of the SMs; small ones at the highest
+    // priority on all of them, so they pass a large request's kernels
+    engine_set_class(slot.engine, !job->large, job->large ? S->large_sms : 0);
     run_job(slot.engine, job);
     const size_t held = engine_device_bytes(slot.engine);
     lock.lock();
@@ -393,6 +430,12 @@ extern "C" int32_t rg_server_create(const rg_server_config* cfg, rg_server** out
     S->max_large = cfg && cfg->max_large_slots > 0 ? std::min(cfg->max_large_slots, n_slots)
                                                    : std::max(1, n_slots / 2);
     S->large_work = cfg && cfg->large_work > 0 ? (double)cfg->large_work : 2147483648.0;
+    {
+      int sms = 0;
+      cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+      const int want = cfg ? cfg->large_max_sms : 0;
+      S->large_sms = want < 0 ? 0 : (want == 0 ? sms - sms / 3 : std::min(want, sms));
+    }
     S->slots.resize(n_slots);
     for (int k = 0; k < n_slots; ++k) {
       int32_t st = rg_engine_create(device, &S->slots[k].engine);

@@ -291,7 +291,7 @@ BUMP_BASE, BUMP_SPOT, BUMP_VOL, BUMP_RATE, BUMP_SPOT_PAIR = 0, 1, 2, 3, 4
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("device_memory_budget", C.c_uint64),
-                ("max_large_slots", C.c_int32), ("large_work", C.c_uint64)]
+                ("max_large_slots", C.c_int32), ("large_work", C.c_uint64), ("large_max_sms", C.c_int32)]
 
 
 class JobInfo(C.Structure):

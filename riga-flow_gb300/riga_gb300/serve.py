@@ -34,14 +34,15 @@ STATES = ("working", "working", "completed", "failed", "cancelled")  # SEP-2663 
 
 class Server:
     """One ``rg_server``: `slots` engines on `device`, admission within `memory_budget` bytes; requests
-    of at least `large_work` path-steps × scenarios hold at most `max_large_slots` slots (0: the
-    library's defaults, half the slots and 2^31)."""
+    of at least `large_work` path-steps × scenarios hold at most `max_large_slots` slots and size
+    their kernels for `large_max_sms` SMs (0: the library's defaults, half the slots, 2^31 and two
+    thirds of the SMs; -1: every SM)."""
 
     def __init__(self, device: int = 0, slots: int = 4, memory_budget: int = 0, lib=None,
-                 max_large_slots: int = 0, large_work: int = 0):
+                 max_large_slots: int = 0, large_work: int = 0, large_max_sms: int = 0):
         self.lib = lib or load_library()
         self.device = device
-        cfg = abi.ServerConfig(device, slots, memory_budget, max_large_slots, large_work)
+        cfg = abi.ServerConfig(device, slots, memory_budget, max_large_slots, large_work, large_max_sms)
         h = C.c_void_p()
         check(self.lib, self.lib.rg_server_create(C.byref(cfg), C.byref(h)))
         self.handle = h
