@@ -95,6 +95,11 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     const uint32_t ga = (uint32_t)((n1 & ~(uint64_t)31) ^ ((n1 & ~(uint64_t)31) >> 1));  // gray(a)
     const int cw = __ffsll((long long)((n1 >> 5) + 1)) - 1 + 5;  // a / 32 + 1: its lowest set bit + 5
     int cb = -kNb;  // first node of the batch in s_hi
+    // the lanes' low-bit terms of the next node, loaded a node ahead so that their latency
+    // overlaps the current step
+    uint32_t lnext[N];
+#pragma unroll
+    for (int f = 0; f < N; ++f) lnext[f] = lut ? __ldg(tb.sob_lut + (size_t)f * 32 + lane) : 0u;
     float x[N], wcur[N];
     float* const stk = s_stk + tid;  // entry (depth d, factor f) at stk[(d * N + f) * P32D_THREADS]
 #pragma unroll
@@ -127,9 +132,16 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
             __syncwarp();
           }
           const int hb = (c - cb) * N + (upper ? 33 : 0);
+          uint32_t lcur[N];
+          const bool more = (c + 1) * N < tb.sob_nq;
 #pragma unroll
           for (int f = 0; f < N; ++f) {
-            const uint32_t xs = s_hi[wib][hb + f] ^ __ldg(tb.sob_lut + ((size_t)c * N + f) * 32 + lane);
+            lcur[f] = lnext[f];
+            if (more) lnext[f] = __ldg(tb.sob_lut + ((size_t)(c + 1) * N + f) * 32 + lane);
+          }
+#pragma unroll
+          for (int f = 0; f < N; ++f) {
+            const uint32_t xs = s_hi[wib][hb + f] ^ lcur[f];
             zf[f] = rg_probit32(tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT
                                     ? xs
                                     : rg_owen(xs, (uint64_t)__ldg(tb.node_k + c) * N + f, tr.seed));

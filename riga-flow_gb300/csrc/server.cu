@@ -173,7 +173,8 @@ struct Slot {
   size_t held = 0;      // device bytes the engine's workspace holds
   size_t running = 0;   // estimate of the request it runs (0 when idle)
   bool busy = false;
-  bool trimming = false;  // another worker releases this idle engine's buffers (outside the lock)
+  bool busy_large = false;  // running a large request
+  bool trimming = false;    // another worker releases this idle engine's buffers (outside the lock)
 };
 
 }  // namespace
@@ -270,9 +271,10 @@ void run_job(rg_engine* E, Job* job) {
 // except that a large one waiting for a large slot is passed, and one that does not fit the memory
 // budget is passed only by requests of at most a sixteenth of the budget (later requests with larger
 // estimates never overtake it on memory).
-// A request larger than a sixteenth of the budget goes to an idle slot whose buffers already hold
-// most of its estimate (80%; estimates are upper bounds) when there is one, so that no buffers are
-// released and allocated again.
+// A request larger than a sixteenth of the budget goes to a slot whose buffers already hold most
+// of its estimate (80%; estimates are upper bounds) when there is one — waiting for it if it is
+// running a short request — so that no buffers are released and allocated again (cudaFree and a
+// large cudaMalloc wait for the whole device).
 Job* next_job(rg_server* S, int k, std::vector<int>& trim) {
   if (S->slots[k].trimming) return nullptr;
   bool waiting = false;  // an earlier request waits for memory
@@ -284,7 +286,7 @@ Job* next_job(rg_server* S, int k, std::vector<int>& trim) {
       bool other = false;
       for (size_t i = 0; i < S->slots.size(); ++i) {
         const Slot& s = S->slots[i];
-        other = other || ((int)i != k && !s.busy && !s.trimming && holds(s));
+        other = other || ((int)i != k && !s.trimming && !s.busy_large && holds(s));
       }
       if (other) continue;  // left to that slot's worker
     }
@@ -313,6 +315,7 @@ void worker(rg_server* S, int k) {
     if (job->large) ++S->n_large;
     Slot& slot = S->slots[k];
     slot.busy = true;
+    slot.busy_large = job->large;
     slot.running = job->est;
     for (int i : trim) {  // counted free from now on; released below, outside the lock
       S->slots[i].trimming = true;
@@ -343,6 +346,7 @@ void worker(rg_server* S, int k) {
     if (job->large) --S->n_large;
     if (--S->n_running == 0) S->busy_s += job->t_end - S->busy_since;
     slot.busy = false;
+    slot.busy_large = false;
     slot.running = 0;
     slot.held = held;
     S->peak_reserved = std::max(S->peak_reserved, reserved(S));
