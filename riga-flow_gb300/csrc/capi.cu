@@ -33,10 +33,19 @@ void cuda_check(cudaError_t e, const char* what) {
   }
 }
 
+// Capacity for n bytes: below 1 GiB the next power of two, so that requests of growing size
+// re-allocate a few times rather than at every step (cudaFree waits for the whole device).
+static size_t grown(size_t n) {
+  if (n < 256) return 256;
+  if (n >= (size_t(1) << 30)) return n;
+  size_t c = 256;
+  while (c < n) c <<= 1;
+  return c;
+}
 void DevBuf::ensure(size_t n) {
   if (n <= bytes && ptr) return;
   release();
-  size_t want = n < 256 ? 256 : n;
+  const size_t want = grown(n);
   cuda_check(cudaMalloc(&ptr, want), "cudaMalloc");
   bytes = want;
 }
@@ -48,7 +57,7 @@ void DevBuf::release() {
 void HostBuf::ensure(size_t n) {
   if (n <= bytes && ptr) return;
   release();
-  size_t want = n < 256 ? 256 : n;
+  const size_t want = grown(n);
   cuda_check(cudaMallocHost(&ptr, want), "cudaMallocHost");
   bytes = want;
 }
