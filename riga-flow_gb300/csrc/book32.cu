@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <mutex>
 
+#include "rg_async.cuh"
 #include "rg_internal.h"
 
 namespace rg {
@@ -77,31 +78,10 @@ void launch_book_gen32(const DevTrade& gen, const DevTables& tb, const float* L3
 // buffer, and each warp releases a buffer on its "empty" mbarrier when it is done with it.
 // Every wait is bounded: a wait that runs out sets the status word and the kernel returns.
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait for the phase of `bar` with the given parity to complete.
+// Bounded wait for the phase of `bar` with the given parity to complete; sets the status word
+// when it runs out.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t it = 0; it < (1u << 24); ++it)
-    if (mbar_test(bar, parity)) return true;
+  if (mbar_wait_bounded(bar, parity)) return true;
   atomicExch(status, KSTAT_TIMEOUT);
   return false;
 }

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "p32_path.cuh"
+#include "rg_async.cuh"
 #include "rg_internal.h"
 
 namespace rg {
@@ -38,8 +39,14 @@ namespace rg {
 // Byte offsets of the kernel's dynamic shared-memory regions, 16-byte aligned, and their total.
 // Computed by the same function on the host (to size the launch) and in the kernel (to carve).
 struct P32Layout {
-  uint32_t flags, per, thr, noff, ncf, qmc, node4, plan, z, dw, total;
+  uint32_t flags, per, thr, noff, ncf, qmc, node4, plan, z, dw, lvs, total;
 };
+
+// Bytes of the staged local-vol rows (LV = 2): per warp two mbarriers and two buffers of a pair of
+// steps × N assets × gx (v, slope).
+__host__ __device__ inline uint32_t p32_lvs_bytes(int N, int gx, int nwarp) {
+  return (uint32_t)nwarp * (16u + 4u * (uint32_t)N * (uint32_t)gx * 8u);
+}
 
 // Floats per row of the Z array: N·(Pb + 4) and one more, so that rows start in different banks.
 __host__ __device__ inline int p32_zrow(int N, int Pb) { return N * (Pb + 4) + 1; }
@@ -47,7 +54,8 @@ __host__ __device__ inline int p32_zrow(int N, int Pb) { return N * (Pb + 4) + 1
 // path + 1) pairs are read as one aligned 8-byte load.
 __host__ __device__ inline int p32_dwstep(int N, int Pb, int ppt) { return Pb * N + (ppt == 2 ? 2 : 1); }
 
-__host__ __device__ inline P32Layout p32_layout(int N, int Pb, int TT, int NNmax, int stack_max, int ppt) {
+__host__ __device__ inline P32Layout p32_layout(int N, int Pb, int TT, int NNmax, int stack_max, int ppt,
+                                                uint32_t lvs_bytes = 0) {
   P32Layout L;
   uint32_t o = 0;
   auto put = [&o](uint32_t& field, uint32_t bytes) {
@@ -71,6 +79,7 @@ __host__ __device__ inline P32Layout p32_layout(int N, int Pb, int TT, int NNmax
   put(L.plan, (uint32_t)(NNmax + (NNmax + 1) + (TT + 1) + stack_max) * 4u);
   put(L.z, zb);
   put(L.dw, (uint32_t)TT * (uint32_t)p32_dwstep(N, Pb, ppt) * 4u);  // dW[step][factor][path]
+  put(L.lvs, lvs_bytes);  // per warp: its scenario's local-vol rows of the next two pairs of steps
   L.total = o;
   return L;
 }
@@ -136,7 +145,7 @@ __device__ unsigned long long g_p32_phase_clocks[4];
 #define RG_PHASE_END()
 #endif
 
-template <int N, bool LV, bool REC, int PPT>
+template <int N, int LV, bool REC, int PPT>
 __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
     DevTrade tr, DevTables tb, const DevScenario* __restrict__ scen,
     const DevScen32* __restrict__ scen32, int S, int Pb, int TT, int NNmax, int stack_max,
@@ -151,7 +160,8 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   const int T = (int)tr.steps;
   const uint64_t nchunks = (npaths + 31) / 32;
   // ---- shared-memory carve-up (the host sizes the launch from the same layout)
-  const P32Layout L = p32_layout(N, Pb, TT, NNmax, stack_max, PPT);
+  const uint32_t lvs_bytes = LV == 2 ? p32_lvs_bytes(N, tr.gx, (int)(blockDim.x >> 5)) : 0u;
+  const P32Layout L = p32_layout(N, Pb, TT, NNmax, stack_max, PPT, lvs_bytes);
   uint32_t dyn_bytes;
   asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
   if (L.total > dyn_bytes) {
@@ -226,6 +236,23 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   // for this launch's offset within a 32-point block; a lane's point may lie in the next block
   const bool sob_lut = tr.vr == RG_VR_SOBOL && tb.sob_lut != nullptr && (int32_t)((path0 + 1) & 31) == tb.sob_lut_o;
   const bool upper = (uint32_t)tb.sob_lut_o + (uint32_t)lane >= 32u;
+  // LV == 2: the warp's own region of staged local-vol rows — two mbarriers, then two buffers of a
+  // pair of steps × N assets × gx (v, slope) — filled by lane 0 with bulk copies a pair ahead
+  uint64_t* s_lvbar = nullptr;
+  float2* s_lvrows = nullptr;
+  uint32_t lv_par = 0, lv_pend = 0;  // per buffer: parity of its next completion, copy in flight
+  bool lv_bad = false;               // a bounded wait ran out: this warp's sums are poisoned
+  if (LV == 2) {
+    unsigned char* r = smem_raw + L.lvs + (size_t)wid * (16u + 32u * (uint32_t)N * (uint32_t)gx);
+    s_lvbar = reinterpret_cast<uint64_t*>(r);
+    s_lvrows = reinterpret_cast<float2*>(r + 16);
+    if (lane == 0) {
+      mbar_init(&s_lvbar[0], 1);
+      mbar_init(&s_lvbar[1], 1);
+      mbar_init_fence();
+    }
+    __syncwarp();
+  }
   RG_PHASE_BEGIN();
   const uint64_t ntiles = (npaths + Pb - 1) / Pb;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -446,7 +473,7 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       if (warp_on) {
         // one Euler step of every asset (correlated increment, local-vol lookup, log-space update);
         // returns the worst-of log performance of each path after the step
-        auto euler = [&](int tt, float (&wmin)[PPT]) {
+        auto euler = [&](int tt, float (&wmin)[PPT], const float2* srow) {
           const int tg = (t0 + tt) * gx;
           V d[N], y[N];
 #pragma unroll
@@ -480,8 +507,13 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
               const V w = V::fma(u01, gxm1, V::fma(fl, neg1, two23));
 #pragma unroll
               for (int j = 0; j < PPT; ++j) {
-                const uint32_t idx = lvo[f] + (uint32_t)tg + (uint32_t)__float_as_int(fl.v[j]);
-                const float2 r = __ldg(tb.lv_rows + idx);
+                float2 r;
+                if (LV == 2) {
+                  r = srow[f * gx + ((uint32_t)__float_as_int(fl.v[j]) - 0x4B000000u)];
+                } else {
+                  const uint32_t idx = lvo[f] + (uint32_t)tg + (uint32_t)__float_as_int(fl.v[j]);
+                  r = __ldg(tb.lv_rows + idx);
+                }
                 sg.v[j] = fmaf(w.v[j], r.y, r.x);
               }
             } else {
@@ -523,11 +555,51 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
             }
           }
         };
-        int tt = 0;
+        // LV == 2: lane 0 copies the rows of the pair of steps starting at tp into buffer b (its
+        // last readers, this warp's pair two earlier, are done: every lane passed __syncwarp)
+        const uint32_t row_floats = 2u * (uint32_t)gx;  // float2 entries of a row, as floats
+        auto stage_pair = [&](int tp, int b) {
+          if (LV != 2 || lv_bad) return;
+          lv_pend |= 1u << b;
+          if (lane != 0) return;
+          const int ns = min(2, tn - tp);
+          fence_proxy_async_smem();
+          mbar_expect_tx(&s_lvbar[b], (uint32_t)(ns * N) * row_floats * 4u);
+          for (int js = 0; js < ns; ++js)
+#pragma unroll
+            for (int f = 0; f < N; ++f)
+              bulk_g2s(s_lvrows + ((b * 2 + js) * N + f) * gx,
+                       tb.lv_rows + (lvo[f] + 0x4B000000u) + (uint32_t)((t0 + tp + js) * gx), row_floats * 4u,
+                       &s_lvbar[b]);
+        };
+        // the rows of buffer b once its copies have landed: every lane waits on the buffer's
+        // mbarrier (bounded; when a wait runs out the warp stops waiting and issuing, and its sums
+        // are poisoned)
+        auto rows_of = [&](int b) -> const float2* {
+          if (LV != 2) return nullptr;
+          if (!lv_bad) {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&s_lvbar[b], (lv_par >> b) & 1u));
+            if (ok) {
+              lv_par ^= 1u << b;
+              lv_pend &= ~(1u << b);
+            } else {
+              lv_bad = true;
+            }
+          }
+          return s_lvrows + b * 2 * N * gx;
+        };
+        int tt = 0, bsel = 0;
+        stage_pair(0, 0);
         for (; tt + 1 < tn; tt += 2) {
+          if (LV == 2) {
+            __syncwarp();
+            if (tt + 2 < tn) stage_pair(tt + 2, bsel ^ 1);
+          }
+          const float2* srow = rows_of(bsel);
+          bsel ^= 1;
           float w0[PPT], w1[PPT];
-          euler(tt, w0);
-          euler(tt + 1, w1);
+          euler(tt, w0, srow);
+          euler(tt + 1, w1, LV == 2 ? srow + N * gx : nullptr);
 #pragma unroll
           for (int j = 0; j < PPT; ++j) worst[j] = w1[j];
           const uint32_t f0 = s_flags[tt], f1 = s_flags[tt + 1];
@@ -555,8 +627,9 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
           }
         }
         if (tt < tn) {
+          const float2* srow = rows_of(bsel);
           float w0[PPT];
-          euler(tt, w0);
+          euler(tt, w0, srow);
 #pragma unroll
           for (int j = 0; j < PPT; ++j) worst[j] = w0[j];
           phoenix(tt, w0);
@@ -592,32 +665,42 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       }
       const uint64_t chunk = (tile0 + (uint64_t)(pl0 & ~31)) >> 5;
       if (lane_ok && lk < RG_ACC && chunk < nchunks)
-        partial[((size_t)chunk * S + s) * RG_ACC + lk] = (double)mine;
+        partial[((size_t)chunk * S + s) * RG_ACC + lk] =
+            LV == 2 && lv_bad ? __longlong_as_double(0x7ff8000000000000LL) : (double)mine;
     }
     RG_PHASE_MARK(3);
   }
+  // copies still in flight after a wait ran out land before the CTA's shared memory is released
+  if (LV == 2)
+    for (int b = 0; b < 2; ++b)
+      if ((lv_pend >> b) & 1u) mbar_wait_bounded(&s_lvbar[b], (lv_par >> b) & 1u);
   RG_PHASE_END();
 }
 
-template <int N, bool LV, int PPT>
+template <int N, int LV, int PPT>
 static const void* kernel_ptr(bool rec) {
-  return rec ? reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, true, PPT>)
+  return rec ? reinterpret_cast<const void*>(&phoenix32_kernel<N, LV == 2 ? 1 : LV, true, PPT>)
              : reinterpret_cast<const void*>(&phoenix32_kernel<N, LV, false, PPT>);
 }
 
+// lv: 0 flat vol, 1 local-vol rows gathered from global memory, 2 rows staged per warp (records
+// launches always gather)
 template <int PPT>
-static const void* select_kernel_ppt(int n, bool lv, bool rec) {
+static const void* select_kernel_ppt(int n, int lv, bool rec) {
+#define RG_SEL(NN) \
+  return lv == 2 ? kernel_ptr<NN, 2, PPT>(rec) : (lv ? kernel_ptr<NN, 1, PPT>(rec) : kernel_ptr<NN, 0, PPT>(rec));
   switch (n) {
-    case 1: return lv ? kernel_ptr<1, true, PPT>(rec) : kernel_ptr<1, false, PPT>(rec);
-    case 2: return lv ? kernel_ptr<2, true, PPT>(rec) : kernel_ptr<2, false, PPT>(rec);
-    case 3: return lv ? kernel_ptr<3, true, PPT>(rec) : kernel_ptr<3, false, PPT>(rec);
-    case 4: return lv ? kernel_ptr<4, true, PPT>(rec) : kernel_ptr<4, false, PPT>(rec);
-    case 5: return lv ? kernel_ptr<5, true, PPT>(rec) : kernel_ptr<5, false, PPT>(rec);
+    case 1: RG_SEL(1)
+    case 2: RG_SEL(2)
+    case 3: RG_SEL(3)
+    case 4: RG_SEL(4)
+    case 5: RG_SEL(5)
     default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
   }
+#undef RG_SEL
 }
 
-static const void* select_kernel(int n, bool lv, bool rec, int ppt) {
+static const void* select_kernel(int n, int lv, bool rec, int ppt) {
   return ppt == 2 ? select_kernel_ppt<2>(n, lv, rec) : select_kernel_ppt<1>(n, lv, rec);
 }
 
@@ -631,11 +714,19 @@ static int formula_tt(const Prepared& P, int Pb) {
   return tt < 8 ? 8 : (tt > 64 ? 64 : tt);
 }
 
-// Whether a tile of Pb paths at `ppt` paths per thread and `tt` steps fits: the shared-memory
-// layout within 227 KB.
-static bool p32_fits(const Prepared& P, int Pb, int ppt, int tt) {
-  return p32_layout(P.n, Pb, tt, tt + P.stack_max, P.stack_max, ppt).total <= 227u * 1024u;
+// Shared-memory bytes of a tiled shape: Sb scenario slots × Pb paths per tile at `ppt` paths per
+// thread, `tt` steps per tile, local-vol rows staged per warp or not.
+static uint32_t p32_smem(const Prepared& P, int Sb, int Pb, int ppt, int tt, int lvs) {
+  const uint32_t lvs_bytes = lvs ? p32_lvs_bytes(P.n, P.trade.gx, Sb * Pb / ppt / 32) : 0u;
+  return p32_layout(P.n, Pb, tt, tt + P.stack_max, P.stack_max, ppt, lvs_bytes).total;
 }
+// Whether the shape fits in 227 KB of shared memory.
+static bool p32_fits(const Prepared& P, int Sb, int Pb, int ppt, int tt, int lvs) {
+  return p32_smem(P, Sb, Pb, ppt, tt, lvs) <= 227u * 1024u;
+}
+// Whether a launch may stage its local-vol rows: local vol, and rows whose bulk copies start and
+// end on 16-byte boundaries (an even grid width).
+static bool p32_lvs_ok(const Prepared& P) { return P.trade.has_lv && (P.trade.gx % 2) == 0; }
 
 // The tiled kernel's block and formula tile depth.  Scenario slots: S rounded up to a power of
 // two, at least 4 (two scenarios run padded: a CTA on half the slots beats both the direct kernel
@@ -647,10 +738,11 @@ static void tiled_shape(const Prepared& P, Fp32Shape& sh, int ppt) {
   sh.Sb = sb;
   sh.Pb = 1024 / sb;
   sh.TT = formula_tt(P, sh.Pb);
-  if (ppt == 2 && !p32_fits(P, sh.Pb, 2, sh.TT)) ppt = 1;
+  if (ppt == 2 && !p32_fits(P, sb, sh.Pb, 2, sh.TT, 0)) ppt = 1;
   sh.ppt = ppt;
+  sh.lvs = 0;
   sh.threads = sb * sh.Pb / ppt;
-  sh.smem = (int)p32_layout(P.n, sh.Pb, sh.TT, sh.TT + P.stack_max, P.stack_max, ppt).total;
+  sh.smem = (int)p32_smem(P, sb, sh.Pb, ppt, sh.TT, 0);
 }
 
 // Tile depths the autotuner times besides the formula depth.
@@ -798,9 +890,9 @@ static void p32_set_attributes() {
   cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem opt-in");
   for (int ppt = 1; ppt <= 2; ++ppt)
     for (int n = 1; n <= RG_NMAX; ++n)
-      for (int lv = 0; lv < 2; ++lv)
+      for (int lv = 0; lv < 3; ++lv)
         for (int rec = 0; rec < 2; ++rec) {
-          const void* kr = select_kernel(n, lv != 0, rec != 0, ppt);
+          const void* kr = select_kernel(n, lv, rec != 0, ppt);
           cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, optin),
                      "phoenix32 smem attribute");
           cuda_check(cudaFuncSetAttribute(kr, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
@@ -811,7 +903,7 @@ static void p32_set_attributes() {
 
 // Grid of a tiled shape: as many CTAs as are resident on the SMs, at most one per tile.
 static int tiled_grid(const Prepared& P, const Fp32Shape& sh, uint64_t npaths, int sm_count) {
-  const void* k = select_kernel(P.n, P.trade.has_lv != 0, false, sh.ppt);
+  const void* k = select_kernel(P.n, P.trade.has_lv ? (sh.lvs ? 2 : 1) : 0, false, sh.ppt);
   int per_sm = 0;
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, sh.threads, sh.smem),
              "phoenix32 occupancy");
@@ -847,29 +939,32 @@ uint64_t p32_chunks(uint64_t npaths) { return (npaths + 31) / 32; }
 
 // ---------------------------------------------------------------------- tiled-shape autotuner --
 namespace {
-// A tiled launch shape: paths per CTA tile, paths per thread, tile depth.
+// A tiled launch shape: paths per CTA tile, paths per thread, tile depth, local-vol rows staged.
 struct TiledKnobs {
-  int pb, ppt, tt;
-  bool operator==(const TiledKnobs& o) const { return pb == o.pb && ppt == o.ppt && tt == o.tt; }
+  int pb, ppt, tt, lvs;
+  bool operator==(const TiledKnobs& o) const { return pb == o.pb && ppt == o.ppt && tt == o.tt && lvs == o.lvs; }
 };
 
-// Sets the block (Pb paths per tile), paths per thread and tile depth of a tiled shape if the
-// block keeps a warp on 32·ppt paths of one scenario and its layout fits.
+// Sets the block (Pb paths per tile), paths per thread, tile depth and row staging of a tiled
+// shape if the block keeps a warp on 32·ppt paths of one scenario and its layout fits.
 bool p32_with(const Prepared& P, Fp32Shape& sh, TiledKnobs k) {
-  if (k.pb < 32 * k.ppt || (k.pb & (k.pb - 1)) || k.pb * sh.Sb > 1024 || !p32_fits(P, k.pb, k.ppt, k.tt)) return false;
+  if (k.pb < 32 * k.ppt || (k.pb & (k.pb - 1)) || k.pb * sh.Sb > 1024) return false;
+  if (k.lvs && !p32_lvs_ok(P)) return false;
+  if (!p32_fits(P, sh.Sb, k.pb, k.ppt, k.tt, k.lvs)) return false;
   sh.Pb = k.pb;
   sh.ppt = k.ppt;
+  sh.lvs = k.lvs;
   sh.threads = sh.Sb * k.pb / k.ppt;
   sh.TT = k.tt;
-  sh.smem = (int)p32_layout(P.n, k.pb, k.tt, k.tt + P.stack_max, P.stack_max, k.ppt).total;
+  sh.smem = (int)p32_smem(P, sh.Sb, k.pb, k.ppt, k.tt, k.lvs);
   return true;
 }
 
 std::mutex g_tune_mu;
 std::map<std::vector<int64_t>, TiledKnobs> g_tuned;  // launch shape -> (block, paths per thread, tile depth)
 bool g_tune_enabled = true;
-TiledKnobs g_forced{0, 0, 0};  // (block, paths per thread, tile depth) every tiled launch takes, or none
-                               // (pb 0: the formula block)
+TiledKnobs g_forced{0, 0, 0, 0};  // the shape every tiled launch takes, or none (ppt 0); pb 0: the
+                                  // formula block
 
 
 }  // namespace
@@ -880,22 +975,24 @@ void p32_set_autotune(bool enabled) {
   g_tuned.clear();
 }
 
-void p32_force_shape(int ppt, int tt, int pb) {
-  if (!((ppt == 0 && tt == 0 && pb == 0) || ((ppt == 1 || ppt == 2) && tt > 0 && pb >= 0)))
-    raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: paths per thread 1 or 2, a tile depth and a block, or (0, 0, 0)");
+void p32_force_shape(int ppt, int tt, int pb, int lvs) {
+  if (!((ppt == 0 && tt == 0 && pb == 0 && lvs == 0) || ((ppt == 1 || ppt == 2) && tt > 0 && pb >= 0 && (lvs == 0 || lvs == 1))))
+    raise(RG_ERR_INVALID_ARGUMENT,
+          "tiled shape: paths per thread 1 or 2, a tile depth, a block and row staging 0 or 1, or (0, 0, 0, 0)");
   if (pb != 0 && (pb < 32 * ppt || pb > 1024 || (pb & (pb - 1))))
     raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the block must be a power of two of 32 x paths per thread to 1024 paths");
   bool plan = tt == 0;
   for (int c : kTileCandidates) plan = plan || c == tt;
   if (!plan) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the tile depth must be one of the autotuner's candidates");
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_forced = TiledKnobs{pb, ppt, tt};
+  g_forced = TiledKnobs{pb, ppt, tt, lvs};
 }
 
-// Times every (block, paths per thread, tile depth) candidate on a prefix of the launch's paths and
-// keeps the fastest for the launch shape.  No knob changes a path's arithmetic or the 32-path
-// chunks of the sums, so prices are identical whichever wins.  Blocks: the formula's Pb paths per
-// tile and half of it (two smaller CTAs per SM where they fit).
+// Times every (block, paths per thread, tile depth, row staging) candidate on a prefix of the
+// launch's paths and keeps the fastest for the launch shape.  No knob changes a path's arithmetic or
+// the 32-path chunks of the sums, so prices are identical whichever wins.  Blocks: the formula's Pb
+// paths per tile and half of it (two smaller CTAs per SM where they fit); staging: local-vol rows
+// gathered per lane from global memory, or copied per warp into shared memory ahead of use.
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,
                          const DevScen32* scen32, uint64_t path0, uint64_t npaths, Fp32Shape sh,
                          const LaunchOut& out, bool may_tune, int sm_count, cudaStream_t st) {
@@ -914,7 +1011,7 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     if (g_forced.ppt) {
-      Fp32Shape t = apply({g_forced.pb ? g_forced.pb : sh.Pb, g_forced.ppt, g_forced.tt}, npaths);
+      Fp32Shape t = apply({g_forced.pb ? g_forced.pb : sh.Pb, g_forced.ppt, g_forced.tt, g_forced.lvs}, npaths);
       if (!t.tuned) raise(RG_ERR_INVALID_ARGUMENT, "tiled shape: the forced tile does not fit in shared memory");
       return t;
     }
@@ -931,11 +1028,12 @@ Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenar
   tts.insert(tts.end(), std::begin(kTileCandidates), std::end(kTileCandidates));
   for (int pb : {sh.Pb, sh.Pb / 2})
     for (int ppt = 1; ppt <= 2; ++ppt)
-      for (int tt : tts) {
-        Fp32Shape c = sh;
-        const TiledKnobs k{pb, ppt, tt};
-        if (std::find(cand.begin(), cand.end(), k) == cand.end() && p32_with(P, c, k)) cand.push_back(k);
-      }
+      for (int tt : tts)
+        for (int lvs = 0; lvs <= (p32_lvs_ok(P) ? 1 : 0); ++lvs) {
+          Fp32Shape c = sh;
+          const TiledKnobs k{pb, ppt, tt, lvs};
+          if (std::find(cand.begin(), cand.end(), k) == cand.end() && p32_with(P, c, k)) cand.push_back(k);
+        }
   LaunchOut lo = out;  // the partial sums are overwritten by the real launch afterwards
   lo.ko_steps = nullptr;
   lo.records = nullptr;
@@ -979,25 +1077,32 @@ void launch_phoenix32(const Prepared& P, const DevTables& tb, const DevScenario*
   if (!plan) raise(RG_ERR_GPU_ERROR, "phoenix32: no bridge plan staged for the tile depth");
   if (sh.Pb < 32 || (sh.Pb & (sh.Pb - 1)) || sh.threads * sh.ppt != sh.Sb * sh.Pb || (sh.ppt != 1 && sh.ppt != 2))
     raise(RG_ERR_GPU_ERROR, "phoenix32: invalid tile shape");
+  // records launches gather their local-vol rows (the staged variant has no records instance)
+  const int lvk = P.trade.has_lv ? (sh.lvs && !out.records ? 2 : 1) : 0;
+  if (sh.lvs && !p32_lvs_ok(P)) raise(RG_ERR_GPU_ERROR, "phoenix32: local-vol rows cannot be staged");
 #define RG_LAUNCH(NN, LVV)                                                                        \
   if (sh.ppt == 2) {                                                                              \
-    if (out.records) RG_LAUNCH_R(NN, LVV, true, 2) else RG_LAUNCH_R(NN, LVV, false, 2)            \
+    if (out.records) RG_LAUNCH_R(NN, (LVV == 2 ? 1 : LVV), true, 2) else RG_LAUNCH_R(NN, LVV, false, 2) \
   } else {                                                                                        \
-    if (out.records) RG_LAUNCH_R(NN, LVV, true, 1) else RG_LAUNCH_R(NN, LVV, false, 1)            \
+    if (out.records) RG_LAUNCH_R(NN, (LVV == 2 ? 1 : LVV), true, 1) else RG_LAUNCH_R(NN, LVV, false, 1) \
   }
 #define RG_LAUNCH_R(NN, LVV, REC, PPT)                                                            \
   phoenix32_kernel<NN, LVV, REC, PPT><<<sh.grid, sh.threads, sh.smem, st>>>(                      \
       P.trade, tb, scen, scen32, P.n_scen, sh.Pb, sh.TT, NNmax, P.stack_max, ln_ko, ln_cb, ln_ki, \
       path0, npaths, plan, out.partial, out.ko_steps, out.records);
-  const bool lv = P.trade.has_lv != 0;
+#define RG_LAUNCH_N(NN)                         \
+  if (lvk == 2) { RG_LAUNCH(NN, 2) }            \
+  else if (lvk == 1) { RG_LAUNCH(NN, 1) }       \
+  else { RG_LAUNCH(NN, 0) }
   switch (P.n) {
-    case 1: if (lv) { RG_LAUNCH(1, true) } else { RG_LAUNCH(1, false) } break;
-    case 2: if (lv) { RG_LAUNCH(2, true) } else { RG_LAUNCH(2, false) } break;
-    case 3: if (lv) { RG_LAUNCH(3, true) } else { RG_LAUNCH(3, false) } break;
-    case 4: if (lv) { RG_LAUNCH(4, true) } else { RG_LAUNCH(4, false) } break;
-    case 5: if (lv) { RG_LAUNCH(5, true) } else { RG_LAUNCH(5, false) } break;
+    case 1: RG_LAUNCH_N(1) break;
+    case 2: RG_LAUNCH_N(2) break;
+    case 3: RG_LAUNCH_N(3) break;
+    case 4: RG_LAUNCH_N(4) break;
+    case 5: RG_LAUNCH_N(5) break;
     default: raise(RG_ERR_INVALID_MARKET_SHAPE, "unsupported asset count");
   }
+#undef RG_LAUNCH_N
 #undef RG_LAUNCH
 #undef RG_LAUNCH_R
   cuda_check(cudaGetLastError(), "phoenix32_kernel launch");

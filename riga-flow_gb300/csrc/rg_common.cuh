@@ -196,13 +196,11 @@ __device__ __forceinline__ double rg_probit64(double p) {
 // polynomial fit (csrc/probit32_fit.py): degree 9 in w - 2.5 for w < 5 (p >= 0.0017, 99.6% of
 // draws, so nearly every warp stays on one branch) and degree 11 in sqrt(w) - 3.7161102 beyond.
 // No division, one fast logarithm; within 2.7e-7 relative (4.5 FP32 ulps) of the exact inverse
-// normal, which the reference's Acklam approximation (qmc.rs:37-91) matches to 1.15e-9.  The
-// central polynomial runs on every lane and the tail one only when a lane of the warp needs it
-// (a vote among the active lanes), so straight-line callers do not pay both branches.
+// normal, which the reference's Acklam approximation (qmc.rs:37-91) matches to 1.15e-9.
 __device__ __forceinline__ float rg_ninv32_lower(float p, float s) {
   const float w = -__logf(4.0f * p * (1.0f - p));
   float g;
-  {
+  if (w < 5.0f) {
     const float t = w - 2.5f;
     g = -1.243237249e-08f;
     g = fmaf(g, t, 3.285588946e-08f);
@@ -214,9 +212,7 @@ __device__ __forceinline__ float rg_ninv32_lower(float p, float s) {
     g = fmaf(g, t, -5.907717039e-03f);
     g = fmaf(g, t, 3.488020377e-01f);
     g = fmaf(g, t, 2.123313479e+00f);
-  }
-  const bool tail = w >= 5.0f;
-  if (__any_sync(__activemask(), tail) && tail) {
+  } else {
     const float v = sqrtf(w) - 3.716110200f;
     g = 5.467908077e-06f;
     g = fmaf(g, v, -1.174909974e-05f);
