@@ -472,8 +472,8 @@ def run_gpu(args):
     build_library()
     eng = Engine(local)
     if args.shape:
-        knobs = [int(x) for x in args.shape.split(",")] + [0, 0]
-        abi.check(eng.lib, eng.lib.rg_set_tiled_shape(knobs[0], knobs[1], knobs[2], knobs[3]))
+        knobs = [int(x) for x in args.shape.split(",")] + [0]
+        abi.check(eng.lib, eng.lib.rg_set_tiled_shape(knobs[0], knobs[1], knobs[2]))
     P, T = args.paths, args.timesteps
     req, scen = workload_request(P, T, fp32=True, rank=rank, world=world)
     n_scen = len(scen)
@@ -568,7 +568,6 @@ def run_gpu(args):
         "launch": {"grid": tm.grid, "block": tm.block, "smem_bytes": tm.smem_bytes,
                    "tile_steps": tm.tile_steps, "paths_per_thread": tm.paths_per_thread,
                    "paths_per_cta_tile": tm.block * tm.paths_per_thread // n_scen_slots(n_scen),
-                   "lv_rows_staged": tm.lv_rows_staged,
                    "tuned_by": (f"forced by --shape {args.shape} (rg_set_tiled_shape)" if args.shape else
                                 "autotuner (rg_set_autotune): paths per CTA tile, paths per thread and tile depth, "
                                 "timed during warm-up")},
@@ -629,10 +628,10 @@ def main():
     ap.add_argument("--serving-seconds", type=float, default=60.0, help="window of the serving (cfg 3) run")
     ap.add_argument("--phase-clocks", action="store_true",
                     help="report the tiled kernel's per-phase clock cycles (needs a library built with RG_PHASE_CLOCKS=1)")
-    ap.add_argument("--shape", default=None, metavar="PPT,TT[,PB[,LVS]]",
-                    help="force the tiled FP32 kernel's paths per thread, tile depth, paths per CTA tile and "
-                         "local-vol row staging (rg_set_tiled_shape) instead of autotuning them, e.g. for a "
-                         "profiler capture with no tuning launches")
+    ap.add_argument("--shape", default=None, metavar="PPT,TT[,PB]",
+                    help="force the tiled FP32 kernel's paths per thread, tile depth and paths per CTA tile "
+                         "(rg_set_tiled_shape) instead of autotuning them, e.g. for a profiler capture with no "
+                         "tuning launches")
     args = ap.parse_args()
     if args.only:
         import torch

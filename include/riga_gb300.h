@@ -332,7 +332,6 @@ typedef struct rg_timing {
   int32_t grid, block, smem_bytes; /* launch shape of the fused kernel */
   int32_t tile_steps; /* steps per time tile of the tiled FP32 kernel (0 for the other kernels) */
   int32_t paths_per_thread; /* paths each thread of the tiled FP32 kernel steps (1 or 2) */
-  int32_t lv_rows_staged;   /* 1: the tiled FP32 kernel staged its local-vol rows in shared memory */
 } rg_timing;
 int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
 
@@ -346,16 +345,13 @@ int32_t rg_engine_last_timing(rg_engine* engine, rg_timing* out);
  * counterpart in the reference. */
 int32_t rg_set_autotune(int32_t enabled);
 /* Forces every tiled FP32 launch of the process onto one schedule: paths per thread 1 or 2, a tile
- * depth among the autotuner's candidates (24, 32, 48, 64, 80, 96, 128), a block of
+ * depth among the autotuner's candidates (24, 32, 48, 64, 80, 96, 128) and a block of
  * paths_per_block paths per CTA tile (0 = the formula block of 1024 / scenario slots; otherwise a
- * power of two of at least 32 × paths per thread) and stage_lv_rows 1 to copy each warp's
- * local-vol rows into shared memory ahead of use (bulk copies; local-vol requests with an even
- * grid width) or 0 to gather them from global memory; (0, 0, 0, 0) returns to the formula shape or
- * the autotuner.  A forced shape that does not fit (shared memory, 1024 threads, row staging)
- * fails the pricing call with RG_ERR_INVALID_ARGUMENT.  For callers that need a fixed schedule,
- * and for checking that schedules do not change prices.  No counterpart in the reference. */
-int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block,
-                           int32_t stage_lv_rows);
+ * power of two of at least 32 × paths per thread); (0, 0, 0) returns to the formula shape or the
+ * autotuner.  A forced shape that does not fit (shared memory, 1024 threads) fails the pricing
+ * call with RG_ERR_INVALID_ARGUMENT.  For callers that need a fixed schedule, and for checking
+ * that schedules do not change prices.  No counterpart in the reference. */
+int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block);
 /* Clock cycles the tiled FP32 kernel's CTAs spent in generation, bridge, stepping and path close
  * (out[0..3], summed over CTAs since the last reset), for profiling.  Only a library built with
  * RG_PHASE_CLOCKS=1 records them; others return RG_ERR_UNSUPPORTED.  No counterpart in the

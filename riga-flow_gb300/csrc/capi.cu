@@ -621,7 +621,6 @@ void price_with(Workspace& W, const rg_price_request* req, const rg_scenario* sc
       W.timing->smem_bytes = fp32 ? sh.smem : 0;
       W.timing->tile_steps = fp32 && !sh.direct ? sh.TT : 0;
       W.timing->paths_per_thread = fp32 && !sh.direct ? sh.ppt : 1;
-      W.timing->lv_rows_staged = fp32 && !sh.direct ? sh.lvs : 0;
       W.timing->grid = fp32 ? sh.grid : grid;
       W.timing->kernel_launches += 2;
       W.timing->d2h_bytes += sums_bytes;
@@ -1003,9 +1002,8 @@ extern "C" int32_t rg_set_autotune(int32_t enabled) {
   RG_TRY({ p32_set_autotune(enabled != 0); })
 }
 
-extern "C" int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block,
-                                      int32_t stage_lv_rows) {
-  RG_TRY({ p32_force_shape(paths_per_thread, tile_steps, paths_per_block, stage_lv_rows); })
+extern "C" int32_t rg_set_tiled_shape(int32_t paths_per_thread, int32_t tile_steps, int32_t paths_per_block) {
+  RG_TRY({ p32_force_shape(paths_per_thread, tile_steps, paths_per_block); })
 }
 
 extern "C" int32_t rg_phase_clocks(uint64_t out[4], int32_t reset) {

@@ -1,0 +1,7 @@
+// phoenix32_n2p1.cu — the tiled FP32 kernel's instantiations for 2 assets, 1 path per thread
+// (p32_tiled.cuh).
+#include "p32_tiled.cuh"
+
+namespace rg {
+RG_P32_DEFINE(2, 1)
+}  // namespace rg

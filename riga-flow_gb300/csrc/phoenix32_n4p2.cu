@@ -1,0 +1,7 @@
+// phoenix32_n4p2.cu — the tiled FP32 kernel's instantiations for 4 assets, 2 paths per thread
+// (p32_tiled.cuh).
+#include "p32_tiled.cuh"
+
+namespace rg {
+RG_P32_DEFINE(4, 2)
+}  // namespace rg

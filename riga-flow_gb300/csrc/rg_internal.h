@@ -246,7 +246,6 @@ void launch_phoenix64(const Prepared& P, const DevTables& tb, const DevScenario*
 struct Fp32Shape {
   int Sb, Pb, TT, threads, grid, smem;
   int ppt;     // paths per thread of the tiled kernel (1 or 2)
-  int lvs;     // 1: the tiled kernel stages each warp's local-vol rows in shared memory
   int tuned;   // 1: Pb, ppt and TT came from the autotuner's cache (or were forced)
   int direct;  // 1: the per-thread kernel of phoenix32d.cu; then only grid and threads are used
 };
@@ -281,7 +280,7 @@ std::shared_ptr<const BridgePlans> p32_bridge_plans(const Prepared& P);
 // changes the schedule, never the arithmetic) and caches the fastest.  Returns `sh` with TT set.
 // Enables or disables the autotuner process-wide; either way its cache is cleared.
 void p32_set_autotune(bool enabled);
-void p32_force_shape(int ppt, int tt, int pb, int lvs);
+void p32_force_shape(int ppt, int tt, int pb);
 // Phase clocks of the tiled FP32 kernel (a build option); 0 when the build has none.
 int p32_phase_clocks(unsigned long long out[4], bool reset);
 Fp32Shape phoenix32_tune(const Prepared& P, const DevTables& tb, const DevScenario* scen,

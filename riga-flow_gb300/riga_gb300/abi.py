@@ -185,8 +185,7 @@ class Timing(C.Structure):
                 ("reduce_ms", C.c_double), ("d2h_ms", C.c_double), ("device_ms", C.c_double),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("kernel_launches", C.c_int32), ("grid", C.c_int32), ("block", C.c_int32),
-                ("smem_bytes", C.c_int32), ("tile_steps", C.c_int32), ("paths_per_thread", C.c_int32),
-                ("lv_rows_staged", C.c_int32)]
+                ("smem_bytes", C.c_int32), ("tile_steps", C.c_int32), ("paths_per_thread", C.c_int32)]
 
 
 class Scenario(C.Structure):
@@ -347,7 +346,7 @@ SIGNATURES = {
     "rg_merge_results": (_i32, [C.POINTER(PriceResult), _i32, _u64, C.POINTER(PriceResult)]),
     "rg_engine_last_timing": (_i32, [_vp, C.POINTER(Timing)]),
     "rg_set_autotune": (_i32, [_i32]),
-    "rg_set_tiled_shape": (_i32, [_i32, _i32, _i32, _i32]),
+    "rg_set_tiled_shape": (_i32, [_i32, _i32, _i32]),
     "rg_phase_clocks": (_i32, [C.POINTER(C.c_uint64), _i32]),
     "rg_surfaces_upload": (_i32, [_vp, C.POINTER(PriceRequest), C.POINTER(Scenario), _i32, C.POINTER(_i32)]),
     "rg_price_book": (_i32, [_vp, C.POINTER(BookRequest), C.POINTER(Market), _i32,

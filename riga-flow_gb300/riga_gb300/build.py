@@ -69,7 +69,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
             print(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "static", "-lpthread"]

@@ -345,17 +345,14 @@ def test_every_tiled_shape_prices_identically(engine, n, lv):
         scen.append((m, [0.01 if (lv and k % 4 == 2 and i == f) else 0.0 for i in range(n)]))
     got = []
     try:
-        shapes = [(1, 24, 0, 0), (2, 24, 0, 0), (2, 48, 0, 0), (1, 32, 0, 0), (1, 48, 32, 0), (2, 32, 64, 0)]
-        if lv:  # local-vol rows staged per warp in shared memory
-            shapes += [(2, 48, 0, 1), (1, 32, 0, 1), (1, 24, 32, 1), (2, 80, 0, 1)]
-        for ppt, tt, pb, lvs in shapes:
-            abi.check(lib, lib.rg_set_tiled_shape(ppt, tt, pb, lvs))
+        for ppt, tt, pb in ((1, 24, 0), (2, 24, 0), (2, 48, 0), (1, 32, 0), (1, 48, 32), (2, 32, 64)):
+            abi.check(lib, lib.rg_set_tiled_shape(ppt, tt, pb))
             got.append(engine.price_scenarios_raw(r, scen))
             tm = engine.last_timing()
-            assert (tm.paths_per_thread, tm.tile_steps, tm.lv_rows_staged) == (ppt, tt, lvs)
+            assert (tm.paths_per_thread, tm.tile_steps) == (ppt, tt)
             assert tm.block * ppt == 16 * (pb or 64)  # 16 scenario slots x paths per CTA tile
     finally:
-        abi.check(lib, lib.rg_set_tiled_shape(0, 0, 0, 0))
+        abi.check(lib, lib.rg_set_tiled_shape(0, 0, 0))
     for g in got[1:]:
         assert [bytes(a) for a in g] == [bytes(a) for a in got[0]]
 
