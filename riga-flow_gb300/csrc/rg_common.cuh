@@ -190,28 +190,28 @@ __device__ __forceinline__ double rg_probit64(double p) {
   }
 }
 
-// -Φ^-1(p) >= 0 in FP32 for a lower-tail probability p in [1e-12, 1/2], given p and s = 1 - 2p
-// (each formed exactly or to FP32 rounding by the caller).  With w = -ln(4p(1-p)) = -ln(1 - s²),
-// -Φ^-1(p) = s · g(w) for a smooth g (g(0) = sqrt(π/2)); g is this project's own near-minimax
-// polynomial fit (csrc/probit32_fit.py): degree 9 in w - 2.5 for w < 5 (p >= 0.0017, 99.6% of
-// draws, so nearly every warp stays on one branch) and degree 11 in sqrt(w) - 3.7161102 beyond.
-// No division, one fast logarithm; within 2.7e-7 relative (4.5 FP32 ulps) of the exact inverse
-// normal, which the reference's Acklam approximation (qmc.rs:37-91) matches to 1.15e-9.
-__device__ __forceinline__ float rg_ninv32_lower(float p, float s) {
-  const float w = -__logf(4.0f * p * (1.0f - p));
+// -Φ^-1(p) >= 0 in FP32 for a lower-tail probability p in [1e-12, 1/2], given p2 = 2p and
+// s = 1 - 2p (each formed exactly or to FP32 rounding by the caller).  With
+// w = -ln(4p(1-p)) = -ln(p2·(1 + s)), -Φ^-1(p) = s · g(w) for a smooth g (g(0) = sqrt(π/2)); g is
+// this project's own near-minimax polynomial fit (csrc/probit32_fit.py): degree 8 in w - 2.5 for
+// w < 5 (p >= 0.0017, 99.6% of draws, so nearly every warp stays on one branch) and degree 11 in
+// sqrt(w) - 3.7161102 beyond.  No division, one fast logarithm, no FP64; within 4e-7 relative of
+// the exact inverse normal, which the reference's Acklam approximation (qmc.rs:37-91) matches to
+// 1.15e-9.
+__device__ __forceinline__ float rg_ninv32_lower(float p2, float s) {
+  const float w = -__logf(fmaf(p2, s, p2));
   float g;
   if (w < 5.0f) {
     const float t = w - 2.5f;
-    g = -1.243237249e-08f;
-    g = fmaf(g, t, 3.285588946e-08f);
-    g = fmaf(g, t, 6.592640639e-07f);
-    g = fmaf(g, t, -4.897003649e-06f);
-    g = fmaf(g, t, -7.019230142e-06f);
-    g = fmaf(g, t, 3.087856661e-04f);
-    g = fmaf(g, t, -1.771644561e-03f);
-    g = fmaf(g, t, -5.907717039e-03f);
-    g = fmaf(g, t, 3.488020377e-01f);
-    g = fmaf(g, t, 2.123313479e+00f);
+    g = 4.035466097e-08f;
+    g = fmaf(g, t, 4.861039695e-07f);
+    g = fmaf(g, t, -4.990565522e-06f);
+    g = fmaf(g, t, -6.217993119e-06f);
+    g = fmaf(g, t, 3.091502040e-04f);
+    g = fmaf(g, t, -1.773010155e-03f);
+    g = fmaf(g, t, -5.908170971e-03f);
+    g = fmaf(g, t, 3.488026599e-01f);
+    g = fmaf(g, t, 2.123313567e+00f);
   } else {
     const float v = sqrtf(w) - 3.716110200f;
     g = 5.467908077e-06f;
@@ -230,16 +230,16 @@ __device__ __forceinline__ float rg_ninv32_lower(float p, float s) {
   return s * g;
 }
 
-// The FP32 inverse normal of u = (x + 1/2) / 2^32: the lower-tail probability p = min(u, 1 - u)
-// and s = 1 - 2p formed from x or ~x (s from the integer distance to the centre, exact for points
-// near it), rg_ninv32_lower, and the sign by symmetry.  It tracks the exact inverse normal, so
+// The FP32 inverse normal of u = (x + 1/2) / 2^32: twice the lower-tail probability
+// p = min(u, 1 - u) and s = 1 - 2p formed from x or ~x (s from the integer distance to the centre,
+// exact for points near it), rg_ninv32_lower, and the sign by symmetry.  It tracks the exact inverse normal, so
 // the FP32 lanes' normals agree with the FP64 lanes' Acklam normals to a few FP32 ulps.
 __device__ __forceinline__ float rg_probit32(uint32_t x) {
   const bool lower = x < 0x80000000u;
   const uint32_t xl = lower ? x : ~x;
-  const float p = fmaf((float)xl, 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+  const float p2 = fmaf((float)xl, 4.656612873077393e-10f, 2.3283064365386963e-10f);
   const float s = fmaf((float)(0x7FFFFFFFu - xl), 4.656612873077393e-10f, 2.3283064365386963e-10f);
-  const float q = rg_ninv32_lower(p, s);
+  const float q = rg_ninv32_lower(p2, s);
   return lower ? -q : q;
 }
 
@@ -297,15 +297,16 @@ __host__ __device__ __forceinline__ double rg_halton_hashed_u(uint32_t n, uint32
   return (double)R / (double)Bk;
 }
 
-// The FP32 inverse normal of u = R / Bk: the lower-tail probability p = min(R, Bk - R) / Bk and
-// s = |Bk - 2R| / Bk formed in FP32 from the exact integers (no FP64 division), p clamped below at
-// the reference's 1e-12, rg_ninv32_lower and the sign by symmetry (as rg_probit32).
+// The FP32 inverse normal of u = R / Bk: twice the lower-tail probability p = min(R, Bk - R) / Bk
+// and s = |Bk - 2R| / Bk formed in FP32 from the exact integers by one reciprocal (no FP64), p
+// clamped below at the reference's 1e-12, rg_ninv32_lower and the sign by symmetry (as
+// rg_probit32).
 __device__ __forceinline__ float rg_probit32_frac(uint64_t R, uint64_t Bk) {
   const bool lower = 2 * R < Bk;
   const float inv = __frcp_rn((float)Bk);
-  const float p = fmaxf((float)(lower ? R : Bk - R) * inv, 1.0e-12f);
+  const float p2 = fmaxf((float)(2 * (lower ? R : Bk - R)) * inv, 2.0e-12f);
   const float s = (float)(lower ? Bk - 2 * R : 2 * R - Bk) * inv;
-  const float q = rg_ninv32_lower(p, s);
+  const float q = rg_ninv32_lower(p2, s);
   return lower ? -q : q;
 }
 
