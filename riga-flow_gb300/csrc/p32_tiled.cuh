@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   const bool warp_on = ((tid & ~31) / tps) < S;
   const int gx = tr.gx;
   const V gxm1 = V::splat((float)(gx - 1));
-  const V two23 = V::splat(8388608.0f), neg1 = V::splat(-1.0f);
+  const V two23 = V::splat(8388608.0f);
   const V nhdt = V::splat((float)(-0.5 * tr.dt));
   // generation and bridge: warp-wide items over 32-path groups of the tile
   const int ngrp = Pb >> 5, lg_ngrp = lg_pb - 5;
@@ -489,17 +489,17 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
               // sigma at the step's time row, linear in log-spot.  u01 = the grid position scaled
               // to [0, 1], clamped by the FMA's saturation (NaN -> 0); 2^23 + floor(u01·(gx-1))
               // by one round-down FMA, whose bit pattern minus 0x4B000000 is the grid index —
-              // that bias is folded into the row offset lvo; then one (value, slope) gather
+              // that bias is folded into the row offset lvo; then one gather of the cell's line
+              // (c, d) in u01 and sigma = c + u01·d
               V u01;
 #pragma unroll
               for (int j = 0; j < PPT; ++j) u01.v[j] = __saturatef(fmaf(x[f].v[j], lvb[f], lva[f]));
               const V fl = V::fma_rd(u01, gxm1, two23);
-              const V w = V::fma(u01, gxm1, V::fma(fl, neg1, two23));
 #pragma unroll
               for (int j = 0; j < PPT; ++j) {
                 const uint32_t idx = lvo[f] + (uint32_t)tg + (uint32_t)__float_as_int(fl.v[j]);
                 const float2 r = __ldg(tb.lv_rows + idx);
-                sg.v[j] = fmaf(w.v[j], r.y, r.x);
+                sg.v[j] = fmaf(u01.v[j], r.y, r.x);
               }
             } else {
               sg = sig[f];

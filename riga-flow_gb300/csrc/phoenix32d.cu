@@ -187,15 +187,15 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
       for (int f = 0; f < N; ++f) {
         float sg;
         if (LV) {
-          // the saturating grid lookup of phoenix32.cu: u01 clamped by the FMA's saturation, the
-          // grid index from a round-down FMA's bit pattern (bias folded into c4.z), one gather
+          // the saturating grid lookup of the tiled kernel: u01 clamped by the FMA's saturation, the
+          // grid index from a round-down FMA's bit pattern (bias folded into c4.z), one gather of
+          // the cell's line (c, d) and sigma = c + u01·d
           const float4 c4 = lvc[f];
           const float u01 = __saturatef(fmaf(x[f], c4.y, c4.x));
           const float fl = __fmaf_rd(u01, gxm1, 8388608.0f);
-          const float w = fmaf(u01, gxm1, 8388608.0f - fl);
           const uint32_t idx = (uint32_t)__float_as_int(c4.z) + (uint32_t)tg + (uint32_t)__float_as_int(fl);
           const float2 r = __ldg(tb.lv_rows + idx);
-          sg = fmaf(w, r.y, r.x);
+          sg = fmaf(u01, r.y, r.x);
         } else {
           sg = sig[f];
         }

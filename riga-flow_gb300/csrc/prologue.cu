@@ -169,7 +169,7 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
 }
 
 // One CTA per (surface, step): the FP64 row sigma(step·dt, ·) of the surface, linear in tenor
-// (riga-market/src/lib.rs:345-364), stored as FP32 (value, slope to the next node).
+// (riga-market/src/lib.rs:345-364), stored as FP32 lines of its cells in the grid position.
 __global__ void lvrows_kernel(const double* __restrict__ lv_v, const int32_t* __restrict__ cell_off,
                               const int32_t* __restrict__ surf_asset, const int2* __restrict__ lv_ti,
                               const double* __restrict__ lv_tw, int T, int gx, float2* __restrict__ rows) {
@@ -180,10 +180,14 @@ __global__ void lvrows_kernel(const double* __restrict__ lv_v, const int32_t* __
   const double* v0 = lv_v + cell_off[sfc] + ti.x * gx;
   const double* v1 = lv_v + cell_off[sfc] + ti.y * gx;
   float2* out = rows + ((size_t)sfc * T + t) * gx;
+  // cell j as a line in the grid position u in [0, 1] (u·(gx - 1) = j at node j):
+  // v(u) = v_j + (u·(gx - 1) - j)·(v_{j+1} - v_j) = c_j + u·d_j, with d = 0 on the last node, so
+  // that a lookup is one FMA on the saturated position (flat beyond the grid)
   for (int j = threadIdx.x; j < gx; j += blockDim.x) {
     const double a = (1.0 - wt) * v0[j] + wt * v1[j];
     const double b = j + 1 < gx ? (1.0 - wt) * v0[j + 1] + wt * v1[j + 1] : a;
-    out[j] = make_float2((float)a, (float)(b - a));
+    const double d = (double)(gx - 1) * (b - a);
+    out[j] = make_float2((float)(a - (double)j * (b - a)), (float)d);
   }
 }
 
