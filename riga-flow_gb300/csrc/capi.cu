@@ -466,7 +466,7 @@ static Staged stage(Workspace& W, const rg_price_request* req, Prepared& P) {
       if (W.timing) W.timing->kernel_launches += 1;
     }
   }
-  launch_cholesky(S.scen, P.n_scen, P.n, W.stream);
+  launch_cholesky(S.scen, S.scen32, P.n_scen, P.n, W.stream);
   if (W.timing) W.timing->kernel_launches += 1;
   if (W.ev) cuda_check(cudaEventRecord(W.ev[2], W.stream), "event");
   return S;

@@ -384,6 +384,7 @@ void prepare(const rg_price_request* r, const rg_scenario* sc, int n_scen, Prepa
   tr.ki = t.knock_in_barrier;
   tr.coupon_f = (float)tr.coupon_rate;
   tr.strike_f = (float)tr.strike;
+  tr.neg_half_dt_f = (float)(-0.5 * tr.dt);
   tr.memory = t.memory_coupon ? 1 : 0;
   tr.gx = c.lv_grid_x > 0 ? c.lv_grid_x : 96;  // riga-market/src/lib.rs:28
   P.ln_ko = std::log(tr.call_barrier);

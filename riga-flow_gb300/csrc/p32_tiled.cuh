@@ -207,10 +207,9 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   const int gx = tr.gx;
   const V gxm1 = V::splat((float)(gx - 1));
   const V two23 = V::splat(8388608.0f);
-  const V nhdt = V::splat((float)(-0.5 * tr.dt));
+  const V nhdt = V::splat(tr.neg_half_dt_f);
   // generation and bridge: warp-wide items over 32-path groups of the tile
   const int ngrp = Pb >> 5, lg_ngrp = lg_pb - 5;
-  const int ncg = N * ngrp;  // chain groups (factor, path group)
   const int nwarp = (int)(blockDim.x >> 5), wid = tid >> 5;
 
   // scenario constants in registers: the Cholesky factor, drifts, flat vols and the per-asset
@@ -219,14 +218,13 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
   float lva[N], lvb[N], x0[N];
   uint32_t lvo[N];
   {
-    const DevScenario& sc = scen[ss];
     const DevScen32& s3 = scen32[ss];
     const float inv_gxm1 = 1.0f / (float)(gx - 1);
     int q = 0;
 #pragma unroll
     for (int a = 0; a < N; ++a)
 #pragma unroll
-      for (int b = 0; b <= a; ++b) Lf[q++] = V::splat((float)sc.L[a * N + b]);
+      for (int b = 0; b <= a; ++b) Lf[q++] = V::splat(s3.L[a * N + b]);
 #pragma unroll
     for (int f = 0; f < N; ++f) {
       mu[f] = V::splat(s3.mu_dt[f]);

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
   const int T = (int)tr.steps;
   const int gx = tr.gx;
   const float gxm1 = (float)(gx - 1);
-  const float nhdt = (float)(-0.5 * tr.dt);
+  const float nhdt = tr.neg_half_dt_f;
   // the grid holds a multiple of S warps: warp w serves scenario w % S, path groups w / S + k·(W / S)
   const int gw = blockIdx.x * P32D_WARPS + wib;
   const int nw = gridDim.x * P32D_WARPS;
@@ -66,13 +66,12 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
   }
   float Lf[N * (N + 1) / 2], mu[N], sig[N];
   {
-    const DevScenario& sc = scen[s];
     const DevScen32& s3 = scen32[s];
     int q = 0;
 #pragma unroll
     for (int a = 0; a < N; ++a)
 #pragma unroll
-      for (int b = 0; b <= a; ++b) Lf[q++] = (float)sc.L[a * N + b];
+      for (int b = 0; b <= a; ++b) Lf[q++] = s3.L[a * N + b];
 #pragma unroll
     for (int f = 0; f < N; ++f) {
       mu[f] = s3.mu_dt[f];

@@ -267,8 +267,9 @@ __device__ static void factor_correlation(double* src, int n, double* l, double*
     }
 }
 
-// One thread per scenario, in place on the scenario's correlation block.
-__global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int n) {
+// One thread per scenario, in place on the scenario's correlation block; the FP32 kernels' copy of
+// the factor (rounded once here) when scen32 is given, so their loops convert nothing from FP64.
+__global__ void cholesky_kernel(DevScenario* __restrict__ scen, DevScen32* __restrict__ scen32, int n_scen, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_scen) return;
   DevScenario& sc = scen[i];
@@ -276,6 +277,8 @@ __global__ void cholesky_kernel(DevScenario* __restrict__ scen, int n_scen, int 
   for (int k = 0; k < n * n; ++k) src[k] = sc.L[k];
   factor_correlation(src, n, l, eig);
   for (int k = 0; k < n * n; ++k) sc.L[k] = l[k];
+  if (scen32)
+    for (int k = 0; k < n * n; ++k) scen32[i].L[k] = (float)l[k];
   sc.status = 0;
 }
 
@@ -294,8 +297,8 @@ void launch_cholesky_big(const double* c, int n, double* l, double* work, cudaSt
   cuda_check(cudaGetLastError(), "cholesky_big_kernel launch");
 }
 
-void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s) {
-  cholesky_kernel<<<(n_scen + 63) / 64, 64, 0, s>>>(scen_dev, n_scen, n);
+void launch_cholesky(DevScenario* scen_dev, DevScen32* scen32_dev, int n_scen, int n, cudaStream_t s) {
+  cholesky_kernel<<<(n_scen + 63) / 64, 64, 0, s>>>(scen_dev, scen32_dev, n_scen, n);
   cuda_check(cudaGetLastError(), "cholesky_kernel launch");
 }
 

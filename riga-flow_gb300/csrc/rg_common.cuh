@@ -46,6 +46,7 @@ struct DevTrade {
   double init[RG_NMAX];
   double call_barrier, coupon_barrier, coupon_rate, strike, ki;
   float coupon_f, strike_f;  // coupon_rate and strike rounded to FP32 for the FP32 kernels
+  float neg_half_dt_f;       // -dt / 2 rounded to FP32 (the FP32 kernels' Euler drift term)
   int32_t memory;
 };
 
@@ -231,16 +232,6 @@ __device__ __forceinline__ float rg_ninv32_lower(float p2, float s) {
   return s * g;
 }
 
-// (float)x, rounded to nearest as a conversion instruction would, from FP32 adds and one FMA: each
-// 16-bit half is exact as the low mantissa bits of 2^23 minus 2^23, and hi·2^16 + lo rounds once.
-// (Integer-to-float conversions are not FP32-pipe work on this GPU; the generation loops convert
-// two 32-bit integers per normal.)
-__device__ __forceinline__ float rg_u32_to_f32(uint32_t x) {
-  const float hi = __int_as_float(0x4B000000u | (x >> 16)) - 8388608.0f;
-  const float lo = __int_as_float(0x4B000000u | (x & 0xFFFFu)) - 8388608.0f;
-  return fmaf(hi, 65536.0f, lo);
-}
-
 // The FP32 inverse normal of u = (x + 1/2) / 2^32: twice the lower-tail probability
 // p = min(u, 1 - u) and s = 1 - 2p formed from x or ~x (s from the integer distance to the centre,
 // exact for points near it), rg_ninv32_lower, and the sign by symmetry.  It tracks the exact inverse normal, so
@@ -248,8 +239,8 @@ __device__ __forceinline__ float rg_u32_to_f32(uint32_t x) {
 __device__ __forceinline__ float rg_probit32(uint32_t x) {
   const bool lower = x < 0x80000000u;
   const uint32_t xl = lower ? x : ~x;
-  const float p2 = fmaf(rg_u32_to_f32(xl), 4.656612873077393e-10f, 2.3283064365386963e-10f);
-  const float s = fmaf(rg_u32_to_f32(0x7FFFFFFFu - xl), 4.656612873077393e-10f, 2.3283064365386963e-10f);
+  const float p2 = fmaf((float)xl, 4.656612873077393e-10f, 2.3283064365386963e-10f);
+  const float s = fmaf((float)(0x7FFFFFFFu - xl), 4.656612873077393e-10f, 2.3283064365386963e-10f);
   const float q = rg_ninv32_lower(p2, s);
   return lower ? -q : q;
 }

@@ -84,6 +84,7 @@ struct DevScen32 {
   float a_u[RG_NMAX];     // (ln initial_spot - log_lo) / h
   float inv_h[RG_NMAX];   // 1 / h on the Dupire log-strike axis
   int32_t surf_off[RG_NMAX];  // first FP32 step row of the scenario's surface: surface·T·gx
+  float L[RG_NMAX * RG_NMAX]; // the scenario's Cholesky factor rounded to FP32 (written by cholesky_kernel)
 };
 
 // Everything one request needs on the device, after preparation.
@@ -224,7 +225,7 @@ struct SurfaceCache {
   void release();
 };
 void launch_calibrate(const CalibJob* jobs_dev, int n_jobs, cudaStream_t s);
-void launch_cholesky(DevScenario* scen_dev, int n_scen, int n, cudaStream_t s);
+void launch_cholesky(DevScenario* scen_dev, DevScen32* scen32_dev, int n_scen, int n, cudaStream_t s);
 // Per surface and step, the Dupire row interpolated to the step's time, as FP32 (v_j, v_j+1 - v_j).
 void launch_lvrows(const double* lv_v, const int32_t* surf_cell_off, const int32_t* surf_asset,
                    const int2* lv_ti, const double* lv_tw, int n_surf, int T, int gx, float2* rows,
