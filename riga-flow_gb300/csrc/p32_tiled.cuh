@@ -231,9 +231,7 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       sig[f] = V::splat(s3.sig[f]);
       lva[f] = s3.a_u[f] * inv_gxm1;
       lvb[f] = s3.inv_h[f] * inv_gxm1;
-      // cell j of step t is row (surf_off + j·T + t); the index is formed from the round-down
-      // FMA's bits 0x4B000000 + j as bits·T + (surf_off + t - 0x4B000000·T), wrapping in 32 bits
-      lvo[f] = (uint32_t)s3.surf_off[f] - 0x4B000000u * (uint32_t)T;
+      lvo[f] = (uint32_t)s3.surf_off[f] - 0x4B000000u;
       x0[f] = s3.x0[f];
     }
   }
@@ -464,7 +462,7 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
         // one Euler step of every asset (correlated increment, local-vol lookup, log-space update);
         // returns the worst-of log performance of each path after the step
         auto euler = [&](int tt, float (&wmin)[PPT]) {
-          const uint32_t tg = (uint32_t)(t0 + tt);
+          const int tg = (t0 + tt) * gx;
           V d[N], y[N];
 #pragma unroll
           for (int f = 0; f < N; ++f) {
@@ -490,15 +488,14 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
               // to [0, 1], clamped by the FMA's saturation (NaN -> 0); 2^23 + floor(u01·(gx-1))
               // by one round-down FMA, whose bit pattern minus 0x4B000000 is the grid index —
               // that bias is folded into the row offset lvo; then one gather of the cell's line
-              // (c, d) in u01 (cell-major rows: consecutive steps of a cell share a cache line)
-              // and sigma = c + u01·d
+              // (c, d) in u01 and sigma = c + u01·d
               V u01;
 #pragma unroll
               for (int j = 0; j < PPT; ++j) u01.v[j] = __saturatef(fmaf(x[f].v[j], lvb[f], lva[f]));
               const V fl = V::fma_rd(u01, gxm1, two23);
 #pragma unroll
               for (int j = 0; j < PPT; ++j) {
-                const uint32_t idx = (uint32_t)__float_as_int(fl.v[j]) * (uint32_t)T + (lvo[f] + tg);
+                const uint32_t idx = lvo[f] + (uint32_t)tg + (uint32_t)__float_as_int(fl.v[j]);
                 const float2 r = __ldg(tb.lv_rows + idx);
                 sg.v[j] = fmaf(u01.v[j], r.y, r.x);
               }

@@ -62,8 +62,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
     const int f = i % N;
     const float inv_gxm1 = 1.0f / (float)(tr.gx - 1);
     s_lv[i] = make_float4(s3.a_u[f] * inv_gxm1, s3.inv_h[f] * inv_gxm1,
-                          __int_as_float((int)((uint32_t)s3.surf_off[f] - 0x4B000000u * (uint32_t)tr.steps)),
-                          s3.x0[f]);
+                          __int_as_float((int)((uint32_t)s3.surf_off[f] - 0x4B000000u)), s3.x0[f]);
   }
   float Lf[N * (N + 1) / 2], mu[N], sig[N];
   {
@@ -173,7 +172,7 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
         d[f] = wn - wcur[f];
         wcur[f] = wn;
       }
-      const uint32_t tg = (uint32_t)t;
+      const int tg = t * gx;
       int q = 0;
 #pragma unroll
       for (int a = 0; a < N; ++a) {
@@ -189,11 +188,11 @@ __global__ void __launch_bounds__(P32D_THREADS, N <= 3 ? 4 : 3) phoenix32d_kerne
         if (LV) {
           // the saturating grid lookup of the tiled kernel: u01 clamped by the FMA's saturation, the
           // grid index from a round-down FMA's bit pattern (bias folded into c4.z), one gather of
-          // the cell's line (c, d) from the cell-major rows and sigma = c + u01·d
+          // the cell's line (c, d) and sigma = c + u01·d
           const float4 c4 = lvc[f];
           const float u01 = __saturatef(fmaf(x[f], c4.y, c4.x));
           const float fl = __fmaf_rd(u01, gxm1, 8388608.0f);
-          const uint32_t idx = (uint32_t)__float_as_int(fl) * (uint32_t)T + ((uint32_t)__float_as_int(c4.z) + tg);
+          const uint32_t idx = (uint32_t)__float_as_int(c4.z) + (uint32_t)tg + (uint32_t)__float_as_int(fl);
           const float2 r = __ldg(tb.lv_rows + idx);
           sg = fmaf(u01, r.y, r.x);
         } else {

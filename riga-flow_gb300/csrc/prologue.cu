@@ -179,9 +179,7 @@ __global__ void lvrows_kernel(const double* __restrict__ lv_v, const int32_t* __
   const double wt = lv_tw[f * T + t];
   const double* v0 = lv_v + cell_off[sfc] + ti.x * gx;
   const double* v1 = lv_v + cell_off[sfc] + ti.y * gx;
-  // cell-major within the surface, [cell j][step t], so that a path's lookups on consecutive steps
-  // in the same cell read one cache line
-  float2* out = rows + (size_t)sfc * T * gx + t;
+  float2* out = rows + ((size_t)sfc * T + t) * gx;
   // cell j as a line in the grid position u in [0, 1] (u·(gx - 1) = j at node j):
   // v(u) = v_j + (u·(gx - 1) - j)·(v_{j+1} - v_j) = c_j + u·d_j, with d = 0 on the last node, so
   // that a lookup is one FMA on the saturated position (flat beyond the grid)
@@ -189,7 +187,7 @@ __global__ void lvrows_kernel(const double* __restrict__ lv_v, const int32_t* __
     const double a = (1.0 - wt) * v0[j] + wt * v1[j];
     const double b = j + 1 < gx ? (1.0 - wt) * v0[j + 1] + wt * v1[j + 1] : a;
     const double d = (double)(gx - 1) * (b - a);
-    out[(size_t)j * T] = make_float2((float)(a - (double)j * (b - a)), (float)d);
+    out[j] = make_float2((float)(a - (double)j * (b - a)), (float)d);
   }
 }
 

@@ -79,8 +79,8 @@ struct DevTables {
   const float* lv_twf;         // [n][T] tenor weight in FP32
   const double* lv_v;          // [surfaces][n_t][gx] FP64 local vol
   const float2* lv_vf;         // [surfaces][n_t][gx] (v, v[j+1]-v[j]) FP32
-  const float2* lv_rows;       // [surfaces][gx][T] the row at each step's time, cell-major: cell j's
-                               // line (c, d) in the grid position u in [0, 1], v = c + u·d, FP32
+  const float2* lv_rows;       // [surfaces][T][gx] the row at each step's time: cell j's line (c, d) in
+                               // the grid position u in [0, 1], v = c + u·d, FP32
   const double* lv_logs;       // [surfaces][gx] log-strike axis
   const double* df;            // [scenarios][T] exp(-r_s * (t+1) dt)
   const double* df_mat;        // [scenarios] exp(-r_s * maturity)
