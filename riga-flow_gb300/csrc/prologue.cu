@@ -128,7 +128,7 @@ __global__ void calibrate_kernel(const CalibJob* __restrict__ jobs) {
   const double* T = J.mats;
   const double lo2 = 0.10 * 0.10, hi2 = 3.00 * 3.00;  // LV_CLAMP_LO/HI, lib.rs:30-32
   for (int c = threadIdx.x; c < nt * gx; c += blockDim.x) {
-    int k = c / gx;
+    int k = c / gx, i = c % gx;
     double dw;
     if (nt == 1) {
       dw = w[i] / (T[0] > 1e-9 ? T[0] : 1e-9);
