@@ -100,7 +100,7 @@ static const DeviceInfo& device_info() {
     info.sm_count = p.multiProcessorCount;
     if (!(p.major == 10 && p.minor == 3)) {
       info.status = RG_ERR_GPU_UNAVAILABLE;
-      info.message = "this build holds sm_103a code only; device 0 is " + info.arch;
+      info.message = "the library holds sm_103a code only; device 0 is " + info.arch;
     }
   });
   return info;
@@ -1011,7 +1011,7 @@ extern "C" int32_t rg_phase_clocks(uint64_t out[4], int32_t reset) {
     if (!out) raise(RG_ERR_INVALID_ARGUMENT, "null argument");
     unsigned long long v[4];
     if (!p32_phase_clocks(v, reset != 0))
-      raise(RG_ERR_UNSUPPORTED, "this build has no phase clocks (build with RG_PHASE_CLOCKS=1)");
+      raise(RG_ERR_UNSUPPORTED, "the library was built without phase clocks (build it with RG_PHASE_CLOCKS=1)");
     for (int k = 0; k < 4; ++k) out[k] = v[k];
   })
 }
