@@ -323,9 +323,10 @@ __global__ void __launch_bounds__(PPT == 1 ? 1024 : 512, 1) phoenix32_kernel(
       }
       {
         // kGB items per warp at a time in straight-line code, so that their global loads, shuffles
-        // and inverse normals overlap; a warp's surplus slots recompute its last item (the same
-        // values stored twice), and items of paths past the request compute values nobody reads
-        constexpr int kGB = 4;
+        // and inverse normals overlap (three: four spilled registers, measured 0.7% slower); a
+        // warp's surplus slots recompute its last item (the same values stored twice), and items
+        // of paths past the request compute values nobody reads
+        constexpr int kGB = 3;
         const int nitems = nn << lg_ngrp;
         const bool shift_lane = tr.vr == RG_VR_SOBOL && tr.scrambler == RG_SCRAMBLE_DIGITAL_SHIFT;
         for (int base = wid; base < nitems; base += kGB * nwarp) {
