@@ -288,7 +288,10 @@ Job* next_job(rg_server* S, int k, std::vector<int>& trim) {
         const Slot& s = S->slots[i];
         other = other || ((int)i != k && !s.trimming && !s.busy_large && holds(s));
       }
-      if (other) continue;  // left to that slot's worker
+      if (other) {  // left to that slot's worker; nothing larger than small requests passes it
+        waiting = true;
+        continue;
+      }
     }
     if (admit(S, k, j, trim)) return j;
     if (!j->waited_memory) {
